@@ -1,0 +1,359 @@
+#!/usr/bin/env python3
+"""Benchmark: exact k-NN queries/s on one GB300 (N=1,000,000 points, d=3, k=16,
+L2, leafsize 16, 1,000,000 queries per step; uniform [0,1)^3, data seed 2,
+queries seed 3).
+
+A step is one pass of the query hot path over one batch of 1,000,000 queries.
+
+  value   queries/s with queries, tree and outputs resident in HBM: the C-ABI
+          kd_query_device call timed with CUDA events on the stream it runs on,
+          L2 flushed (a 256 MiB write) before every timed step.
+  e2e     the same metric through the C-ABI kd_query with HOST buffers (pinned):
+          the 24 MB query upload and the 256 MB (distances + indices) download
+          are inside the timed region.
+  roofline  algorithmic bytes per launch of the query kernel (per-query node,
+          leaf-row and box counts from the oracle's instrumented descent on the
+          identical inputs) / its event-timed duration, against the measured
+          HBM copy bandwidth.
+  cpu_baseline  the oracle (a C restatement of the reference's build + query,
+          OpenMP over all host cores) on the same workload.
+
+`--impl reference` times the reference's CPU algorithm (the oracle port: the
+Rust crate cannot be built without a Rust toolchain) on the same config.
+
+Under torchrun (N > 1) every rank holds a replica of the tree and queries its
+own 1,000,000-query batch (weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "kdtree-rs_gb300"))
+
+N_POINTS = 1_000_000
+N_QUERIES = 1_000_000
+DIM = 3
+K = 16
+P = 2.0
+LEAFSIZE = 16
+METRIC = "exact kNN queries/s (N=1M, d=3, k=16, L2)"
+WORKLOAD = "plain-scale uniform N=1,000,000 d=3 leafsize=16, 1,000,000 queries/step, k=16, p=2"
+
+
+def workload(rank: int = 0):
+    data = np.random.default_rng(2).uniform(size=(N_POINTS, DIM))
+    q = np.random.default_rng(3 + 1000 * rank).uniform(size=(N_QUERIES, DIM))
+    return data, q
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        if self.path and os.path.exists(self.path):
+            for line in open(self.path):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(data, q, threads, reps=3):
+    """The oracle on the same workload, all host threads (query) -> q/s."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import kdtree_oracle
+
+    t0 = time.perf_counter()
+    t = kdtree_oracle.OracleKDTree(data, leafsize=LEAFSIZE, parallel=True)
+    build_s = time.perf_counter() - t0
+    best = None
+    counts = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        t.query(q, k=K, p=P, threads=threads)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+        counts = t.last_counts
+    return {"qps": len(q) / best, "build_s": build_s, "counts": counts, "tree": t}
+
+
+def algorithmic_bytes(counts, n_queries):
+    """Per-query B_q = 8d + 16k + 8d*S_q + 24*V_q + 16d*X_q summed over the batch
+    (V = nodes visited, S = leaf rows scanned, X = boxes evaluated)."""
+    visits, scanned, boxes = counts
+    return 8 * DIM * n_queries + 16 * K * n_queries + 8 * DIM * scanned + 24 * visits + 16 * DIM * boxes
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        j = json.loads(p.read_text())
+        return float(j["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    p = ROOT / "profiles" / "roofline_traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text()).get("query_kernel_dram_bytes_per_launch")
+        except Exception:
+            return None
+    return None
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import kdtree_oracle
+
+    threads = kdtree_oracle.max_threads()
+    data, q = workload(0)
+    t = kdtree_oracle.OracleKDTree(data, leafsize=LEAFSIZE, parallel=True)
+    sample = q[:200_000]
+    for _ in range(args.warmup):
+        t.query(sample, k=K, p=P, threads=threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        t.query(sample, k=K, p=P, threads=threads)
+        times.append(time.perf_counter() - t0)
+    qps = len(sample) * len(times) / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (numpy default_rng seeds 2 / 3)",
+        "config": {"workload": WORKLOAD, "sample_queries_per_step": len(sample)},
+        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+                         "sample": f"{len(sample)} of the 1,000,000 queries per step (first rows), "
+                                   "oracle restatement of the reference (Rust crate not buildable here)"},
+        "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from kdtree import KDTree
+    from kdtree import _core
+
+    lib = _core._lib
+    data, q = workload(rank)
+
+    # build (GPU), timed on the host around the synchronous call
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tree = KDTree(data, leafsize=LEAFSIZE)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    tree = KDTree(data, leafsize=LEAFSIZE)
+    build_s = min(build_s, time.perf_counter() - t0)
+
+    dev = torch.device("cuda", local)
+    dq = torch.from_numpy(q).to(dev)
+    dd = torch.empty((N_QUERIES, K), dtype=torch.float64, device=dev)
+    di = torch.empty((N_QUERIES, K), dtype=torch.int64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+
+    def step():
+        st = lib.kd_query_device(tree._h, ctypes.c_void_p(dq.data_ptr()), dq.numel(), K, P, 0, 0.0, 0.0,
+                                 ctypes.c_void_p(dd.data_ptr()), ctypes.c_void_p(di.data_ptr()),
+                                 ctypes.c_void_p(stream.cuda_stream))
+        if st:
+            raise RuntimeError(f"kd_query_device failed: {st} {_core._last_error()}")
+
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            flush.zero_()
+            step()
+    torch.cuda.synchronize()
+
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    sampler = ClockSampler(local)
+    with sampler:
+        t_wall0 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            for e0, e1 in events:
+                flush.zero_()
+                e0.record(stream)
+                step()
+                e1.record(stream)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall0
+    if ws > 1:
+        dist.barrier()
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in events]
+    total_s = sum(step_ms) / 1e3
+    if ws > 1:
+        tt = torch.tensor([total_s], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_s = float(tt.item())
+    value = ws * N_QUERIES * args.steps / total_s
+    clocks = sampler.summary()
+
+    # end to end through the C ABI with pinned host buffers
+    hq = torch.from_numpy(q).pin_memory()
+    hd = torch.empty((N_QUERIES, K), dtype=torch.float64).pin_memory()
+    hi = torch.empty((N_QUERIES, K), dtype=torch.int64).pin_memory()
+
+    def e2e_step():
+        st = lib.kd_query(tree._h, ctypes.c_void_p(hq.data_ptr()), hq.numel(), K, P, 0, 0.0, 0.0, 0,
+                          ctypes.c_void_p(hd.data_ptr()), ctypes.c_void_p(hi.data_ptr()))
+        if st:
+            raise RuntimeError(f"kd_query failed: {st} {_core._last_error()}")
+
+    for _ in range(max(args.warmup, 3)):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_times)
+    if ws > 1:
+        tt = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e_value = ws * N_QUERIES * args.steps / e2e_s
+
+    if rank != 0:
+        if ws > 1:
+            dist.destroy_process_group()
+        return 0
+
+    # CPU baseline (rank 0, N=1 only) and the per-query work counts
+    cpu = None
+    counts = None
+    if not args.no_cpu and ws == 1:
+        import kdtree_oracle
+
+        threads = kdtree_oracle.max_threads()
+        cpu = cpu_baseline(data, q, threads)
+        counts = cpu["counts"]
+    peak, peak_kind = measured_peak()
+    roofline = None
+    if counts:
+        per_launch = algorithmic_bytes(counts, N_QUERIES)
+        mean_s = total_s / args.steps
+        achieved = per_launch / mean_s / 1e9
+        traffic = profiled_traffic()
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                    "traffic": traffic, "peak_kind": peak_kind,
+                    "algorithmic_bytes_per_launch": per_launch,
+                    "per_query": {"nodes_visited": counts[0] / N_QUERIES, "rows_scanned": counts[1] / N_QUERIES,
+                                  "boxes_evaluated": counts[2] / N_QUERIES},
+                    "kernel": "k_query<L2, d=3, K=16>"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (numpy default_rng: data seed 2, queries seed 3)",
+        "config": {"workload": WORKLOAD, "n_points": N_POINTS, "queries_per_step": N_QUERIES, "d": DIM, "k": K,
+                   "p": P, "leafsize": LEAFSIZE, "l2": "flushed (256 MiB write) before every timed step",
+                   "parallelism": f"replicas x{ws}"},
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+        "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),
+                "d2h_bytes_per_step": int(N_QUERIES * K * 16)},
+        "roofline": roofline,
+        "build": {"gpu_s": build_s, "cpu_oracle_s": cpu["build_s"] if cpu else None,
+                  "note": "host wall time of kd_build incl. the 24 MB upload; oracle build on all host cores"},
+        "cpu_baseline": None if cpu is None else {
+            "value": cpu["qps"], "unit": "queries/s", "cores": kdtree_oracle.max_threads(), "kind": "port",
+            "sample": "the full 1,000,000-query step, best of 3 runs (oracle restatement of the reference)"},
+        "wall_s_timed_region": t_wall,
+    }
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,126 @@
+/*
+ * kdtree_gb300.h -- C ABI of the GB300 kd-tree engine (libkdtree_gb300.so).
+ *
+ * This is the drop-in boundary for FujishigeTemma/kdtree-rs's hot path: the
+ * median-split build and the pruned exact k-NN query.  Each entry point names
+ * the reference interface it replaces.  Plain pointers and sizes only; no CUDA
+ * or torch types (a CUDA stream is passed as `void*`).
+ *
+ * Conventions
+ *  - Every function returning `int` returns a KD_* status; KD_OK is 0.  The
+ *    message of the last failure on the calling thread is read with
+ *    kd_last_error() and matches the reference's `KDTreeError` Display text
+ *    (src/error.rs:18-51) for the statuses that mirror it.
+ *  - Arrays are row-major.  A point set is `n_values = n_points * ndim`
+ *    doubles, as the reference's `&[f64]` slices are (src/tree.rs:39-46,
+ *    src/query.rs:29-37).
+ *  - A tree is immutable once built; concurrent queries on one tree from many
+ *    host threads are safe (each call owns its scratch and stream work).
+ *  - `parallel` is accepted for API parity and has no effect: the GPU path
+ *    computes the same result either way, as the reference's serial and rayon
+ *    paths do (src/build.rs:345-359).
+ */
+#ifndef KDTREE_GB300_H
+#define KDTREE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  1..10 map 1:1 to the reference's KDTreeError variants
+ * (src/error.rs:3-16); 11 is the boundary's DimensionMismatch; 100+ are
+ * device-side failures the reference has no counterpart for. */
+enum kd_status {
+  KD_OK = 0,
+  KD_ERR_EMPTY_DATA = 1,            /* KDTreeError::EmptyData */
+  KD_ERR_INVALID_LEAFSIZE = 2,      /* KDTreeError::InvalidLeafsize */
+  KD_ERR_INVALID_K = 3,             /* KDTreeError::InvalidK */
+  KD_ERR_INVALID_METRIC = 4,        /* KDTreeError::InvalidMetric(p) */
+  KD_ERR_INVALID_EPS = 5,           /* KDTreeError::InvalidEps(eps) */
+  KD_ERR_INVALID_MAX_DISTANCE = 6,  /* KDTreeError::InvalidMaxDistance(d) */
+  KD_ERR_NONFINITE_DATA = 7,        /* KDTreeError::NonFiniteData */
+  KD_ERR_TOO_MANY_POINTS = 8,       /* KDTreeError::TooManyPoints(n) */
+  KD_ERR_TOO_MANY_NODES = 9,        /* KDTreeError::TooManyNodes(n) */
+  KD_ERR_INVALID_SHAPE = 10,        /* KDTreeError::InvalidShape(msg) */
+  KD_ERR_DIMENSION_MISMATCH = 11,   /* KDTreeError::DimensionMismatch */
+  KD_ERR_CUDA = 100,                /* a CUDA runtime call failed */
+  KD_ERR_OUT_OF_MEMORY = 101,       /* device or host allocation failed */
+  KD_ERR_INVALID_ARGUMENT = 102,    /* NULL pointer or unusable argument */
+  KD_ERR_NO_DEVICE = 103            /* no CUDA device is visible */
+};
+
+typedef struct kd_tree kd_tree;
+
+/* Build a tree from host data.  Replaces `Tree::new(data, ndim, leafsize,
+ * parallel)` (src/tree.rs:39-46 -> src/build.rs:19-82): the same validation
+ * order, and a layout (row order, indices, nodes, boxes) bit-identical to the
+ * reference's.  The data is copied; the caller keeps ownership of `data`. */
+int kd_build(const double* data, uint64_t n_values, uint64_t ndim, uint64_t leafsize,
+             int parallel, kd_tree** out);
+
+/* Same as kd_build with `d_data` already in device memory (it is read, not
+ * modified), the build work ordered on `stream` (NULL = the legacy default
+ * stream).  Returns once the tree is complete. */
+int kd_build_device(const double* d_data, uint64_t n_values, uint64_t ndim, uint64_t leafsize,
+                    void* stream, kd_tree** out);
+
+/* Release a tree and its device memory.  NULL is ignored. */
+void kd_free(kd_tree* tree);
+
+/* Exact k-NN query from host buffers.  Replaces `Tree::query(queries, k, p,
+ * max_distance, eps, parallel)` (src/query.rs:29-78): same validation order
+ * and messages, same (distance, index) results and tie order.  `out_distances`
+ * and `out_indices` hold n_queries * k values; slots without a neighbour are
+ * (+inf, n_points).  `has_max_distance` = 0 is the reference's `None`. */
+int kd_query(const kd_tree* tree, const double* queries, uint64_t n_values, uint64_t k, double p,
+             int has_max_distance, double max_distance, double eps, int parallel,
+             double* out_distances, int64_t* out_indices);
+
+/* Same as kd_query with queries and outputs in device memory, the work ordered
+ * on `stream`.  Returns after the stream work of this call has finished (the
+ * finiteness check of the queries is read back before returning). */
+int kd_query_device(const kd_tree* tree, const double* d_queries, uint64_t n_values, uint64_t k,
+                    double p, int has_max_distance, double max_distance, double eps,
+                    double* d_out_distances, int64_t* d_out_indices, void* stream);
+
+/* Getters: `Tree::ndim`, `Tree::n_points`, `Tree::leafsize`
+ * (src/tree.rs:48-58).  kd_n_nodes has no Python getter in the reference. */
+uint64_t kd_ndim(const kd_tree* tree);
+uint64_t kd_n_points(const kd_tree* tree);
+uint64_t kd_leafsize(const kd_tree* tree);
+uint64_t kd_n_nodes(const kd_tree* tree);
+
+/* Copy the points back in the caller's original row order into host memory
+ * (n_points * ndim doubles).  Replaces `Tree::original_data`
+ * (src/tree.rs:60-68). */
+int kd_original_data(const kd_tree* tree, double* out);
+
+/* Export the tree layout into host memory for inspection and parity tests
+ * (any pointer may be NULL to skip that array).  Mirrors the reference's
+ * `Tree` fields (src/tree.rs:29-36):
+ *   data       n_points * ndim doubles, tree (leaf-contiguous) row order
+ *   indices    n_points u32, tree position -> original row
+ *   node_words n_nodes * 4 u32: {is_leaf, left|start, right|end,
+ *              split_dim | order_by_box << 31}
+ *   split      n_nodes doubles (split_value; 0 for leaves)
+ *   boxes      n_nodes * 2 * ndim doubles, [lo | hi] per node. */
+int kd_export(const kd_tree* tree, double* data, uint32_t* indices, uint32_t* node_words,
+              double* split, double* boxes);
+
+/* Copy the calling thread's last error message (NUL-terminated, truncated to
+ * `len`) and return its full length.  The Rust reference surfaces the same
+ * text through `KDTreeError`'s Display (src/error.rs:18-51). */
+size_t kd_last_error(char* buf, size_t len);
+
+/* Number of nodes `count_nodes(n_points, leafsize)` (src/build.rs:166-173)
+ * a tree of this size has; lets callers size kd_export buffers up front. */
+uint64_t kd_count_nodes(uint64_t n_points, uint64_t leafsize);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KDTREE_GB300_H */

@@ -1,0 +1,1045 @@
+// kd_build.cu -- GPU median-split kd-tree build, level by level.
+//
+// Restates src/build.rs:19-314 of FujishigeTemma/kdtree-rs as per-level
+// segmented kernels.  The reference recurses depth-first; because the split is
+// always at len / 2 (build.rs:162-164) the tree's shape is a pure function of
+// (n_points, leafsize), so every node of one depth can be processed at once:
+//
+//   level L segments = the nodes at depth L, each a contiguous row range.
+//   per level:  bbox (min / max per dim, build.rs:175-181, kernel.rs:93-151)
+//            -> split_dim = widest axis (layout.rs:168-179)
+//            -> pivot = mid-th key under f64::total_cmp (build.rs:199-205),
+//               by a segmented 8-bit radix select over total-order keys
+//            -> lt = #{key < pivot} (build.rs:209)
+//            -> the exact row permutation of partition_rows (build.rs:266-314)
+//            -> node records and the next level's segments.
+//
+// The permutation: with R = ascending positions in [0, lt) holding key >= pivot
+// and L = ascending positions in [lt, len) holding key < pivot (|R| = |L| = n),
+// the reference swaps R[i] <-> L[n-1-i].  Listing the 2n misplaced positions in
+// ascending order as P[0..2n) (R then L), that swap sends P[r] to P[2n-1-r]: a
+// reversal of the misplaced list, computed from one segmented prefix sum.  The
+// pivot-equal fix-up (build.rs:303-313) is a Lomuto compaction of the first
+// m = mid - lt pivot-equal rows of [lt, len) into [lt, mid); with E[t] the t-th
+// such row, the row at place lt+t moves to E[t], so a displaced row's final
+// position is the end of the chain pos -> E[pos - lt] while pos - lt < m --
+// evaluated sequentially in shared memory for small segments and by pointer
+// jumping for large ones.  Only data with duplicated split coordinates takes it.
+//
+// Segments up to SMALL_MAX rows are processed entirely by one CTA in shared
+// memory; larger ones (the top levels) by grids of CTAs over row chunks with
+// global histograms, counts and scans.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "kd_internal.hpp"
+
+namespace kd {
+
+namespace {
+
+constexpr uint32_t HOLE = 0xffffffffu;
+constexpr uint32_t NONE = 0xffffffffu;
+constexpr int SMALL_MAX = 8192;  // rows a single CTA partitions in shared memory
+constexpr int SMALL_THREADS = 512;
+constexpr int LG_THREADS = 256;
+constexpr int LG_ITEMS = 8;
+constexpr int LG_CHUNK = LG_THREADS * LG_ITEMS;  // rows per CTA in the large path
+constexpr int RADIX_PASSES = 8;
+constexpr uint64_t KEY_MAX = ~0ull;
+
+// IEEE comparison key: total order with -0 folded onto +0, so that integer
+// '<' and '==' on it are f64 '<' and '==' for finite values
+// (partition_rows compares with '<', '>=', '==', not total_cmp).
+__device__ __forceinline__ uint64_t canon(uint64_t k) {
+  return k == 0x7fffffffffffffffull ? 0x8000000000000000ull : k;
+}
+
+// count_nodes (src/build.rs:166-173), level by level over the at most two
+// distinct sizes of one depth (same result as the reference's recursion).
+__host__ __device__ uint64_t count_nodes_impl(uint64_t len, uint64_t leafsize) {
+  uint64_t sz[4] = {len, 0, 0, 0}, cnt[4] = {1, 0, 0, 0};
+  int n = 1;
+  uint64_t total = 0;
+  while (n > 0) {
+    uint64_t nsz[8], ncnt[8];
+    int nn = 0;
+    for (int i = 0; i < n; ++i) {
+      total += cnt[i];
+      if (sz[i] <= leafsize) continue;
+      uint64_t halves[2] = {sz[i] / 2, sz[i] - sz[i] / 2};
+      for (int h = 0; h < 2; ++h) {
+        int j = 0;
+        while (j < nn && nsz[j] != halves[h]) ++j;
+        if (j == nn) {
+          nsz[nn] = halves[h];
+          ncnt[nn] = 0;
+          ++nn;
+        }
+        ncnt[j] += cnt[i];
+      }
+    }
+    for (int i = 0; i < nn; ++i) {
+      sz[i] = nsz[i];
+      cnt[i] = ncnt[i];
+    }
+    n = nn;
+  }
+  return total;
+}
+
+// widest_axis (src/layout.rs:168-179) on a box held as total-order keys.
+__device__ uint32_t widest_axis_keys(const uint64_t* box, uint64_t d) {
+  uint32_t best = 0;
+  double span = dsub(from_total_key(box[d]), from_total_key(box[0]));
+  for (uint64_t j = 1; j < d; ++j) {
+    double s = dsub(from_total_key(box[d + j]), from_total_key(box[j]));
+    if (s > span) {
+      span = s;
+      best = static_cast<uint32_t>(j);
+    }
+  }
+  return best;
+}
+
+struct Level {
+  const double* din;
+  double* dout;
+  const uint32_t* iin;
+  uint32_t* iout;
+  uint64_t d;
+  uint64_t leafsize;
+  // current level's segments (slot-indexed; HOLE marks an absent node)
+  const uint32_t* seg_node;
+  const uint32_t* seg_start;
+  const uint32_t* seg_len;
+  // next level's segments: children of slot s go to slots 2s and 2s+1
+  uint32_t* nseg_node;
+  uint32_t* nseg_start;
+  uint32_t* nseg_len;
+  DNode* nodes;
+  uint64_t* boxkeys;  // n_nodes * 2d total-order keys during the build
+  uint32_t* node_len;
+  uint64_t n_slots;
+};
+
+__device__ __forceinline__ void write_leaf(DNode* nodes, uint32_t node, uint32_t start, uint32_t len) {
+  DNode nd;
+  nd.split = bitsd(static_cast<uint64_t>(start) | (static_cast<uint64_t>(start + len) << 32));
+  nd.right = 0;
+  nd.meta = KD_NODE_LEAF;
+  nodes[node] = nd;
+}
+
+// Record an inner node and open its two children in the next level (their box
+// keys start at the identities of min / max for the bbox atomics).
+__device__ void expand_inner(const Level& L, uint64_t slot, uint32_t node, uint32_t start, uint32_t len,
+                             uint32_t dim, uint64_t pivot_key) {
+  uint32_t mid = len / 2;
+  uint32_t right = node + 1 + static_cast<uint32_t>(count_nodes_impl(mid, L.leafsize));
+  DNode nd;
+  nd.split = from_total_key(pivot_key);
+  nd.right = right;
+  nd.meta = dim;
+  L.nodes[node] = nd;
+  L.node_len[node] = len;
+  L.nseg_node[2 * slot] = node + 1;
+  L.nseg_start[2 * slot] = start;
+  L.nseg_len[2 * slot] = mid;
+  L.nseg_node[2 * slot + 1] = right;
+  L.nseg_start[2 * slot + 1] = start + mid;
+  L.nseg_len[2 * slot + 1] = len - mid;
+}
+
+__device__ void close_leaf(const Level& L, uint64_t slot, uint32_t node, uint32_t start, uint32_t len) {
+  write_leaf(L.nodes, node, start, len);
+  L.node_len[node] = len;
+  L.nseg_node[2 * slot] = HOLE;
+  L.nseg_node[2 * slot + 1] = HOLE;
+  L.nseg_len[2 * slot] = 0;
+  L.nseg_len[2 * slot + 1] = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Bounding boxes: per (segment, chunk) CTA, min / max per dim as total-order
+// keys, merged into the node's box with 64-bit atomics.  The block size is a
+// multiple of d (d <= 256) so each thread's dimension is fixed and it reduces in
+// registers.  Level 0 also checks finiteness (all_finite, kernel.rs:67-74).
+// ---------------------------------------------------------------------------
+__global__ void k_init_boxkeys(uint64_t* boxkeys, uint64_t n_nodes, uint64_t d) {
+  uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  uint64_t total = n_nodes * 2 * d;
+  if (i < total) boxkeys[i] = ((i / d) & 1) ? 0ull : KEY_MAX;
+}
+
+__global__ void k_bbox(Level L, uint32_t chunk_rows, uint32_t n_chunks, int check_finite, uint32_t* status) {
+  extern __shared__ uint64_t sbox[];  // [lo d | hi d]
+  const uint64_t slot = blockIdx.x;
+  const uint32_t node = L.seg_node[slot];
+  if (node == HOLE) return;
+  const uint32_t start = L.seg_start[slot], len = L.seg_len[slot];
+  if (static_cast<uint64_t>(blockIdx.y) * chunk_rows >= len) return;
+  const uint64_t d = L.d;
+  for (uint64_t j = threadIdx.x; j < d; j += blockDim.x) {
+    sbox[j] = KEY_MAX;
+    sbox[d + j] = 0;
+  }
+  __syncthreads();
+  bool bad = false;
+  uint64_t lo = KEY_MAX, hi = 0;
+  for (uint32_t c = blockIdx.y; c < n_chunks; c += gridDim.y) {
+    const uint64_t r0 = static_cast<uint64_t>(c) * chunk_rows;
+    if (r0 >= len) break;
+    const uint64_t r1 = min(static_cast<uint64_t>(len), r0 + chunk_rows);
+    const double* base = L.din + (static_cast<uint64_t>(start) + r0) * d;
+    const uint64_t n_el = (r1 - r0) * d;
+    if (d <= 256) {
+      // blockDim.x is a multiple of d: the thread's dimension is fixed.
+      for (uint64_t f = threadIdx.x; f < n_el; f += blockDim.x) {
+        double v = base[f];
+        bad |= !isfinite(v);
+        uint64_t k = total_key(v);
+        lo = k < lo ? k : lo;
+        hi = k > hi ? k : hi;
+      }
+    } else {
+      for (uint64_t f = threadIdx.x; f < n_el; f += blockDim.x) {
+        double v = base[f];
+        bad |= !isfinite(v);
+        uint64_t k = total_key(v);
+        uint64_t j = f % d;
+        atomicMin(reinterpret_cast<unsigned long long*>(&sbox[j]), k);
+        atomicMax(reinterpret_cast<unsigned long long*>(&sbox[d + j]), k);
+      }
+    }
+  }
+  if (d <= 256) {
+    const uint32_t j = threadIdx.x % d;
+    atomicMin(reinterpret_cast<unsigned long long*>(&sbox[j]), lo);
+    atomicMax(reinterpret_cast<unsigned long long*>(&sbox[d + j]), hi);
+  }
+  if (check_finite && bad) atomicOr(status, 1u);
+  __syncthreads();
+  uint64_t* gbox = L.boxkeys + static_cast<uint64_t>(node) * 2 * d;
+  for (uint64_t j = threadIdx.x; j < d; j += blockDim.x) {
+    atomicMin(reinterpret_cast<unsigned long long*>(&gbox[j]), sbox[j]);
+    atomicMax(reinterpret_cast<unsigned long long*>(&gbox[d + j]), sbox[d + j]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Block-wide helpers.
+// ---------------------------------------------------------------------------
+template <int THREADS>
+__device__ uint32_t block_excl_scan(uint32_t v, uint32_t* total, uint32_t* sh_warp) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < THREADS / 32 ? sh_warp[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < THREADS / 32) sh_warp[lane] = w;
+  }
+  __syncthreads();
+  uint32_t warp_off = warp ? sh_warp[warp - 1] : 0;
+  *total = sh_warp[THREADS / 32 - 1];
+  __syncthreads();
+  return warp_off + x - v;
+}
+
+template <int THREADS>
+__device__ uint32_t block_sum(uint32_t v, uint32_t* sh_warp) {
+  uint32_t total;
+  block_excl_scan<THREADS>(v, &total, sh_warp);
+  return total;
+}
+
+// ---------------------------------------------------------------------------
+// Small path: one CTA per segment of at most SMALL_MAX rows, in shared memory.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(SMALL_THREADS) k_small_level(Level L) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint64_t* keys = reinterpret_cast<uint64_t*>(smem);              // SMALL_MAX
+  uint16_t* cur = reinterpret_cast<uint16_t*>(keys + SMALL_MAX);    // SMALL_MAX
+  uint16_t* plist = cur + SMALL_MAX;                                // SMALL_MAX
+  __shared__ uint32_t sh_warp[SMALL_THREADS / 32];
+  __shared__ uint32_t hist[256];
+  __shared__ uint64_t s_pivot;
+  __shared__ uint32_t s_dim, s_rank;
+  __shared__ uint64_t s_prefix;
+
+  const uint64_t slot = blockIdx.x;
+  const uint32_t node = L.seg_node[slot];
+  if (node == HOLE) {
+    if (threadIdx.x == 0) {
+      L.nseg_node[2 * slot] = HOLE;
+      L.nseg_node[2 * slot + 1] = HOLE;
+      L.nseg_len[2 * slot] = 0;
+      L.nseg_len[2 * slot + 1] = 0;
+    }
+    return;
+  }
+  const uint32_t start = L.seg_start[slot], len = L.seg_len[slot];
+  const uint64_t d = L.d;
+  const double* din = L.din + static_cast<uint64_t>(start) * d;
+  double* dout = L.dout + static_cast<uint64_t>(start) * d;
+  const uint32_t* iin = L.iin + start;
+  uint32_t* iout = L.iout + start;
+
+  if (len <= L.leafsize) {  // a leaf at this depth: rows stay where they are
+    for (uint64_t f = threadIdx.x; f < static_cast<uint64_t>(len) * d; f += SMALL_THREADS) dout[f] = din[f];
+    for (uint32_t i = threadIdx.x; i < len; i += SMALL_THREADS) iout[i] = iin[i];
+    if (threadIdx.x == 0) close_leaf(L, slot, node, start, len);
+    return;
+  }
+
+  if (threadIdx.x == 0) s_dim = widest_axis_keys(L.boxkeys + static_cast<uint64_t>(node) * 2 * d, d);
+  __syncthreads();
+  const uint32_t dim = s_dim;
+  const uint32_t mid = len / 2;
+  for (uint32_t i = threadIdx.x; i < len; i += SMALL_THREADS) keys[i] = total_key(din[i * d + dim]);
+  __syncthreads();
+
+  // pivot = the mid-th smallest key under total order (select_nth_unstable_by)
+  if (len <= SMALL_THREADS) {
+    if (threadIdx.x < len) {
+      const uint64_t ki = keys[threadIdx.x];
+      uint32_t cl = 0, ce = 0;
+      for (uint32_t j = 0; j < len; ++j) {
+        uint64_t kj = keys[j];
+        cl += kj < ki;
+        ce += kj == ki;
+      }
+      if (cl <= mid && mid < cl + ce) s_pivot = ki;  // all writers agree
+    }
+  } else {
+    if (threadIdx.x == 0) {
+      s_prefix = 0;
+      s_rank = mid;
+    }
+    for (int pass = 0; pass < RADIX_PASSES; ++pass) {
+      const int shift = 56 - 8 * pass;
+      for (int b = threadIdx.x; b < 256; b += SMALL_THREADS) hist[b] = 0;
+      __syncthreads();
+      const uint64_t prefix = s_prefix;
+      for (uint32_t i = threadIdx.x; i < len; i += SMALL_THREADS) {
+        uint64_t k = keys[i];
+        if (pass == 0 || ((k ^ prefix) >> (shift + 8)) == 0) atomicAdd(&hist[(k >> shift) & 255], 1u);
+      }
+      __syncthreads();
+      if (threadIdx.x < 32) {
+        // warp 0 scans the 256 bins, 8 per lane
+        const int lane = threadIdx.x;
+        uint32_t c[8], s = 0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          c[i] = hist[lane * 8 + i];
+          s += c[i];
+        }
+        uint32_t x = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+          if (lane >= o) x += y;
+        }
+        uint32_t excl = x - s;
+        const uint32_t rank = s_rank;
+        if (excl <= rank && rank < x) {
+          uint32_t acc = excl;
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            if (acc <= rank && rank < acc + c[i]) {
+              s_prefix = prefix | (static_cast<uint64_t>(lane * 8 + i) << shift);
+              s_rank = rank - acc;
+            }
+            acc += c[i];
+          }
+        }
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) s_pivot = s_prefix;
+  }
+  __syncthreads();
+  const uint64_t pk = s_pivot;
+  const uint64_t pc = canon(pk);
+
+  // lt = #{key < pivot} under f64 '<' (build.rs:209)
+  uint32_t my_lt = 0;
+  for (uint32_t i = threadIdx.x; i < len; i += SMALL_THREADS) my_lt += canon(keys[i]) < pc;
+  const uint32_t lt = block_sum<SMALL_THREADS>(my_lt, sh_warp);
+
+  // misplaced rows: key >= pivot in [0, lt), key < pivot in [lt, len); each
+  // thread owns a contiguous run of positions so ranks come out ascending.
+  const uint32_t per = (len + SMALL_THREADS - 1) / SMALL_THREADS;
+  const uint32_t b0 = min(len, threadIdx.x * per), b1 = min(len, b0 + per);
+  uint32_t cnt = 0;
+  for (uint32_t i = b0; i < b1; ++i) {
+    bool below = canon(keys[i]) < pc;
+    cnt += (i < lt) ? !below : below;
+  }
+  uint32_t n2;
+  uint32_t r = block_excl_scan<SMALL_THREADS>(cnt, &n2, sh_warp);
+  for (uint32_t i = b0; i < b1; ++i) {
+    bool below = canon(keys[i]) < pc;
+    if ((i < lt) ? !below : below) plist[r++] = static_cast<uint16_t>(i);
+  }
+  for (uint32_t i = threadIdx.x; i < len; i += SMALL_THREADS) cur[i] = static_cast<uint16_t>(i);
+  __syncthreads();
+  // swap R[i] <-> L[n-1-i]: the row at plist[2n-1-j] lands on plist[j]
+  for (uint32_t j = threadIdx.x; j < n2; j += SMALL_THREADS) cur[plist[j]] = plist[n2 - 1 - j];
+  __syncthreads();
+  if (mid > lt && threadIdx.x == 0) {
+    // pivot-equal fix-up (build.rs:303-313), sequentially on the shared copy
+    uint32_t place = lt, scan = lt;
+    while (place < mid && scan < len) {
+      if (canon(keys[cur[scan]]) == pc) {
+        uint16_t t = cur[scan];
+        cur[scan] = cur[place];
+        cur[place] = t;
+        ++place;
+      }
+      ++scan;
+    }
+  }
+  __syncthreads();
+  // gather rows into their new positions
+  for (uint64_t f = threadIdx.x; f < static_cast<uint64_t>(len) * d; f += SMALL_THREADS) {
+    uint32_t p = static_cast<uint32_t>(f / d);
+    uint32_t j = static_cast<uint32_t>(f - static_cast<uint64_t>(p) * d);
+    dout[f] = din[static_cast<uint64_t>(cur[p]) * d + j];
+  }
+  for (uint32_t i = threadIdx.x; i < len; i += SMALL_THREADS) iout[i] = iin[cur[i]];
+  if (threadIdx.x == 0) expand_inner(L, slot, node, start, len, dim, pk);
+  // children's boxes start at the identities of min / max
+  uint64_t* cl = L.boxkeys + static_cast<uint64_t>(node + 1) * 2 * d;
+  uint64_t* cr = L.boxkeys + static_cast<uint64_t>(node + 1 + count_nodes_impl(mid, L.leafsize)) * 2 * d;
+  for (uint64_t j = threadIdx.x; j < 2 * d; j += SMALL_THREADS) {
+    cl[j] = (j < d) ? KEY_MAX : 0;
+    cr[j] = (j < d) ? KEY_MAX : 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Large path: grids of (segment slot, row chunk) CTAs.
+// ---------------------------------------------------------------------------
+struct LargeScratch {
+  uint64_t* keys;       // N: split-coordinate keys of the current level
+  uint64_t* keys_out;   // N: keys moved with their rows (for the fix-up)
+  uint32_t* rankbuf;    // N: rank among the misplaced rows, or NONE
+  uint32_t* plist;      // N: misplaced positions by rank
+  uint32_t* hist;       // slots * RADIX_PASSES * 256
+  uint64_t* sel_prefix; // slots * (RADIX_PASSES + 1)
+  uint32_t* sel_rank;   // slots * (RADIX_PASSES + 1)
+  uint32_t* seg_dim;    // slots
+  uint64_t* seg_pivot;  // slots
+  uint32_t* seg_lt;     // slots
+  uint32_t* chunk_cnt;  // slots * n_chunks
+  uint32_t* seg_mis;    // slots
+};
+
+__global__ void k_lg_prepare(Level L, LargeScratch S) {
+  uint64_t slot = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  if (slot >= L.n_slots) return;
+  uint32_t node = L.seg_node[slot];
+  if (node == HOLE || L.seg_len[slot] <= L.leafsize) {
+    S.seg_dim[slot] = NONE;
+    return;
+  }
+  S.seg_dim[slot] = widest_axis_keys(L.boxkeys + static_cast<uint64_t>(node) * 2 * L.d, L.d);
+  S.sel_prefix[slot * (RADIX_PASSES + 1)] = 0;
+  S.sel_rank[slot * (RADIX_PASSES + 1)] = L.seg_len[slot] / 2;
+  S.seg_lt[slot] = 0;
+}
+
+// Pick the digit bucket of pass `pass` holding the wanted rank; returns the
+// state after that pass.  Every CTA of the segment computes the same answer.
+__device__ void pick_digit(const uint32_t* hist, int pass, uint64_t prefix_in, uint32_t rank_in,
+                           uint64_t* prefix_out, uint32_t* rank_out) {
+  uint32_t acc = 0;
+  const int shift = 56 - 8 * pass;
+  for (int b = 0; b < 256; ++b) {
+    uint32_t c = hist[b];
+    if (rank_in < acc + c) {
+      *prefix_out = prefix_in | (static_cast<uint64_t>(b) << shift);
+      *rank_out = rank_in - acc;
+      return;
+    }
+    acc += c;
+  }
+  *prefix_out = prefix_in;
+  *rank_out = rank_in;
+}
+
+// Chunks of one segment: CTA (slot, y) handles chunks y, y + gridDim.y, ...
+#define KD_FOR_CHUNKS(len)                                                        \
+  for (uint32_t chunk = blockIdx.y, r0 = blockIdx.y * LG_CHUNK; r0 < (len);      \
+       chunk += gridDim.y, r0 = chunk * LG_CHUNK)
+
+__global__ void k_lg_keys(Level L, LargeScratch S) {
+  const uint64_t slot = blockIdx.x;
+  const uint32_t dim = S.seg_dim[slot];
+  if (dim == NONE) return;
+  const uint32_t start = L.seg_start[slot], len = L.seg_len[slot];
+  KD_FOR_CHUNKS(len) {
+    for (uint32_t i = r0 + threadIdx.x; i < min(len, r0 + LG_CHUNK); i += LG_THREADS) {
+      uint64_t row = static_cast<uint64_t>(start) + i;
+      S.keys[row] = total_key(L.din[row * L.d + dim]);
+    }
+  }
+}
+
+// Histogram pass `pass`; first replays the pick of pass-1 from its histogram.
+__global__ void k_lg_hist(Level L, LargeScratch S, int pass) {
+  __shared__ uint32_t sh[256];
+  __shared__ uint64_t s_prefix;
+  const uint64_t slot = blockIdx.x;
+  if (S.seg_dim[slot] == NONE) return;
+  const uint32_t start = L.seg_start[slot], len = L.seg_len[slot];
+  if (blockIdx.y * LG_CHUNK >= len) return;
+  for (int b = threadIdx.x; b < 256; b += LG_THREADS) sh[b] = 0;
+  if (threadIdx.x == 0) {
+    uint64_t prefix = S.sel_prefix[slot * (RADIX_PASSES + 1) + (pass > 0 ? pass - 1 : 0)];
+    if (pass > 0) {
+      uint32_t rank = S.sel_rank[slot * (RADIX_PASSES + 1) + pass - 1], nr;
+      uint64_t np;
+      pick_digit(S.hist + (slot * RADIX_PASSES + pass - 1) * 256, pass - 1, prefix, rank, &np, &nr);
+      prefix = np;
+      if (blockIdx.y == 0) {  // publish the state for the next pass (all CTAs agree)
+        S.sel_prefix[slot * (RADIX_PASSES + 1) + pass] = np;
+        S.sel_rank[slot * (RADIX_PASSES + 1) + pass] = nr;
+      }
+    }
+    s_prefix = prefix;
+  }
+  __syncthreads();
+  const uint64_t prefix = s_prefix;
+  const int shift = 56 - 8 * pass;
+  KD_FOR_CHUNKS(len) {
+    for (uint32_t i = r0 + threadIdx.x; i < min(len, r0 + LG_CHUNK); i += LG_THREADS) {
+      uint64_t k = S.keys[static_cast<uint64_t>(start) + i];
+      if (pass == 0 || ((k ^ prefix) >> (shift + 8)) == 0) atomicAdd(&sh[(k >> shift) & 255], 1u);
+    }
+  }
+  __syncthreads();
+  uint32_t* g = S.hist + (slot * RADIX_PASSES + pass) * 256;
+  for (int b = threadIdx.x; b < 256; b += LG_THREADS)
+    if (sh[b]) atomicAdd(&g[b], sh[b]);
+}
+
+// Final pick -> pivot; then lt = #{key < pivot}.
+__global__ void k_lg_count_lt(Level L, LargeScratch S) {
+  __shared__ uint32_t sh_warp[LG_THREADS / 32];
+  __shared__ uint64_t s_pivot;
+  const uint64_t slot = blockIdx.x;
+  if (S.seg_dim[slot] == NONE) return;
+  const uint32_t start = L.seg_start[slot], len = L.seg_len[slot];
+  if (blockIdx.y * LG_CHUNK >= len) return;
+  if (threadIdx.x == 0) {
+    const int p = RADIX_PASSES - 1;
+    uint64_t np;
+    uint32_t nr;
+    pick_digit(S.hist + (slot * RADIX_PASSES + p) * 256, p, S.sel_prefix[slot * (RADIX_PASSES + 1) + p],
+               S.sel_rank[slot * (RADIX_PASSES + 1) + p], &np, &nr);
+    s_pivot = np;
+    if (blockIdx.y == 0) S.seg_pivot[slot] = np;
+  }
+  __syncthreads();
+  const uint64_t pc = canon(s_pivot);
+  uint32_t c = 0;
+  KD_FOR_CHUNKS(len) {
+    for (uint32_t i = r0 + threadIdx.x; i < min(len, r0 + LG_CHUNK); i += LG_THREADS)
+      c += canon(S.keys[static_cast<uint64_t>(start) + i]) < pc;
+  }
+  uint32_t total = block_sum<LG_THREADS>(c, sh_warp);
+  if (threadIdx.x == 0 && total) atomicAdd(&S.seg_lt[slot], total);
+}
+
+__device__ __forceinline__ bool misplaced(uint64_t key, uint64_t pc, uint32_t i, uint32_t lt) {
+  bool below = canon(key) < pc;
+  return (i < lt) ? !below : below;
+}
+
+__global__ void k_lg_flagcount(Level L, LargeScratch S, uint32_t n_chunks) {
+  __shared__ uint32_t sh_warp[LG_THREADS / 32];
+  const uint64_t slot = blockIdx.x;
+  if (S.seg_dim[slot] == NONE) return;
+  const uint32_t start = L.seg_start[slot], len = L.seg_len[slot];
+  const uint64_t pc = canon(S.seg_pivot[slot]);
+  const uint32_t lt = S.seg_lt[slot];
+  KD_FOR_CHUNKS(len) {
+    uint32_t c = 0;
+    for (uint32_t i = r0 + threadIdx.x; i < min(len, r0 + LG_CHUNK); i += LG_THREADS)
+      c += misplaced(S.keys[static_cast<uint64_t>(start) + i], pc, i, lt);
+    uint32_t total = block_sum<LG_THREADS>(c, sh_warp);
+    if (threadIdx.x == 0) S.chunk_cnt[slot * n_chunks + chunk] = total;
+  }
+}
+
+__global__ void k_lg_chunkscan(Level L, LargeScratch S, uint32_t n_chunks) {
+  __shared__ uint32_t sh_warp[1024 / 32];
+  __shared__ uint32_t s_run;
+  const uint64_t slot = blockIdx.x;
+  if (S.seg_dim[slot] == NONE) return;
+  uint32_t* c = S.chunk_cnt + slot * n_chunks;
+  if (threadIdx.x == 0) s_run = 0;
+  __syncthreads();
+  for (uint32_t b = 0; b < n_chunks; b += 1024) {
+    uint32_t i = b + threadIdx.x;
+    uint32_t v = i < n_chunks ? c[i] : 0;
+    uint32_t tot;
+    uint32_t ex = block_excl_scan<1024>(v, &tot, sh_warp);
+    uint32_t run = s_run;
+    if (i < n_chunks) c[i] = run + ex;
+    __syncthreads();
+    if (threadIdx.x == 0) s_run = run + tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) S.seg_mis[slot] = s_run;
+}
+
+__global__ void k_lg_lists(Level L, LargeScratch S, uint32_t n_chunks) {
+  __shared__ uint32_t sh_warp[LG_THREADS / 32];
+  const uint64_t slot = blockIdx.x;
+  if (S.seg_dim[slot] == NONE) return;
+  const uint32_t start = L.seg_start[slot], len = L.seg_len[slot];
+  const uint64_t pc = canon(S.seg_pivot[slot]);
+  const uint32_t lt = S.seg_lt[slot];
+  KD_FOR_CHUNKS(len) {
+  // each thread owns LG_ITEMS consecutive rows
+  const uint32_t i0 = r0 + threadIdx.x * LG_ITEMS;
+  uint32_t flags = 0, c = 0;
+#pragma unroll
+  for (int t = 0; t < LG_ITEMS; ++t) {
+    uint32_t i = i0 + t;
+    if (i < len && misplaced(S.keys[static_cast<uint64_t>(start) + i], pc, i, lt)) {
+      flags |= 1u << t;
+      ++c;
+    }
+  }
+  uint32_t tot;
+  uint32_t r = block_excl_scan<LG_THREADS>(c, &tot, sh_warp) + S.chunk_cnt[slot * n_chunks + chunk];
+#pragma unroll
+  for (int t = 0; t < LG_ITEMS; ++t) {
+    uint32_t i = i0 + t;
+    if (i >= len) break;
+    uint64_t row = static_cast<uint64_t>(start) + i;
+    if (flags & (1u << t)) {
+      S.rankbuf[row] = r;
+      S.plist[static_cast<uint64_t>(start) + r] = i;
+      ++r;
+    } else {
+      S.rankbuf[row] = NONE;
+    }
+  }
+  }
+}
+
+// Move rows to their post-swap positions; leaf segments copy through.
+__global__ void k_lg_move(Level L, LargeScratch S) {
+  const uint64_t slot = blockIdx.x;
+  const uint32_t node = L.seg_node[slot];
+  if (node == HOLE) return;
+  const uint32_t start = L.seg_start[slot], len = L.seg_len[slot];
+  const bool inner = S.seg_dim[slot] != NONE;
+  const uint32_t n2 = inner ? S.seg_mis[slot] : 0;
+  const uint64_t d = L.d;
+  KD_FOR_CHUNKS(len)
+  for (uint32_t i = r0 + threadIdx.x; i < min(len, r0 + LG_CHUNK); i += LG_THREADS) {
+    const uint64_t row = static_cast<uint64_t>(start) + i;
+    uint32_t p = i;
+    if (inner) {
+      uint32_t r = S.rankbuf[row];
+      if (r != NONE) p = S.plist[static_cast<uint64_t>(start) + n2 - 1 - r];
+    }
+    const uint64_t dst = static_cast<uint64_t>(start) + p;
+    for (uint64_t j = 0; j < d; ++j) L.dout[dst * d + j] = L.din[row * d + j];
+    L.iout[dst] = L.iin[row];
+    if (inner) S.keys_out[dst] = S.keys[row];
+  }
+}
+
+// Pivot-equal fix-up for large segments (build.rs:303-313), one CTA per
+// segment, in place on the moved rows; only segments with mid > lt do work.
+constexpr int FIX_THREADS = 1024;
+__global__ void __launch_bounds__(FIX_THREADS) k_lg_fixup(Level L, LargeScratch S) {
+  __shared__ uint32_t sh_warp[FIX_THREADS / 32];
+  __shared__ uint32_t s_count, s_changed, s_stop;
+  const uint64_t slot = blockIdx.x;
+  if (S.seg_dim[slot] == NONE) return;
+  const uint32_t start = L.seg_start[slot], len = L.seg_len[slot];
+  const uint32_t lt = S.seg_lt[slot], mid = len / 2;
+  if (mid <= lt) return;
+  const uint32_t m = mid - lt;
+  const uint64_t pc = canon(S.seg_pivot[slot]);
+  const uint64_t d = L.d;
+  const uint64_t base = start;
+  uint32_t* E = S.plist + base;     // E[t]: relative position of the t-th pivot-equal row
+  uint32_t* J = S.rankbuf + base;   // J[t]: chain pointer of place lt + t
+  uint32_t* dest = reinterpret_cast<uint32_t*>(S.keys + base);  // destinations of [lt, stop]
+  if (threadIdx.x == 0) s_count = 0;
+  __syncthreads();
+  // 1. first m pivot-equal rows of [lt, len), in order
+  for (uint32_t b = lt; b < len; b += FIX_THREADS) {
+    uint32_t i = b + threadIdx.x;
+    uint32_t eq = (i < len) && canon(S.keys_out[base + i]) == pc;
+    uint32_t tot;
+    uint32_t r = block_excl_scan<FIX_THREADS>(eq, &tot, sh_warp);
+    uint32_t c0 = s_count;
+    if (eq && c0 + r < m) {
+      E[c0 + r] = i;
+      dest[i - lt] = lt + c0 + r;
+    } else if (i < len) {
+      dest[i - lt] = NONE;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_count = c0 + tot;
+    __syncthreads();
+    if (s_count >= m) break;
+  }
+  // The pivot is the mid-th order statistic, so [lt, len) holds at least m
+  // pivot-equal rows; if not, leave the rows unpermuted rather than read past E.
+  if (s_count < m) return;
+  if (threadIdx.x == 0) s_stop = E[m - 1];
+  __syncthreads();
+  const uint32_t stop = s_stop;
+  // 2. chains: the row at place lt+t moves to E[t]; follow until past the places
+  for (uint32_t t = threadIdx.x; t < m; t += FIX_THREADS) J[t] = E[t];
+  __syncthreads();
+  for (;;) {
+    if (threadIdx.x == 0) s_changed = 0;
+    __syncthreads();
+    for (uint32_t t = threadIdx.x; t < m; t += FIX_THREADS) {
+      uint32_t j = J[t];
+      if (j - lt < m) {
+        uint32_t nj = J[j - lt];
+        if (nj != j) {
+          J[t] = nj;
+          s_changed = 1;
+        }
+      }
+    }
+    __syncthreads();
+    if (!s_changed) break;
+    __syncthreads();
+  }
+  // 3. destinations of the displaced (not pivot-equal or beyond the m-th) rows
+  for (uint32_t i = lt + threadIdx.x; i <= stop; i += FIX_THREADS) {
+    if (dest[i - lt] == NONE) dest[i - lt] = (i - lt < m) ? J[i - lt] : i;
+  }
+  __syncthreads();
+  // 4. permute [lt, stop] through the (now free) source buffer of this segment
+  double* tmp = const_cast<double*>(L.din);
+  uint32_t* itmp = const_cast<uint32_t*>(L.iin);
+  for (uint64_t f = static_cast<uint64_t>(lt) * d + threadIdx.x; f < (static_cast<uint64_t>(stop) + 1) * d;
+       f += FIX_THREADS)
+    tmp[base * d + f] = L.dout[base * d + f];
+  for (uint32_t i = lt + threadIdx.x; i <= stop; i += FIX_THREADS) itmp[base + i] = L.iout[base + i];
+  __syncthreads();
+  for (uint64_t f = static_cast<uint64_t>(lt) * d + threadIdx.x; f < (static_cast<uint64_t>(stop) + 1) * d;
+       f += FIX_THREADS) {
+    uint32_t i = static_cast<uint32_t>(f / d);
+    uint64_t j = f - static_cast<uint64_t>(i) * d;
+    L.dout[(base + dest[i - lt]) * d + j] = tmp[base * d + f];
+  }
+  for (uint32_t i = lt + threadIdx.x; i <= stop; i += FIX_THREADS) L.iout[base + dest[i - lt]] = itmp[base + i];
+}
+
+__global__ void k_lg_expand(Level L, LargeScratch S) {
+  uint64_t slot = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  if (slot >= L.n_slots) return;
+  const uint32_t node = L.seg_node[slot];
+  if (node == HOLE) {
+    L.nseg_node[2 * slot] = HOLE;
+    L.nseg_node[2 * slot + 1] = HOLE;
+    L.nseg_len[2 * slot] = 0;
+    L.nseg_len[2 * slot + 1] = 0;
+    return;
+  }
+  const uint32_t start = L.seg_start[slot], len = L.seg_len[slot];
+  if (S.seg_dim[slot] == NONE) {
+    close_leaf(L, slot, node, start, len);
+    return;
+  }
+  expand_inner(L, slot, node, start, len, S.seg_dim[slot], S.seg_pivot[slot]);
+  const uint64_t d = L.d;
+  uint64_t* cl = L.boxkeys + static_cast<uint64_t>(node + 1) * 2 * d;
+  uint64_t* cr = L.boxkeys + static_cast<uint64_t>(L.nseg_node[2 * slot + 1]) * 2 * d;
+  for (uint64_t j = 0; j < 2 * d; ++j) {
+    cl[j] = (j < d) ? KEY_MAX : 0;
+    cr[j] = (j < d) ? KEY_MAX : 0;
+  }
+}
+
+// All-leaf level: record the leaves.
+__global__ void k_leaf_records(Level L) {
+  uint64_t slot = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  if (slot >= L.n_slots) return;
+  const uint32_t node = L.seg_node[slot];
+  if (node == HOLE) return;
+  write_leaf(L.nodes, node, L.seg_start[slot], L.seg_len[slot]);
+  L.node_len[node] = L.seg_len[slot];
+}
+
+// order_by_box (src/build.rs:234-238, 248-252), after every box is known.
+__global__ void k_order_by_box(DNode* nodes, const uint64_t* boxkeys, const uint32_t* node_len,
+                               uint64_t n_nodes, uint64_t d) {
+  uint64_t id = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  if (id >= n_nodes) return;
+  DNode nd = nodes[id];
+  if (nd.meta & KD_NODE_LEAF) return;
+  if (d <= 1 || node_len[id] < 64) return;
+  const uint32_t dim = nd.meta & KD_NODE_DIM_MASK;
+  const uint64_t* own = boxkeys + id * 2 * d;
+  const uint64_t kids[2] = {id + 1, nd.right};
+  for (int c = 0; c < 2; ++c) {
+    const uint64_t* ch = boxkeys + kids[c] * 2 * d;
+    for (uint64_t j = 0; j < d; ++j) {
+      if (j == dim) continue;
+      double ce = dsub(from_total_key(ch[d + j]), from_total_key(ch[j]));
+      double pe = dsub(from_total_key(own[d + j]), from_total_key(own[j]));
+      if (!(ce < dmul(0.6, pe))) return;
+    }
+  }
+  nodes[id].meta = nd.meta | KD_NODE_BOX_ORDER;
+}
+
+__global__ void k_boxes_finalize(uint64_t* boxkeys, uint64_t total) {
+  uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  if (i < total) boxkeys[i] = from_total_key_bits(boxkeys[i]);
+}
+
+__global__ void k_iota(uint32_t* idx, uint64_t n) {
+  uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  if (i < n) idx[i] = static_cast<uint32_t>(i);
+}
+
+// FP32 filter copies: data rounded to nearest; boxes rounded outward.
+__global__ void k_make_f32(const double* data, float* data32, uint64_t n_el, const double* boxes, float* boxes32,
+                           uint64_t n_nodes, uint64_t d) {
+  uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  if (i < n_el) data32[i] = __double2float_rn(data[i]);
+  uint64_t nb = n_nodes * 2 * d;
+  if (i < nb) {
+    bool hi = ((i / d) & 1) != 0;
+    boxes32[i] = hi ? __double2float_ru(boxes[i]) : __double2float_rd(boxes[i]);
+  }
+}
+
+struct DevBuf {
+  void* p = nullptr;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+};
+
+template <typename T>
+int dalloc(DevBuf& b, uint64_t count) {
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc(&b.p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    b.p = nullptr;
+    return fail(KD_ERR_OUT_OF_MEMORY, "device allocation failed");
+  }
+  return KD_OK;
+}
+
+inline unsigned grid1(uint64_t n, unsigned t) { return static_cast<unsigned>((n + t - 1) / t); }
+
+}  // namespace
+
+uint64_t count_nodes(uint64_t len, uint64_t leafsize) { return count_nodes_impl(len, leafsize); }
+
+int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsize, cudaStream_t st,
+                    kd_tree* t) {
+  const uint64_t n_nodes = count_nodes_impl(n, leafsize);
+  // Level structure (data-independent): sizes per depth, at most two values.
+  struct LevelShape {
+    uint64_t slots, max_len;
+    bool any_inner;
+  };
+  std::vector<LevelShape> shape;
+  {
+    std::vector<std::pair<uint64_t, uint64_t>> cur = {{n, 1}};
+    uint64_t slots = 1;
+    for (;;) {
+      LevelShape s{slots, 0, false};
+      std::vector<std::pair<uint64_t, uint64_t>> nxt;
+      for (auto& sc : cur) {
+        s.max_len = std::max(s.max_len, sc.first);
+        if (sc.first > leafsize) {
+          s.any_inner = true;
+          for (uint64_t h : {sc.first / 2, sc.first - sc.first / 2}) {
+            auto it = std::find_if(nxt.begin(), nxt.end(), [&](auto& x) { return x.first == h; });
+            if (it == nxt.end())
+              nxt.push_back({h, sc.second});
+            else
+              it->second += sc.second;
+          }
+        }
+      }
+      shape.push_back(s);
+      if (!s.any_inner) break;
+      cur = nxt;
+      slots *= 2;
+    }
+  }
+  const uint64_t max_slots = shape.back().slots;
+  uint64_t large_slots = 0;  // widest level handled by the large path
+  for (auto& s : shape)
+    if (s.any_inner && s.max_len > static_cast<uint64_t>(SMALL_MAX)) large_slots = std::max(large_slots, s.slots);
+  const uint32_t max_chunks = static_cast<uint32_t>((n + LG_CHUNK - 1) / LG_CHUNK);
+
+  DevBuf data_a, data_b, idx_a, idx_b, nodes, boxes, node_len, seg_a[3], seg_b[3], status;
+  DevBuf keys, keys_out, rankbuf, plist, hist, sel_prefix, sel_rank, seg_dim, seg_pivot, seg_lt, chunk_cnt, seg_mis;
+  int rc;
+  if ((rc = dalloc<double>(data_a, n * d)) || (rc = dalloc<double>(data_b, n * d)) ||
+      (rc = dalloc<uint32_t>(idx_a, n)) || (rc = dalloc<uint32_t>(idx_b, n)) ||
+      (rc = dalloc<DNode>(nodes, n_nodes)) || (rc = dalloc<uint64_t>(boxes, n_nodes * 2 * d)) ||
+      (rc = dalloc<uint32_t>(node_len, n_nodes)) || (rc = dalloc<uint32_t>(status, 1)))
+    return rc;
+  for (int i = 0; i < 3; ++i)
+    if ((rc = dalloc<uint32_t>(seg_a[i], max_slots)) || (rc = dalloc<uint32_t>(seg_b[i], max_slots))) return rc;
+  if (large_slots) {
+    if ((rc = dalloc<uint64_t>(keys, n)) || (rc = dalloc<uint64_t>(keys_out, n)) ||
+        (rc = dalloc<uint32_t>(rankbuf, n)) || (rc = dalloc<uint32_t>(plist, n)) ||
+        (rc = dalloc<uint32_t>(hist, large_slots * RADIX_PASSES * 256)) ||
+        (rc = dalloc<uint64_t>(sel_prefix, large_slots * (RADIX_PASSES + 1))) ||
+        (rc = dalloc<uint32_t>(sel_rank, large_slots * (RADIX_PASSES + 1))) ||
+        (rc = dalloc<uint32_t>(seg_dim, large_slots)) || (rc = dalloc<uint64_t>(seg_pivot, large_slots)) ||
+        (rc = dalloc<uint32_t>(seg_lt, large_slots)) ||
+        (rc = dalloc<uint32_t>(chunk_cnt, large_slots * static_cast<uint64_t>(max_chunks))) ||
+        (rc = dalloc<uint32_t>(seg_mis, large_slots)))
+      return rc;
+  }
+
+  KD_TRY_CUDA(cudaMemcpyAsync(data_a.p, d_src, n * d * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  k_iota<<<grid1(n, 256), 256, 0, st>>>(static_cast<uint32_t*>(idx_a.p), n);
+  k_init_boxkeys<<<grid1(2 * d, 256), 256, 0, st>>>(static_cast<uint64_t*>(boxes.p), 1, d);
+  KD_TRY_CUDA(cudaMemsetAsync(status.p, 0, sizeof(uint32_t), st));
+  {
+    uint32_t root[3] = {0, 0, static_cast<uint32_t>(n)};
+    for (int i = 0; i < 3; ++i)
+      KD_TRY_CUDA(cudaMemcpyAsync(seg_a[i].p, &root[i], sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+  }
+
+  double* din = static_cast<double*>(data_a.p);
+  double* dout = static_cast<double*>(data_b.p);
+  uint32_t* iin = static_cast<uint32_t*>(idx_a.p);
+  uint32_t* iout = static_cast<uint32_t*>(idx_b.p);
+  DevBuf* scur = seg_a;
+  DevBuf* snxt = seg_b;
+  const unsigned bbox_threads = d <= 256 ? static_cast<unsigned>(d * (256 / d)) : 256u;
+
+  for (size_t lv = 0; lv < shape.size(); ++lv) {
+    const LevelShape& s = shape[lv];
+    Level L{din, dout, iin, iout, d, leafsize,
+            static_cast<uint32_t*>(scur[0].p), static_cast<uint32_t*>(scur[1].p), static_cast<uint32_t*>(scur[2].p),
+            static_cast<uint32_t*>(snxt[0].p), static_cast<uint32_t*>(snxt[1].p), static_cast<uint32_t*>(snxt[2].p),
+            static_cast<DNode*>(nodes.p), static_cast<uint64_t*>(boxes.p), static_cast<uint32_t*>(node_len.p),
+            s.slots};
+    // Boxes: the root and every level below the large path's levels come from
+    // the bbox kernel (the small path initialises its children's box keys).
+    {
+      const uint64_t chunk_rows = std::max<uint64_t>(1, (bbox_threads * 8) / d);
+      const uint64_t nchunk = (s.max_len + chunk_rows - 1) / chunk_rows;
+      dim3 g(static_cast<unsigned>(s.slots), static_cast<unsigned>(std::min<uint64_t>(nchunk, 65535)));
+      k_bbox<<<g, bbox_threads, 2 * d * sizeof(uint64_t), st>>>(L, static_cast<uint32_t>(chunk_rows),
+                                                                static_cast<uint32_t>(nchunk), lv == 0,
+                                                                static_cast<uint32_t*>(status.p));
+      KD_TRY_CUDA(cudaGetLastError());
+    }
+    if (lv == 0) {
+      uint32_t h_status = 0;
+      KD_TRY_CUDA(cudaMemcpyAsync(&h_status, status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+      KD_TRY_CUDA(cudaStreamSynchronize(st));
+      if (h_status) return fail(KD_ERR_NONFINITE_DATA, "all coordinates must be finite");
+    }
+    if (!s.any_inner) {
+      k_leaf_records<<<grid1(s.slots, 256), 256, 0, st>>>(L);
+      KD_TRY_CUDA(cudaGetLastError());
+      break;
+    }
+    if (s.max_len <= static_cast<uint64_t>(SMALL_MAX)) {
+      const size_t smem = SMALL_MAX * (sizeof(uint64_t) + 2 * sizeof(uint16_t));
+      KD_TRY_CUDA(cudaFuncSetAttribute(k_small_level, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem)));
+      k_small_level<<<static_cast<unsigned>(s.slots), SMALL_THREADS, smem, st>>>(L);
+      KD_TRY_CUDA(cudaGetLastError());
+    } else {
+      LargeScratch S{static_cast<uint64_t*>(keys.p),     static_cast<uint64_t*>(keys_out.p),
+                     static_cast<uint32_t*>(rankbuf.p),  static_cast<uint32_t*>(plist.p),
+                     static_cast<uint32_t*>(hist.p),     static_cast<uint64_t*>(sel_prefix.p),
+                     static_cast<uint32_t*>(sel_rank.p), static_cast<uint32_t*>(seg_dim.p),
+                     static_cast<uint64_t*>(seg_pivot.p), static_cast<uint32_t*>(seg_lt.p),
+                     static_cast<uint32_t*>(chunk_cnt.p), static_cast<uint32_t*>(seg_mis.p)};
+      const uint32_t nch = static_cast<uint32_t>((s.max_len + LG_CHUNK - 1) / LG_CHUNK);
+      dim3 g(static_cast<unsigned>(s.slots), std::min<uint32_t>(nch, 65535u));
+      KD_TRY_CUDA(cudaMemsetAsync(hist.p, 0, s.slots * RADIX_PASSES * 256 * sizeof(uint32_t), st));
+      k_lg_prepare<<<grid1(s.slots, 256), 256, 0, st>>>(L, S);
+      k_lg_keys<<<g, LG_THREADS, 0, st>>>(L, S);
+      for (int pass = 0; pass < RADIX_PASSES; ++pass) k_lg_hist<<<g, LG_THREADS, 0, st>>>(L, S, pass);
+      k_lg_count_lt<<<g, LG_THREADS, 0, st>>>(L, S);
+      k_lg_flagcount<<<g, LG_THREADS, 0, st>>>(L, S, nch);
+      k_lg_chunkscan<<<static_cast<unsigned>(s.slots), 1024, 0, st>>>(L, S, nch);
+      k_lg_lists<<<g, LG_THREADS, 0, st>>>(L, S, nch);
+      k_lg_move<<<g, LG_THREADS, 0, st>>>(L, S);
+      k_lg_fixup<<<static_cast<unsigned>(s.slots), FIX_THREADS, 0, st>>>(L, S);
+      k_lg_expand<<<grid1(s.slots, 256), 256, 0, st>>>(L, S);
+      KD_TRY_CUDA(cudaGetLastError());
+    }
+    std::swap(din, dout);
+    std::swap(iin, iout);
+    std::swap(scur, snxt);
+  }
+
+  k_order_by_box<<<grid1(n_nodes, 256), 256, 0, st>>>(static_cast<DNode*>(nodes.p), static_cast<uint64_t*>(boxes.p),
+                                                      static_cast<uint32_t*>(node_len.p), n_nodes, d);
+  k_boxes_finalize<<<grid1(n_nodes * 2 * d, 256), 256, 0, st>>>(static_cast<uint64_t*>(boxes.p), n_nodes * 2 * d);
+  KD_TRY_CUDA(cudaGetLastError());
+
+  // The final row order sits in `din` (the last level's destination, or the
+  // copy of the input when the root is a leaf).
+  DevBuf data32, boxes32;
+  if ((rc = dalloc<float>(data32, n * d)) || (rc = dalloc<float>(boxes32, n_nodes * 2 * d))) return rc;
+  k_make_f32<<<grid1(std::max(n * d, n_nodes * 2 * d), 256), 256, 0, st>>>(
+      din, static_cast<float*>(data32.p), n * d, reinterpret_cast<const double*>(boxes.p),
+      static_cast<float*>(boxes32.p), n_nodes, d);
+  KD_TRY_CUDA(cudaGetLastError());
+  KD_TRY_CUDA(cudaStreamSynchronize(st));
+
+  t->n_points = n;
+  t->ndim = d;
+  t->leafsize = leafsize;
+  t->n_nodes = n_nodes;
+  // hand the final buffers to the tree; the DevBuf destructors free the rest
+  DevBuf* final_data = (din == data_a.p) ? &data_a : &data_b;
+  DevBuf* final_idx = (iin == idx_a.p) ? &idx_a : &idx_b;
+  t->data = static_cast<double*>(final_data->p);
+  final_data->p = nullptr;
+  t->indices = static_cast<uint32_t*>(final_idx->p);
+  final_idx->p = nullptr;
+  t->nodes = static_cast<DNode*>(nodes.p);
+  nodes.p = nullptr;
+  t->boxes = reinterpret_cast<double*>(boxes.p);
+  boxes.p = nullptr;
+  t->data32 = static_cast<float*>(data32.p);
+  data32.p = nullptr;
+  t->boxes32 = static_cast<float*>(boxes32.p);
+  boxes32.p = nullptr;
+  return KD_OK;
+}
+
+}  // namespace kd

@@ -1,0 +1,63 @@
+// kd_internal.hpp -- host-side definitions shared by the C-ABI, the build and the
+// query translation units of libkdtree_gb300.so.
+#pragma once
+
+#include <cstdint>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "kd_common.cuh"
+
+// The tree object behind the opaque `kd_tree*` of the C ABI.  Everything the
+// query touches lives in device memory; the host keeps only the sizes.
+struct kd_tree {
+  uint64_t n_points = 0;
+  uint64_t ndim = 0;
+  uint64_t leafsize = 0;
+  uint64_t n_nodes = 0;
+  int device = 0;
+  double* data = nullptr;       // n_points * ndim, tree (leaf-contiguous) order
+  uint32_t* indices = nullptr;  // tree position -> original row
+  kd::DNode* nodes = nullptr;   // n_nodes, preorder
+  double* boxes = nullptr;      // n_nodes * 2 * ndim, [lo | hi] per node
+  float* data32 = nullptr;      // n_points * ndim, round-to-nearest FP32 copy (filters)
+  float* boxes32 = nullptr;     // n_nodes * 2 * ndim, [lo rounded down | hi rounded up]
+};
+
+namespace kd {
+
+// Thread-local last-error text (read through kd_last_error).
+void set_error(const std::string& msg);
+int fail(int status, const std::string& msg);
+int cuda_fail(cudaError_t err, const char* what);
+
+#define KD_TRY_CUDA(call)                                   \
+  do {                                                      \
+    cudaError_t kd_err_ = (call);                           \
+    if (kd_err_ != cudaSuccess) return ::kd::cuda_fail(kd_err_, #call); \
+  } while (0)
+
+uint64_t count_nodes(uint64_t len, uint64_t leafsize);
+
+// Build the tree from device data (already validated for shape and size).
+// Returns a KD_* status; on success fills t's device buffers.
+int build_on_device(const double* d_src, uint64_t n_points, uint64_t ndim, uint64_t leafsize,
+                    cudaStream_t stream, kd_tree* t);
+
+// Parameters of one query call after validation (src/query.rs:38-62).
+struct QueryParams {
+  int metric;         // MetricKind
+  double p;           // exponent (LP only)
+  double cutoff;      // reduce(max_distance), -0 normalised to +0
+  double eps_factor;  // reduce(1 + eps)
+  uint64_t k;
+};
+
+// Run the query on device buffers; `d_status` is a device word the kernels set
+// when a query is non-finite.  Work is ordered on `stream`.
+int query_on_device(const kd_tree* t, const double* d_queries, uint64_t n_queries,
+                    const QueryParams& qp, double* d_out_d, int64_t* d_out_i,
+                    cudaStream_t stream, uint32_t* d_status);
+
+}  // namespace kd

@@ -1,0 +1,235 @@
+"""`KDTree` over the GB300 engine's C ABI (include/kdtree_gb300.h).
+
+Restates the reference's pyo3 boundary (src/lib.rs:1-190) on top of
+libkdtree_gb300.so through ctypes:
+
+- inputs: any numpy.ndarray, promoted with `astype("float64")` and copied
+  row-major (lib.rs:25-45); anything else raises TypeError;
+- `data` must be 2-D, a query 1-D (single point) or 2-D (lib.rs:54-72), and a
+  query of the wrong width raises ValueError("dimension mismatch: ...")
+  (lib.rs:74-84);
+- reference errors (src/error.rs) raise ValueError with the reference's text;
+- results are fresh float64 / int64 arrays of shape (n, k), or (k,) for a 1-D
+  query (lib.rs:161-182);
+- ctypes releases the GIL for the duration of every native call, as
+  `py.detach` does in the reference (lib.rs:117, 176).
+
+There is no CPU fallback: a missing library raises ImportError, a machine
+without a CUDA device raises RuntimeError on the first build.
+"""
+from __future__ import annotations
+
+import ctypes
+import operator
+from pathlib import Path
+
+import numpy as np
+
+_LIB_PATH = Path(__file__).resolve().parent.parent / "_build" / "libkdtree_gb300.so"
+
+# Status codes (include/kdtree_gb300.h).  1..11 are the reference's KDTreeError.
+KD_OK = 0
+_VALUE_ERRORS = set(range(1, 12))
+KD_ERR_OUT_OF_MEMORY = 101
+
+
+def _load():
+    if not _LIB_PATH.exists():
+        raise ImportError(
+            f"{_LIB_PATH} is missing: build the CUDA engine first "
+            "(python kdtree-rs_gb300/build_lib.py); there is no CPU fallback"
+        )
+    L = ctypes.CDLL(str(_LIB_PATH))
+    P = ctypes.c_void_p
+    u64 = ctypes.c_uint64
+    d = ctypes.c_double
+    L.kd_build.argtypes = [P, u64, u64, u64, ctypes.c_int, ctypes.POINTER(P)]
+    L.kd_build.restype = ctypes.c_int
+    L.kd_build_device.argtypes = [P, u64, u64, u64, P, ctypes.POINTER(P)]
+    L.kd_build_device.restype = ctypes.c_int
+    L.kd_free.argtypes = [P]
+    L.kd_free.restype = None
+    L.kd_query.argtypes = [P, P, u64, u64, d, ctypes.c_int, d, d, ctypes.c_int, P, P]
+    L.kd_query.restype = ctypes.c_int
+    L.kd_query_device.argtypes = [P, P, u64, u64, d, ctypes.c_int, d, d, P, P, P]
+    L.kd_query_device.restype = ctypes.c_int
+    for name in ("kd_ndim", "kd_n_points", "kd_leafsize", "kd_n_nodes"):
+        getattr(L, name).argtypes = [P]
+        getattr(L, name).restype = u64
+    L.kd_count_nodes.argtypes = [u64, u64]
+    L.kd_count_nodes.restype = u64
+    L.kd_original_data.argtypes = [P, P]
+    L.kd_original_data.restype = ctypes.c_int
+    L.kd_export.argtypes = [P, P, P, P, P, P]
+    L.kd_export.restype = ctypes.c_int
+    L.kd_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    L.kd_last_error.restype = ctypes.c_size_t
+    return L
+
+
+_lib = _load()
+
+
+def library_path() -> Path:
+    return _LIB_PATH
+
+
+def _last_error() -> str:
+    n = _lib.kd_last_error(None, 0)
+    buf = ctypes.create_string_buffer(n + 1)
+    _lib.kd_last_error(buf, n + 1)
+    return buf.value.decode("utf-8", "replace")
+
+
+def _raise(status: int):
+    msg = _last_error()
+    if status in _VALUE_ERRORS:
+        raise ValueError(msg)
+    if status == KD_ERR_OUT_OF_MEMORY:
+        raise MemoryError(msg)
+    raise RuntimeError(f"kdtree engine error {status}: {msg}")
+
+
+def _usize(v, name: str) -> int:
+    """pyo3's `usize` extraction: an integer (TypeError otherwise) >= 0
+    (OverflowError otherwise)."""
+    v = operator.index(v)
+    if v < 0:
+        raise OverflowError(f"can't convert negative int to unsigned ({name})")
+    if v > 0xFFFFFFFFFFFFFFFF:
+        raise OverflowError(f"int too big to convert ({name})")
+    return v
+
+
+def _f64(v) -> float:
+    return float(v)
+
+
+def _bool(v, name: str) -> bool:
+    if isinstance(v, (bool, np.bool_)):
+        return bool(v)
+    raise TypeError(f"'{type(v).__name__}' object cannot be converted to 'PyBool' ({name})")
+
+
+def _as_f64_array(obj) -> np.ndarray:
+    """lib.rs:25-38."""
+    if not isinstance(obj, np.ndarray):
+        raise TypeError(f"expected a numpy.ndarray, got {type(obj).__name__}")
+    if obj.dtype != np.float64:
+        obj = obj.astype("float64")
+    return obj
+
+
+def _as_points(obj, what: str, allow_single: bool):
+    """lib.rs:54-72: returns (row-major float64 2-D array, single)."""
+    a = _as_f64_array(obj)
+    if a.ndim == 1 and allow_single:
+        return np.ascontiguousarray(a).reshape(1, -1), True
+    if a.ndim == 2:
+        return np.ascontiguousarray(a), False
+    raise ValueError(what)
+
+
+def _ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class KDTree:
+    """kd-tree for exact k-nearest-neighbour queries, built and queried on the GPU.
+
+    Same surface as the reference's `kdtree.KDTree` (python/kdtree/_core.pyi).
+    """
+
+    __slots__ = ("_h", "_ndim", "_n", "_leafsize", "__weakref__")
+
+    def __init__(self, data, *, leafsize: int = 32, parallel: bool = False):
+        pts, _ = _as_points(data, "data must be a two-dimensional array", False)
+        leafsize = _usize(leafsize, "leafsize")
+        parallel = _bool(parallel, "parallel")
+        h = ctypes.c_void_p()
+        st = _lib.kd_build(_ptr(pts), pts.size, pts.shape[1], leafsize, int(parallel), ctypes.byref(h))
+        if st != KD_OK:
+            _raise(st)
+        object.__setattr__(self, "_h", h)
+        object.__setattr__(self, "_ndim", int(_lib.kd_ndim(h)))
+        object.__setattr__(self, "_n", int(_lib.kd_n_points(h)))
+        object.__setattr__(self, "_leafsize", int(_lib.kd_leafsize(h)))
+
+    def __setattr__(self, name, value):
+        raise AttributeError(f"'KDTree' object attribute '{name}' is read-only")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            _lib.kd_free(h)
+
+    @property
+    def ndim(self) -> int:
+        return self._ndim
+
+    @property
+    def n_points(self) -> int:
+        return self._n
+
+    @property
+    def leafsize(self) -> int:
+        return self._leafsize
+
+    @property
+    def data(self) -> np.ndarray:
+        """The points in the caller's original order (tree.rs:60-68)."""
+        out = np.empty((self._n, self._ndim), np.float64)
+        st = _lib.kd_original_data(self._h, _ptr(out))
+        if st != KD_OK:
+            _raise(st)
+        return out
+
+    def __len__(self) -> int:
+        return self._n
+
+    def __repr__(self) -> str:
+        return f"KDTree(n_points={self._n}, ndim={self._ndim}, leafsize={self._leafsize})"
+
+    def query(self, x, *, k: int = 1, p: float = 2.0, max_distance: float | None = None, eps: float = 0.0,
+              parallel: bool = False):
+        """Exact k nearest neighbours of each row of `x` (lib.rs:161-182)."""
+        q, single = _as_points(x, "query must be one- or two-dimensional", True)
+        if q.shape[1] != self._ndim:
+            raise ValueError(f"dimension mismatch: expected {self._ndim}, got {q.shape[1]}")
+        k = _usize(k, "k")
+        p = _f64(p)
+        has_max = max_distance is not None
+        md = _f64(max_distance) if has_max else 0.0
+        eps = _f64(eps)
+        parallel = _bool(parallel, "parallel")
+        nq = q.shape[0]
+        if k == 0 or nq == 0:
+            # validation errors; the engine reports them without touching outputs
+            dummy_d = np.empty(1, np.float64)
+            dummy_i = np.empty(1, np.int64)
+            st = _lib.kd_query(self._h, _ptr(q) if q.size else None, q.size, k, p, int(has_max), md, eps,
+                               int(parallel), _ptr(dummy_d), _ptr(dummy_i))
+            _raise(st if st != KD_OK else 10)
+        out_d = np.empty((nq, k), np.float64)
+        out_i = np.empty((nq, k), np.int64)
+        st = _lib.kd_query(self._h, _ptr(q), q.size, k, p, int(has_max), md, eps, int(parallel), _ptr(out_d),
+                           _ptr(out_i))
+        if st != KD_OK:
+            _raise(st)
+        if single:
+            return out_d[0], out_i[0]
+        return out_d, out_i
+
+    # -- inspection (no reference counterpart in Python; mirrors Tree's fields)
+    def _export(self):
+        """(data in tree order, indices, node words [n_nodes, 4], split values, boxes)."""
+        nn = int(_lib.kd_n_nodes(self._h))
+        data = np.empty((self._n, self._ndim), np.float64)
+        idx = np.empty(self._n, np.uint32)
+        words = np.empty((nn, 4), np.uint32)
+        split = np.empty(nn, np.float64)
+        boxes = np.empty((nn, 2, self._ndim), np.float64)
+        st = _lib.kd_export(self._h, _ptr(data), _ptr(idx), _ptr(words), _ptr(split), _ptr(boxes))
+        if st != KD_OK:
+            _raise(st)
+        return data, idx, words, split, boxes

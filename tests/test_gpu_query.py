@@ -1,0 +1,119 @@
+"""GPU query against the oracle, bit for bit: every metric and strategy
+(Packed d<=8 with the d4 / d8 chunk orders, Folded 9..16, Streamed), k from 1
+to 32, eps > 0 (DFS-order dependent), max_distance padding, queries outside the
+root box (seeded CellBound), clustered data (order_by_box descents), and the
+plain workloads at full size."""
+import numpy as np
+import pytest
+
+from helpers import assert_bit_exact, gmm
+
+pytestmark = pytest.mark.gpu
+
+
+def _both(oracle, data, queries, leafsize, **kw):
+    from kdtree import KDTree
+
+    g = KDTree(data, leafsize=leafsize).query(queries, **kw)
+    o = oracle.OracleKDTree(data, leafsize=leafsize).query(queries, parallel=True, **kw)
+    return g, o
+
+
+@pytest.mark.parametrize("d", [1, 2, 3, 4, 5, 6, 7, 8, 9, 12, 16, 17, 24, 64])
+@pytest.mark.parametrize("p", [1.0, 2.0, np.inf])
+def test_widths_and_metrics(oracle, d, p):
+    rng = np.random.default_rng(100 * d + int(p if np.isfinite(p) else 99))
+    data = rng.normal(size=(3000, d))
+    q = rng.normal(size=(300, d)) * 1.3  # some queries outside the root box
+    for k in (1, 5, 16):
+        g, o = _both(oracle, data, q, 6, k=k, p=p)
+        assert_bit_exact(g, o)
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 7, 8, 9, 15, 16, 17, 31, 32])
+def test_k_values(oracle, k):
+    rng = np.random.default_rng(k)
+    data = rng.uniform(size=(20_000, 3))
+    q = rng.uniform(size=(2000, 3))
+    assert_bit_exact(*_both(oracle, data, q, 16, k=k))
+
+
+@pytest.mark.parametrize("p", [1.0, 2.0, np.inf])
+@pytest.mark.parametrize("eps", [0.1, 1.0])
+def test_eps_follows_reference_dfs_order(oracle, p, eps):
+    rng = np.random.default_rng(7)
+    data = gmm(30_000, 3, rng)
+    q = gmm(1000, 3, rng)
+    assert_bit_exact(*_both(oracle, data, q, 16, k=8, p=p, eps=eps))
+
+
+@pytest.mark.parametrize("p", [1.0, 2.0, np.inf])
+def test_max_distance(oracle, p):
+    rng = np.random.default_rng(11)
+    data = rng.uniform(size=(20_000, 3))
+    q = rng.uniform(size=(1000, 3)) * 1.2
+    for md in (0.0, 0.01, 0.05):
+        assert_bit_exact(*_both(oracle, data, q, 16, k=16, p=p, max_distance=md))
+
+
+def test_general_p(oracle):
+    """L^p distances go through pow(): CUDA's and libm's may differ in the last
+    ulp, so distances are compared with a tolerance and indices exactly."""
+    rng = np.random.default_rng(13)
+    data = rng.normal(size=(5000, 4))
+    q = rng.normal(size=(500, 4))
+    for p in (1.5, 3.0):
+        g, o = _both(oracle, data, q, 8, k=6, p=p)
+        np.testing.assert_allclose(g[0], o[0], rtol=1e-13, atol=0)
+        np.testing.assert_array_equal(g[1], o[1])
+
+
+def test_ties(oracle):
+    rng = np.random.default_rng(5)
+    data = rng.integers(0, 5, size=(20_000, 3)).astype(float)
+    q = rng.integers(0, 5, size=(500, 3)).astype(float)
+    for p in (1.0, 2.0, np.inf):
+        assert_bit_exact(*_both(oracle, data, q, 4, k=9, p=p))
+
+
+def test_single_query_shape(oracle):
+    from kdtree import KDTree
+
+    data = np.random.default_rng(1).normal(size=(100, 3))
+    d, i = KDTree(data).query(data[7], k=3)
+    assert d.shape == (3,) and i.shape == (3,) and i[0] == 7 and d[0] == 0.0
+
+
+def test_k_greater_than_points(oracle):
+    data = np.random.default_rng(1).normal(size=(5, 2))
+    g, o = _both(oracle, data, data[:3], 32, k=9)
+    assert_bit_exact(g, o)
+    assert (g[1][:, 5:] == 5).all() and np.isinf(g[0][:, 5:]).all()
+
+
+@pytest.mark.parametrize("dist", ["uniform", "gmm"])
+@pytest.mark.parametrize("k", [1, 16])
+@pytest.mark.parametrize("p", [1.0, 2.0, np.inf])
+def test_plain_scale_sampled(oracle, dist, k, p):
+    """N=1,000,000, d=3, leafsize 16 (data seed 2), 1,000,000 queries (seed 3):
+    all of them on the GPU; a 20,000-query sample bit-exact against the oracle,
+    and every result sorted, in range, and consistent with its own distances."""
+    from kdtree import KDTree
+
+    rd, rq = np.random.default_rng(2), np.random.default_rng(3)
+    if dist == "uniform":
+        data, q = rd.uniform(size=(1_000_000, 3)), rq.uniform(size=(1_000_000, 3))
+    else:
+        centres = np.random.default_rng(4).uniform(size=(64, 3))
+        data = centres[rd.integers(0, 64, 1_000_000)] + 0.01 * rd.standard_normal((1_000_000, 3))
+        q = centres[rq.integers(0, 64, 1_000_000)] + 0.01 * rq.standard_normal((1_000_000, 3))
+    t = KDTree(data, leafsize=16)
+    gd, gi = t.query(q, k=k, p=p)
+    assert np.all(np.diff(gd, axis=1) >= 0)
+    assert gi.min() >= 0 and gi.max() < 1_000_000
+    diff = np.abs(data[gi[:, 0]] - q)
+    ref0 = diff.max(1) if np.isinf(p) else (diff.sum(1) if p == 1 else np.sqrt((diff**2).sum(1)))
+    np.testing.assert_allclose(gd[:, 0], ref0, rtol=1e-12, atol=1e-15)
+    sel = np.random.default_rng(9).choice(1_000_000, 20_000, replace=False)
+    o = oracle.OracleKDTree(data, leafsize=16).query(q[sel], k=k, p=p, parallel=True)
+    assert_bit_exact((gd[sel], gi[sel]), o)

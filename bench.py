@@ -311,6 +311,7 @@ def main():
     cpu = None
     counts = None
     if not args.no_cpu and ws == 1:
+        sys.path.insert(0, str(ROOT / "oracle"))
         import kdtree_oracle
 
         threads = kdtree_oracle.max_threads()

@@ -5,7 +5,7 @@ split values and per-node boxes (src/build.rs, src/tree.rs, src/layout.rs).
 The cases cover the one-CTA shared-memory path (segments <= 8192 rows), the
 multi-CTA path of the top levels, the pivot-equal fix-up of partition_rows in
 both (duplicated coordinates), a root that is a leaf, leafsize 1, widths 1 to
-64, clustered data that sets order_by_box, and the parallel flag."""
+64, data on a line that sets order_by_box, and the parallel flag."""
 import zlib
 
 import numpy as np
@@ -42,7 +42,9 @@ CASES = {
     "d8": (lambda r: r.normal(size=(50_000, 8)), 16),
     "d17": (lambda r: r.normal(size=(20_000, 17)), 32),
     "d64": (lambda r: r.normal(size=(20_000, 64)) * np.exp(r.uniform(np.log(0.1), np.log(10), 64)), 16),
-    "gmm-order-by-box": (lambda r: gmm(100_000, 3, r), 16),
+    "gmm": (lambda r: gmm(100_000, 3, r), 16),
+    "diagonal-order-by-box": (lambda r: (lambda t: np.c_[t, t + 1e-3 * r.normal(size=t.size),
+                                                         t + 1e-3 * r.normal(size=t.size)])(r.uniform(size=60_000)), 16),
     "dups-small": (lambda r: r.integers(0, 4, size=(6000, 3)).astype(float), 4),
     "dups-large": (lambda r: r.integers(0, 3, size=(60_000, 3)).astype(float), 16),
     "dups-one-coordinate": (lambda r: np.c_[np.zeros(40_000), r.normal(size=40_000)], 16),
@@ -58,7 +60,7 @@ def test_build_layout_matches_oracle(oracle, name):
     make, leafsize = CASES[name]
     data = make(np.random.default_rng(zlib.crc32(name.encode())))
     g = _compare(oracle, data, leafsize)
-    if name == "gmm-order-by-box":
+    if name == "diagonal-order-by-box":
         assert (g[2][:, 3] >> 31).any(), "clustered data should set order_by_box somewhere"
 
 

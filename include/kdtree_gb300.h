@@ -86,6 +86,32 @@ int kd_query_device(const kd_tree* tree, const double* d_queries, uint64_t n_val
                     double p, int has_max_distance, double max_distance, double eps,
                     double* d_out_distances, int64_t* d_out_indices, void* stream);
 
+/* Largest n_values (n_queries * ndim) one kd_query_device_noalloc call takes. */
+#define KD_NOALLOC_MAX_VALUES 524256ull
+
+/* kd_query_device for callers that cannot allocate device memory.  This entry
+ * point has no counterpart in the reference; it exists for callers such as
+ * frameworks that reserve almost all device memory for their own pool (where an
+ * allocation from this library fails or fragments that pool) and latency-bound
+ * request loops that keep allocation out of their serving path.
+ *
+ * Same arguments, validation, results and synchronous return as
+ * kd_query_device, but no allocation of any kind: the per-call status word and
+ * the per-query CellBound scratch live in one fixed 4 MiB device array that is
+ * part of the library (every GPU that loads the library holds it until the
+ * process exits).  Hence:
+ *  - n_values must not exceed KD_NOALLOC_MAX_VALUES; larger calls fail with
+ *    KD_ERR_INVALID_ARGUMENT and a message, before any device work;
+ *  - every call on a device uses the same array, which keeps the last call's
+ *    contents (each call clears what must start at zero): calls whose work
+ *    overlaps on the GPU race, so issue them from one stream or serialise them;
+ *  - the first call on each device looks up the array's device address (a
+ *    one-time set-up with that device current); make that first call before any
+ *    stream capture. */
+int kd_query_device_noalloc(const kd_tree* tree, const double* d_queries, uint64_t n_values, uint64_t k,
+                            double p, int has_max_distance, double max_distance, double eps,
+                            double* d_out_distances, int64_t* d_out_indices, void* stream);
+
 /* Getters: `Tree::ndim`, `Tree::n_points`, `Tree::leafsize`
  * (src/tree.rs:48-58).  kd_n_nodes has no Python getter in the reference. */
 uint64_t kd_ndim(const kd_tree* tree);

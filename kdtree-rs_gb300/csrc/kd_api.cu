@@ -104,52 +104,6 @@ int validate_build(uint64_t n_values, uint64_t ndim, uint64_t leafsize, uint64_t
   return KD_OK;
 }
 
-// Scalar validation of Tree::query after the shape and finiteness checks
-// (query.rs:49-62, metric.rs:45-59).  Returns KD_OK and fills qp, or the status
-// with its message staged in *msg (the caller decides which error wins).
-int validate_scalars(uint64_t k, double p, int has_max, double max_distance, double eps, QueryParams* qp,
-                     std::string* msg) {
-  if (!std::isfinite(eps) || eps < 0.0) {
-    *msg = "eps must be finite and non-negative, got " + rust_f64(eps);
-    return KD_ERR_INVALID_EPS;
-  }
-  double md = has_max ? max_distance : INFINITY;
-  if (std::isnan(md) || md < 0.0) {
-    *msg = "max_distance must be finite and non-negative, or infinity, got " + rust_f64(md);
-    return KD_ERR_INVALID_MAX_DISTANCE;
-  }
-  int metric;
-  if (std::isinf(p) && p > 0) {
-    metric = M_LINF;
-  } else if (!std::isfinite(p) || p < 1.0) {
-    *msg = "p must be finite and >= 1, or infinity, got " + rust_f64(p);
-    return KD_ERR_INVALID_METRIC;
-  } else if (p == 1.0) {
-    metric = M_L1;
-  } else if (p == 2.0) {
-    metric = M_L2;
-  } else {
-    metric = M_LP;
-  }
-  auto reduce = [&](double x) {
-    if (metric == M_L2) return x * x;
-    if (metric == M_LP) return std::pow(x, p);
-    return x;
-  };
-  qp->metric = metric;
-  qp->p = p;
-  qp->cutoff = reduce(md);
-  if (qp->cutoff == 0.0) qp->cutoff = 0.0;  // -0 -> +0: compares equal, sorts as bits
-  qp->eps_factor = reduce(1.0 + eps);
-  qp->k = k;
-  return KD_OK;
-}
-
-__global__ void k_check_finite(const double* v, uint64_t n, uint32_t* status) {
-  uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
-  if (i < n && !isfinite(v[i])) atomicOr(status, 1u);
-}
-
 __global__ void k_original(const double* data, const uint32_t* idx, double* out, uint64_t n, uint64_t d) {
   uint64_t f = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
   if (f >= n * d) return;
@@ -271,6 +225,52 @@ int query_common(const kd_tree* t, const double* queries, bool on_device, uint64
 }
 
 }  // namespace
+
+// Scalar validation of Tree::query after the shape and finiteness checks
+// (query.rs:49-62, metric.rs:45-59).  Returns KD_OK and fills qp, or the status
+// with its message staged in *msg (the caller decides which error wins).
+int validate_scalars(uint64_t k, double p, int has_max, double max_distance, double eps, QueryParams* qp,
+                     std::string* msg) {
+  if (!std::isfinite(eps) || eps < 0.0) {
+    *msg = "eps must be finite and non-negative, got " + rust_f64(eps);
+    return KD_ERR_INVALID_EPS;
+  }
+  double md = has_max ? max_distance : INFINITY;
+  if (std::isnan(md) || md < 0.0) {
+    *msg = "max_distance must be finite and non-negative, or infinity, got " + rust_f64(md);
+    return KD_ERR_INVALID_MAX_DISTANCE;
+  }
+  int metric;
+  if (std::isinf(p) && p > 0) {
+    metric = M_LINF;
+  } else if (!std::isfinite(p) || p < 1.0) {
+    *msg = "p must be finite and >= 1, or infinity, got " + rust_f64(p);
+    return KD_ERR_INVALID_METRIC;
+  } else if (p == 1.0) {
+    metric = M_L1;
+  } else if (p == 2.0) {
+    metric = M_L2;
+  } else {
+    metric = M_LP;
+  }
+  auto reduce = [&](double x) {
+    if (metric == M_L2) return x * x;
+    if (metric == M_LP) return std::pow(x, p);
+    return x;
+  };
+  qp->metric = metric;
+  qp->p = p;
+  qp->cutoff = reduce(md);
+  if (qp->cutoff == 0.0) qp->cutoff = 0.0;  // -0 -> +0: compares equal, sorts as bits
+  qp->eps_factor = reduce(1.0 + eps);
+  qp->k = k;
+  return KD_OK;
+}
+
+__global__ void k_check_finite(const double* v, uint64_t n, uint32_t* status) {
+  uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  if (i < n && !isfinite(v[i])) atomicOr(status, 1u);
+}
 
 void set_error(const std::string& msg) { g_last_error = msg; }
 

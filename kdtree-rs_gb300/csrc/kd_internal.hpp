@@ -54,10 +54,24 @@ struct QueryParams {
   uint64_t k;
 };
 
+// Scalar validation of Tree::query (query.rs:49-62, metric.rs:45-59): KD_OK
+// and qp filled, or the status with its message in *msg.
+int validate_scalars(uint64_t k, double p, int has_max, double max_distance, double eps, QueryParams* qp,
+                     std::string* msg);
+
+// Sets bit 0 of *status when any of the n values is not finite.
+__global__ void k_check_finite(const double* v, uint64_t n, uint32_t* status);
+
 // Run the query on device buffers; `d_status` is a device word the kernels set
 // when a query is non-finite.  Work is ordered on `stream`.
 int query_on_device(const kd_tree* t, const double* d_queries, uint64_t n_queries,
                     const QueryParams& qp, double* d_out_d, int64_t* d_out_i,
                     cudaStream_t stream, uint32_t* d_status);
+
+// Same as query_on_device with the dynamic-width CellBound scratch supplied by
+// the caller (n_queries * ndim doubles); allocates nothing.
+int query_on_device_scratch(const kd_tree* t, const double* d_queries, uint64_t n_queries,
+                            const QueryParams& qp, double* d_out_d, int64_t* d_out_i,
+                            cudaStream_t stream, uint32_t* d_status, double* d_axes_scratch);
 
 }  // namespace kd

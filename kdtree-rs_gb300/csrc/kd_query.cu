@@ -609,4 +609,35 @@ int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, cons
   return rc;
 }
 
+int query_on_device_scratch(const kd_tree* t, const double* d_queries, uint64_t nq, const QueryParams& qp,
+                            double* d_out_d, int64_t* d_out_i, cudaStream_t st, uint32_t* d_status,
+                            double* d_axes_scratch) {
+  QArgs a{};
+  a.data = t->data;
+  a.data32 = t->data32;
+  a.indices = t->indices;
+  a.nodes = t->nodes;
+  a.boxes = t->boxes;
+  a.boxes32 = t->boxes32;
+  a.queries = d_queries;
+  a.out_d = d_out_d;
+  a.out_i = d_out_i;
+  a.status = d_status;
+  a.nq = nq;
+  a.d = t->ndim;
+  a.k = qp.k;
+  a.n_points = t->n_points;
+  a.p = qp.p;
+  a.cutoff = qp.cutoff;
+  a.eps_factor = qp.eps_factor;
+  a.use_eps = qp.eps_factor != 1.0;
+  a.axes_scratch = d_axes_scratch;
+  switch (qp.metric) {
+    case M_L1: return dispatch_d<M_L1>(a, st);
+    case M_L2: return dispatch_d<M_L2>(a, st);
+    case M_LINF: return dispatch_d<M_LINF>(a, st);
+    default: return dispatch_d<M_LP>(a, st);
+  }
+}
+
 }  // namespace kd

@@ -18,6 +18,8 @@
 // order.  A rejected point could never have been accepted, so the sequence of
 // accepted offers -- and every bound after them -- is unchanged.
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 
 #include "kd_internal.hpp"
 
@@ -41,6 +43,7 @@ struct QArgs {
   int64_t* out_i;         // nq * k
   double* axes_scratch;   // nq * d, dynamic-d CellBound (unused for static d)
   uint32_t* status;       // bit 0: non-finite query
+  const uint32_t* order;  // optional: thread t runs query order[t] (spatially sorted)
   uint64_t nq;
   uint64_t d;
   uint64_t k;
@@ -204,36 +207,93 @@ __device__ __forceinline__ double exact_box_dist(const QVec<D>& q, const double*
 }
 
 // ---------------------------------------------------------------------------
-// FP32 lower bounds with directed rounding.  data32 = RN(p) and q32 = RN(q)
-// satisfy |p - p32| <= 2^-24 |p32| + 2^-150 (likewise q), so per axis
-//   |p - q| >= |p32 - q32| - e,   e = 2^-24 (|p32| + |q32|) + 2^-149,
-// and every FP32 operation below rounds toward the safe side; non-finite FP32
-// values (overflowing inputs) collapse to a zero contribution.  The caller
-// rejects only when this bound exceeds an FP32 upper bound of the FP64 pruning
-// bound divided by (1 - 2^-40), which covers the FP64 rounding of the exact
-// distance (at most d + 2 relative roundings of 2^-53 each).
+// FP32 interval bounds with directed rounding.
+//
+// A double x is enclosed by FP32 values: q32 = RN(q) gives
+// q in [q32 - e, q32 + e], e = 2^-24 |q32| + 2^-149 (likewise the RN copies of
+// the points); a double converted through its bits (mag_dn32 / mag_up32) is
+// bracketed directly.  Interval sums, differences and squares rounded toward
+// the safe side give an FP32 lower bound lb and upper bound ub of the exact real
+// distance.  The FP64 value the reference computes from the same inputs is
+// within (d + 3) relative roundings of 2^-53 of that real value, so with the
+// FP64 pruning bound b enclosed as [b_lo, b_hi] = [b (1 - 2^-20), b (1 + 2^-20)]
+// (rounded outward):
+//   lb > b_hi  implies  exact > b   (the reference rejects: skip it),
+//   ub < b_lo  implies  exact <= b  (the reference admits: no FP64 needed),
+// and only the remaining cases compute the exact FP64 value.  Non-finite FP32
+// values (inputs beyond FP32 range) make lb 0 and ub inf, deciding nothing.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float axis_lb32(float p32, float q32) {
-  float hi = __fsub_ru(p32, q32), lo = __fsub_rd(p32, q32);
-  float a = lo > 0.f ? lo : (hi < 0.f ? -hi : 0.f);  // lower bound of |p32 - q32|
-  float e = __fadd_ru(__fmul_ru(__fadd_ru(fabsf(p32), fabsf(q32)), 5.9604645e-08f /* 2^-24 */),
-                      1.4e-45f /* 2^-149 */);
-  float t = __fsub_rd(a, e);
-  return t > 0.f ? t : 0.f;  // NaN (inf - inf) also lands on 0
-}
+constexpr float TWO_M24 = 5.9604645e-08f;  // 2^-24
+constexpr float TWO_M23 = 1.1920929e-07f;  // 2^-23
+constexpr float TINY32 = 1.4e-45f;         // 2^-149
+constexpr float LB_SHRINK = 0.99999905f;   // 1 - 2^-20 (exact in FP32)
+constexpr float UB_GROW = 1.0000010f;      // 1 + 2^-20 (exact in FP32)
 
+// |x| of a double given by its bits, rounded down / up to FP32.
+__device__ __forceinline__ float mag_dn32(uint64_t b) {
+  b &= 0x7fffffffffffffffull;
+  const int e = static_cast<int>(b >> 52) - 896;  // FP32 biased exponent
+  if ((b >> 52) == 0x7ff) return (b & 0xfffffffffffffull) ? 0.f : __int_as_float(0x7f800000);
+  if (e >= 255) return 3.40282347e38f;
+  if (e <= 0) return 0.f;
+  return __uint_as_float((static_cast<uint32_t>(e) << 23) | static_cast<uint32_t>((b >> 29) & 0x7fffffu));
+}
+__device__ __forceinline__ float mag_up32(uint64_t b) {
+  b &= 0x7fffffffffffffffull;
+  if (b == 0) return 0.f;
+  const int e = static_cast<int>(b >> 52) - 896;
+  if (e >= 255) return __int_as_float(0x7f800000);
+  if (e <= 0) return 1.17549435e-38f;  // FLT_MIN bounds everything below it
+  uint32_t r = (static_cast<uint32_t>(e) << 23) | static_cast<uint32_t>((b >> 29) & 0x7fffffu);
+  if (b & 0x1fffffffull) r += 1;  // carries into the exponent (or to +inf) correctly
+  return __uint_as_float(r);
+}
+// Signed double (bits) rounded down / up to FP32.
+__device__ __forceinline__ float rd32(uint64_t b) { return (b >> 63) ? -mag_up32(b) : mag_dn32(b); }
+__device__ __forceinline__ float ru32(uint64_t b) { return (b >> 63) ? -mag_dn32(b) : mag_up32(b); }
+
+// Enclosure [lo, hi] of a double whose FP32 round-to-nearest copy is x32.
+__device__ __forceinline__ void rn_enclose(float x32, float* lo, float* hi) {
+  const float e = __fmaf_ru(fabsf(x32), TWO_M24, TINY32);
+  *lo = __fsub_rd(x32, e);
+  *hi = __fadd_ru(x32, e);
+}
+// Lower / upper bound of |x - y| for x in [xl, xh], y in [yl, yh].
+__device__ __forceinline__ float absdiff_lb(float xl, float xh, float yl, float yh) {
+  const float a = __fsub_rd(xl, yh), b = __fsub_rd(yl, xh);
+  const float m = a > b ? a : b;
+  return m > 0.f ? m : 0.f;  // NaN lands on 0
+}
+__device__ __forceinline__ float absdiff_ub(float xl, float xh, float yl, float yh) {
+  const float a = __fsub_ru(xh, yl), b = __fsub_ru(yh, xl);
+  return fmaxf(fmaxf(a, b), 0.f);
+}
 template <int M>
-__device__ __forceinline__ float acc_lb32(float acc, float t) {
-  if (M == M_L2) return __fadd_rd(acc, __fmul_rd(t, t));
-  if (M == M_L1) return __fadd_rd(acc, t);
-  return acc > t ? acc : t;  // LINF
+__device__ __forceinline__ float red_lb(float t) {  // reduce(), rounded down
+  return M == M_L2 ? __fmul_rd(t, t) : t;
+}
+template <int M>
+__device__ __forceinline__ float red_ub(float t) {
+  return M == M_L2 ? __fmul_ru(t, t) : t;
+}
+template <int M>
+__device__ __forceinline__ float fold_lb(float acc, float t) {  // fold(), rounded down
+  if (M == M_LINF) return acc > t ? acc : t;
+  return __fadd_rd(acc, t);
+}
+template <int M>
+__device__ __forceinline__ float fold_ub(float acc, float t) {
+  if (M == M_LINF) return fmaxf(acc, t);
+  return __fadd_ru(acc, t);
 }
 
-// FP32 upper bound of a non-negative FP64 bound, inflated so that rejecting
-// lb32 > ub32 implies exact_fp64 > bound.  +inf stays +inf (never rejects).
-__device__ __forceinline__ float bound_ub32(double b) {
-  float f = __double2float_ru(b);
-  return __fmul_ru(f, 1.0000002f);
+// dist <= bound for a non-negative bound given by its bits, with dist of any
+// sign: a cell bound fl(fl(cell - old) + far_axis) can round slightly below
+// zero, which f64 '<=' admits; NaN never is.
+__device__ __forceinline__ bool leq_bound(double dist, uint64_t bound_bits) {
+  const uint64_t b = dbits(dist);
+  if (b >> 63) return (b & 0x7fffffffffffffffull) <= INF_BITS;
+  return b <= bound_bits;
 }
 
 // ---------------------------------------------------------------------------
@@ -285,13 +345,24 @@ struct Frame {
   double y;       // the pending child's box distance (F_BOX_*)
 };
 
+// The IEEE order of finite doubles as an unsigned key (-0 folded onto +0), so
+// the near-child test q[dim] <= split (query.rs:263-268) is an integer compare.
+__device__ __forceinline__ uint64_t ieee_key(uint64_t b) {
+  uint64_t k = total_key_bits(b);
+  return k == 0x7fffffffffffffffull ? 0x8000000000000000ull : k;
+}
+
 template <int M, int D, int K>
 __global__ void __launch_bounds__(QUERY_THREADS) k_query(QArgs a) {
-  const uint64_t qi = blockIdx.x * static_cast<uint64_t>(QUERY_THREADS) + threadIdx.x;
-  if (qi >= a.nq) return;
+  const uint64_t tid = blockIdx.x * static_cast<uint64_t>(QUERY_THREADS) + threadIdx.x;
+  if (tid >= a.nq) return;
+  const uint64_t qi = a.order ? a.order[tid] : tid;
   const uint64_t d = D > 0 ? D : a.d;
   const double pexp = a.p;
   const int strat = (M != M_LP && d <= 8) ? S_PACKED : ((M == M_L1 || M == M_L2) && d <= 16 ? S_FOLDED : S_STREAMED);
+  // FP32 interval gates: compile-time widths, metrics without pow(), eps = 0.
+  constexpr bool FAST = D > 0 && M != M_LP;
+  const bool gates = FAST && !a.use_eps;
 
   QVec<D> q;
   q.g = a.queries + qi * d;
@@ -309,12 +380,25 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query(QArgs a) {
     atomicOr(a.status, 1u);
     return;
   }
-  // FP32 copy of the query for the filters (static widths only)
-  float q32[D > 0 ? D : 1];
+  // FP32 enclosures and IEEE keys of the query (compile-time widths only)
+  float qlo[D > 0 ? D : 1], qhi[D > 0 ? D : 1];
+  uint64_t qkey[D > 0 ? D : 1];
   if (D > 0) {
 #pragma unroll
-    for (int i = 0; i < D; ++i) q32[i] = __double2float_rn(q.v[i]);
+    for (int i = 0; i < D; ++i) {
+      rn_enclose(__double2float_rn(q.v[i]), &qlo[i], &qhi[i]);
+      qkey[i] = ieee_key(dbits(q.v[i]));
+    }
   }
+  auto qkey_of = [&](uint32_t j) -> uint64_t {
+    if (D > 0) {
+      uint64_t v = 0;
+#pragma unroll
+      for (int i = 0; i < D; ++i) v = (static_cast<uint32_t>(i) == j) ? qkey[i] : v;
+      return v;
+    }
+    return ieee_key(dbits(q.g[j]));
+  };
 
   // CellBound axes (query.rs:156-211)
   double axes_r[D > 0 ? D : 1];
@@ -350,31 +434,40 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query(QArgs a) {
     uint64_t w = best.worst();
     return w < cutoff_bits ? w : cutoff_bits;
   };
-  auto admits_at = [&](double dist, uint64_t bnd) -> bool {
+  // FP32 enclosure of the current bound, refreshed whenever it changes
+  uint64_t bnd = bound_bits();
+  float b_hi = __fmul_ru(mag_up32(bnd), UB_GROW);
+  float b_lo = __fmul_rd(mag_dn32(bnd), LB_SHRINK);
+  auto refresh_bound = [&]() {
+    bnd = bound_bits();
+    b_hi = __fmul_ru(mag_up32(bnd), UB_GROW);
+    b_lo = __fmul_rd(mag_dn32(bnd), LB_SHRINK);
+  };
+  auto admits_at = [&](double dist, uint64_t bb) -> bool {
     if (a.use_eps) dist = dmul(dist, a.eps_factor);
-    return dbits(dist) <= bnd;  // NaN bit patterns sort above +inf: never admitted
+    return leq_bound(dist, bb);
   };
 
-  // Box gate: FP32 lower bound first; exact FP64 box distance only if needed.
-  auto box_admits = [&](uint32_t id, uint64_t bnd) -> bool {
-    if (D > 0 && M != M_LP) {
+  // Far-child box gate (query.rs:283): interval bounds first, exact FP64 box
+  // distance (kernel.rs:565-616) only when they cannot decide.
+  auto box_admits = [&](uint32_t id) -> bool {
+    if (gates) {
       const float* b32 = a.boxes32 + static_cast<uint64_t>(id) * 2 * D;
-      float lb = 0.f;
+      float lb = 0.f, ub = 0.f;
 #pragma unroll
       for (int i = 0; i < D; ++i) {
-        // offset lower bound: max(lo - q, q - hi, 0) with lo / hi rounded outward
-        float o1 = __fsub_rd(b32[i], q32[i]);
-        float o2 = __fsub_rd(q32[i], b32[D + i]);
-        float o = o1 > o2 ? o1 : o2;
-        o = o > 0.f ? o : 0.f;
-        float e = __fmul_ru(fabsf(q32[i]), 5.9604645e-08f);
-        o = __fsub_rd(o, e);
-        o = o > 0.f ? o : 0.f;
-        lb = acc_lb32<M>(lb, o);
+        // lo in [lo32, lo32 + ulp], hi in [hi32 - ulp, hi32]: outward-rounded copies
+        const float lo32 = b32[i], hi32 = b32[D + i];
+        const float lo_up = __fadd_ru(lo32, __fmaf_ru(fabsf(lo32), TWO_M23, TINY32));
+        const float hi_dn = __fsub_rd(hi32, __fmaf_ru(fabsf(hi32), TWO_M23, TINY32));
+        float o_lb = fmaxf(__fsub_rd(lo32, qhi[i]), __fsub_rd(qlo[i], hi32));
+        o_lb = o_lb > 0.f ? o_lb : 0.f;
+        const float o_ub = fmaxf(fmaxf(__fsub_ru(lo_up, qlo[i]), __fsub_ru(qhi[i], hi_dn)), 0.f);
+        lb = fold_lb<M>(lb, red_lb<M>(o_lb));
+        ub = fold_ub<M>(ub, red_ub<M>(o_ub));
       }
-      float ub = bound_ub32(bitsd(bnd));
-      if (a.use_eps) ub = __fdiv_ru(ub, __double2float_rd(a.eps_factor));
-      if (lb > ub) return false;
+      if (lb > b_hi) return false;
+      if (ub < b_lo) return true;
     }
     double bd = exact_box_dist<M, D>(q, a.boxes + static_cast<uint64_t>(id) * 2 * d, d, pexp);
     return admits_at(bd, bnd);
@@ -382,28 +475,29 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query(QArgs a) {
 
   // scan_leaf + Strategy::scan + LeafSink (query.rs:343-375, kernel.rs:366-562)
   auto scan_leaf = [&](uint32_t start, uint32_t end) {
-    uint64_t bnd = bound_bits();
     const uint32_t len = end - start;
     uint32_t chunk_pts = len;
     if (strat == S_PACKED && M != M_LINF) {
       if (d == 4) chunk_pts = len / 2 * 2;
       else if (d == 8) chunk_pts = len / 8 * 8;
     }
-    float ub = bound_ub32(bitsd(bnd));
     for (uint32_t j = 0; j < len; ++j) {
       const uint64_t row = static_cast<uint64_t>(start) + j;
-      if (D > 0 && M != M_LP) {
+      if (FAST) {
         const float* p32 = a.data32 + row * D;
         float lb = 0.f;
 #pragma unroll
-        for (int i = 0; i < D; ++i) lb = acc_lb32<M>(lb, axis_lb32(p32[i], q32[i]));
-        if (lb > ub) continue;  // exact distance > bound: never offered
+        for (int i = 0; i < D; ++i) {
+          float plo, phi;
+          rn_enclose(p32[i], &plo, &phi);
+          lb = fold_lb<M>(lb, red_lb<M>(absdiff_lb(plo, phi, qlo[i], qhi[i])));
+        }
+        if (lb > b_hi) continue;  // exact distance > bound: never offered
       }
       double dist = exact_dist<M, D>(q, a.data + row * d, d, strat, j < chunk_pts, pexp);
       if (dbits(dist) <= bnd) {
         best.consider(dbits(dist), a.indices[row]);
-        bnd = bound_bits();
-        ub = bound_ub32(bitsd(bnd));
+        refresh_bound();
       }
     }
   };
@@ -425,7 +519,7 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query(QArgs a) {
   int sp = 0;
   uint32_t node = 0;
   double cell = seed;
-  bool descending = admits_at(seed, bound_bits());
+  bool descending = admits_at(seed, bnd);
 
   for (;;) {
     while (descending) {
@@ -438,8 +532,8 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query(QArgs a) {
         break;
       }
       const uint32_t dim = nd.meta & KD_NODE_DIM_MASK;
-      const double diff = dsub(q[dim], nd.split);
-      const bool left_near = diff <= 0.0;
+      // diff <= 0  <=>  q[dim] <= split (exact for finite doubles)
+      const bool left_near = qkey_of(dim) <= ieee_key(dbits(nd.split));
       const uint32_t near = left_near ? node + 1 : nd.right;
       const uint32_t far = left_near ? nd.right : node + 1;
       if (nd.meta & KD_NODE_BOX_ORDER) {
@@ -448,7 +542,7 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query(QArgs a) {
         double far_box = exact_box_dist<M, D>(q, a.boxes + static_cast<uint64_t>(far) * 2 * d, d, pexp);
         if (dbits(near_box) <= dbits(far_box)) {
           stack[sp++] = Frame{node, F_BOX_FAR, cell, far_box};
-          if (admits_at(near_box, bound_bits())) {
+          if (admits_at(near_box, bnd)) {
             node = near;
             continue;
           }
@@ -456,8 +550,8 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query(QArgs a) {
           break;
         }
         stack[sp++] = Frame{node, F_BOX_NEAR, cell, near_box};
-        if (admits_at(far_box, bound_bits())) {
-          const double far_axis = reduce<M>(fabs(diff), pexp);
+        if (admits_at(far_box, bnd)) {
+          const double far_axis = reduce<M>(fabs(dsub(q[dim], nd.split)), pexp);
           const double old = axis_get(dim);
           const double far_dist = (M == M_LINF) ? max_nn(cell, far_axis) : dadd(dsub(cell, old), far_axis);
           stack[sp++] = Frame{dim, F_RESTORE, old, 0.0};
@@ -482,27 +576,49 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query(QArgs a) {
       }
       const DNode nd = a.nodes[f.node];
       const uint32_t dim = nd.meta & KD_NODE_DIM_MASK;
-      const double diff = dsub(q[dim], nd.split);
-      const bool left_near = diff <= 0.0;
+      const bool left_near = qkey_of(dim) <= ieee_key(dbits(nd.split));
       const uint32_t near = left_near ? f.node + 1 : nd.right;
       const uint32_t far = left_near ? nd.right : f.node + 1;
       if (f.kind == F_BOX_NEAR) {
-        if (admits_at(f.y, bound_bits())) {
+        if (admits_at(f.y, bnd)) {
           node = near;
           cell = f.x;
           resumed = true;
         }
         continue;
       }
-      const uint64_t bnd = bound_bits();
-      const double far_axis = reduce<M>(fabs(diff), pexp);
       const double old = axis_get(dim);
-      const double far_dist = (M == M_LINF) ? max_nn(f.x, far_axis) : dadd(dsub(f.x, old), far_axis);
-      bool enter;
-      if (f.kind == F_BOX_FAR)
-        enter = admits_at(f.y, bnd);
-      else
-        enter = admits_at(far_dist, bnd) && box_admits(far, bnd);
+      if (f.kind == F_BOX_FAR) {
+        if (!admits_at(f.y, bnd)) continue;
+      }
+      // far_dist = replace_axis(cell, old, reduce(|diff|)) (metric.rs:93-98).
+      // c = cell - old is the first FP64 step; the plane gate is first decided
+      // on c and an FP32 lower bound of reduce(|diff|).
+      const double c = (M == M_LINF) ? f.x : dsub(f.x, old);
+      if (gates && f.kind == F_FAR) {
+        float slo = rd32(dbits(nd.split)), shi = ru32(dbits(nd.split));
+        float qlo_d = 0.f, qhi_d = 0.f;
+#pragma unroll
+        for (int i = 0; i < (D > 0 ? D : 1); ++i)
+          if (static_cast<uint32_t>(i) == dim) {
+            qlo_d = qlo[i];
+            qhi_d = qhi[i];
+          }
+        const float fa_lb = __fmul_rd(red_lb<M>(absdiff_lb(qlo_d, qhi_d, slo, shi)), LB_SHRINK);
+        float lb;
+        if (M == M_LINF) {
+          const float c_lb = mag_dn32(dbits(c));
+          lb = c_lb > fa_lb ? c_lb : fa_lb;
+        } else {
+          lb = __fadd_rd(rd32(dbits(c)), fa_lb);
+          lb = lb > 0.f ? __fmul_rd(lb, LB_SHRINK) : lb;
+        }
+        if (lb > b_hi) continue;  // plane bound already above the bound
+      }
+      const double far_axis = reduce<M>(fabs(dsub(q[dim], nd.split)), pexp);
+      const double far_dist = (M == M_LINF) ? max_nn(c, far_axis) : dadd(c, far_axis);
+      bool enter = true;
+      if (f.kind == F_FAR) enter = admits_at(far_dist, bnd) && box_admits(far);
       if (enter) {
         // enter_far (query.rs:329-341)
         stack[sp++] = Frame{dim, F_RESTORE, old, 0.0};
@@ -534,9 +650,134 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query(QArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Spatial ordering of a batch: each query's landing leaf (where its descent
+// first arrives: left iff q[dim] <= split, query.rs:263-268), then a counting
+// sort by that leaf's preorder id.  Queries that share a leaf then share a warp
+// and follow nearly the same descent.  The order changes no result.
+// ---------------------------------------------------------------------------
+__global__ void k_landing_leaf(const DNode* nodes, const double* queries, uint64_t nq, uint64_t d,
+                               uint32_t* leaf_of, uint32_t* counts) {
+  uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  if (i >= nq) return;
+  const double* q = queries + i * d;
+  uint32_t node = 0;
+  for (;;) {
+    const DNode nd = nodes[node];
+    if (nd.meta & KD_NODE_LEAF) break;
+    node = (q[nd.meta & KD_NODE_DIM_MASK] <= nd.split) ? node + 1 : nd.right;
+  }
+  leaf_of[i] = node;
+  atomicAdd(&counts[node], 1u);
+}
+
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__device__ uint32_t block_scan_excl(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t warp_sums[SCAN_THREADS / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = warp_sums[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    warp_sums[lane] = w;
+  }
+  __syncthreads();
+  const uint32_t off = warp ? warp_sums[warp - 1] : 0;
+  *total = warp_sums[SCAN_THREADS / 32 - 1];
+  __syncthreads();
+  return off + x - v;
+}
+
+// Exclusive scan of a[0, n) in place: per-tile scan, tile sums, offsets.
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(uint32_t* a, uint64_t n, uint32_t* tile_sums) {
+  const uint64_t base = blockIdx.x * static_cast<uint64_t>(SCAN_TILE) + threadIdx.x * SCAN_ITEMS;
+  uint32_t v[SCAN_ITEMS], s = 0;
+#pragma unroll
+  for (int j = 0; j < SCAN_ITEMS; ++j) {
+    v[j] = (base + j < n) ? a[base + j] : 0;
+    s += v[j];
+  }
+  uint32_t total;
+  uint32_t run = block_scan_excl(s, &total);
+#pragma unroll
+  for (int j = 0; j < SCAN_ITEMS; ++j) {
+    if (base + j < n) a[base + j] = run;
+    run += v[j];
+  }
+  if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_sums(uint32_t* sums, uint64_t n_tiles) {
+  __shared__ uint32_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (uint64_t b = 0; b < n_tiles; b += SCAN_THREADS) {
+    uint64_t i = b + threadIdx.x;
+    uint32_t v = i < n_tiles ? sums[i] : 0, total;
+    uint32_t ex = block_scan_excl(v, &total);
+    const uint32_t c = carry;
+    if (i < n_tiles) sums[i] = c + ex;
+    __syncthreads();
+    if (threadIdx.x == 0) carry = c + total;
+    __syncthreads();
+  }
+}
+
+__global__ void k_scan_add(uint32_t* a, uint64_t n, const uint32_t* tile_sums) {
+  const uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  if (i < n) a[i] += tile_sums[i / SCAN_TILE];
+}
+
+__global__ void k_scatter_order(const uint32_t* leaf_of, uint32_t* offsets, uint64_t nq, uint32_t* order) {
+  uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  if (i >= nq) return;
+  order[atomicAdd(&offsets[leaf_of[i]], 1u)] = static_cast<uint32_t>(i);
+}
+
+// Below this many queries the ordering costs more than it saves.
+constexpr uint64_t ORDER_MIN_QUERIES = 4096;
+
+#include "kd_lazy_best.cuh"
+#include "kd_query_fast.cuh"
+#include "kd_query_packet.cuh"
+
+// KD_QUERY_MODE=dfs runs every query through the reference-order descent (the
+// eps > 0 kernel) instead of the packet traversal; a diagnostic switch, same results.
+bool force_reference_order() {
+  static const bool force = [] {
+    const char* m = std::getenv("KD_QUERY_MODE");
+    return m && std::strcmp(m, "dfs") == 0;
+  }();
+  return force;
+}
+
 template <int M, int D, int K>
 int launch(const QArgs& a, cudaStream_t st) {
   const unsigned blocks = static_cast<unsigned>((a.nq + QUERY_THREADS - 1) / QUERY_THREADS);
+  if constexpr (D > 0 && M != M_LP) {
+    if (a.n_points < ROW_NONE) {
+      if (!a.use_eps && !force_reference_order())
+        k_query_packet<M, D, K><<<blocks, QUERY_THREADS, 0, st>>>(a);
+      else
+        k_query_fast<M, D, K><<<blocks, QUERY_THREADS, 0, st>>>(a);
+      KD_TRY_CUDA(cudaGetLastError());
+      return KD_OK;
+    }
+  }
   k_query<M, D, K><<<blocks, QUERY_THREADS, 0, st>>>(a);
   KD_TRY_CUDA(cudaGetLastError());
   return KD_OK;
@@ -598,6 +839,29 @@ int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, cons
     }
     a.axes_scratch = static_cast<double*>(axes);
   }
+  void* sort_mem = nullptr;
+  if (nq >= ORDER_MIN_QUERIES && nq < 0xffffffffull) {
+    const uint64_t n_tiles = (t->n_nodes + SCAN_TILE - 1) / SCAN_TILE;
+    const uint64_t words = 2 * nq + t->n_nodes + n_tiles;
+    cudaError_t e = cudaMallocAsync(&sort_mem, words * sizeof(uint32_t), st);
+    if (e == cudaSuccess) {
+      uint32_t* leaf_of = static_cast<uint32_t*>(sort_mem);
+      uint32_t* order = leaf_of + nq;
+      uint32_t* counts = order + nq;
+      uint32_t* tile_sums = counts + t->n_nodes;
+      cudaMemsetAsync(counts, 0, t->n_nodes * sizeof(uint32_t), st);
+      const unsigned qb = static_cast<unsigned>((nq + 255) / 256);
+      k_landing_leaf<<<qb, 256, 0, st>>>(t->nodes, d_queries, nq, t->ndim, leaf_of, counts);
+      k_scan_tiles<<<static_cast<unsigned>(n_tiles), SCAN_THREADS, 0, st>>>(counts, t->n_nodes, tile_sums);
+      k_scan_sums<<<1, SCAN_THREADS, 0, st>>>(tile_sums, n_tiles);
+      k_scan_add<<<static_cast<unsigned>((t->n_nodes + 255) / 256), 256, 0, st>>>(counts, t->n_nodes, tile_sums);
+      k_scatter_order<<<qb, 256, 0, st>>>(leaf_of, counts, nq, order);
+      a.order = order;
+    } else {
+      cudaGetLastError();  // run unordered: same results, less coherence
+      sort_mem = nullptr;
+    }
+  }
   int rc;
   switch (qp.metric) {
     case M_L1: rc = dispatch_d<M_L1>(a, st); break;
@@ -606,6 +870,7 @@ int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, cons
     default: rc = dispatch_d<M_LP>(a, st); break;
   }
   if (axes) cudaFreeAsync(axes, st);
+  if (sort_mem) cudaFreeAsync(sort_mem, st);
   return rc;
 }
 

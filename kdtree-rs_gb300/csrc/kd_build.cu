@@ -30,6 +30,7 @@
 // memory; larger ones (the top levels) by grids of CTAs over row chunks with
 // global histograms, counts and scans.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -1018,7 +1019,14 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
       din, static_cast<float*>(data32.p), n * d, reinterpret_cast<const double*>(boxes.p),
       static_cast<float*>(boxes32.p), n_nodes, d);
   KD_TRY_CUDA(cudaGetLastError());
+  std::vector<double> root_box(2 * d);
+  KD_TRY_CUDA(cudaMemcpyAsync(root_box.data(), boxes.p, 2 * d * sizeof(double), cudaMemcpyDeviceToHost, st));
   KD_TRY_CUDA(cudaStreamSynchronize(st));
+  double cmax = 0.0;  // the root box holds every coordinate
+  for (double v : root_box) cmax = std::max(cmax, std::fabs(v));
+  float cmax32 = static_cast<float>(cmax);
+  while (static_cast<double>(cmax32) < cmax) cmax32 = std::nextafter(cmax32, INFINITY);
+  t->coord_max32 = cmax32;
 
   t->n_points = n;
   t->ndim = d;

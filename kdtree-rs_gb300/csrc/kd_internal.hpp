@@ -23,6 +23,7 @@ struct kd_tree {
   double* boxes = nullptr;      // n_nodes * 2 * ndim, [lo | hi] per node
   float* data32 = nullptr;      // n_points * ndim, round-to-nearest FP32 copy (filters)
   float* boxes32 = nullptr;     // n_nodes * 2 * ndim, [lo rounded down | hi rounded up]
+  float coord_max32 = 0.f;      // FP32 upper bound of every |coordinate| (the root box)
 };
 
 namespace kd {

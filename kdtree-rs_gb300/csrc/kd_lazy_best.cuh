@@ -200,3 +200,219 @@ __device__ __forceinline__ float box_lb(const float* b32, const float* qlo, cons
   }
   return __fmul_rd(lb, LB_SHRINK);
 }
+
+// ---------------------------------------------------------------------------
+// LazySet: the same k best as LazyBest (BestK keeps the k smallest by
+// (distance, index), query.rs:461-481 -- a set under a strict total order),
+// held unsorted: while slots are empty a candidate fills one (the reference
+// inserts unconditionally then); afterwards an accepted candidate replaces the
+// worst slot, and the k survivors are sorted by their exact (distance, index)
+// once, at the end.  Used by the packet traversal, where offers arrive in no
+// particular order.  Placeholders (k < K) are [-inf, -inf]; empty slots are
+// [+inf, +inf] with row ROW_NONE.
+// ---------------------------------------------------------------------------
+template <int M, int D, int K>
+struct LazySet {
+  float lo[K], hi[K];
+  uint32_t row[K];
+  uint32_t chunk;    // bit j: slot j's point lies in a full Packed d8 chunk
+  uint32_t n_empty;  // empty real slots
+  int worst;         // an empty slot, else the slot with the largest hi
+  float max_lo;      // the k-th exact distance is >= max_lo (when full)
+  float second_hi;   // largest hi among the other slots
+  float b_lo, b_hi;  // enclosure of the pruning bound min(k-th best, cutoff)
+  float cut_lo, cut_hi;
+  uint64_t cut_bits;
+  const QVec<D>* q;
+  const double* data;
+  const uint32_t* indices;
+
+  __device__ __forceinline__ void init(uint64_t k, double cutoff, const QVec<D>* qv, const double* data_,
+                                       const uint32_t* indices_) {
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const bool pad = static_cast<uint64_t>(j) < K - k;
+      lo[j] = pad ? __int_as_float(0xff800000) : __int_as_float(0x7f800000);
+      hi[j] = lo[j];
+      row[j] = ROW_NONE;
+    }
+    chunk = 0;
+    n_empty = static_cast<uint32_t>(k);
+    cut_bits = dbits(cutoff);
+    cut_lo = mag_dn32(cut_bits);
+    cut_hi = mag_up32(cut_bits);
+    q = qv;
+    data = data_;
+    indices = indices_;
+    rescan();
+  }
+  __device__ __forceinline__ bool is_empty(int j) const {
+    return row[j] == ROW_NONE && lo[j] > 0.f;  // placeholders have lo = -inf
+  }
+  // worst, max_lo, second_hi and the bound enclosure after a change
+  __device__ __forceinline__ void rescan() {
+    float mh = __int_as_float(0xff800000), sh = mh, ml = mh;
+    int w = 0, first_empty = -1;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const bool g = hi[j] > mh || (j == 0);
+      sh = g ? mh : fmaxf(sh, hi[j]);
+      mh = g ? hi[j] : mh;
+      w = g ? j : w;
+      ml = fmaxf(ml, lo[j]);
+      first_empty = (first_empty < 0 && is_empty(j)) ? j : first_empty;
+    }
+    if (n_empty) {
+      w = first_empty;
+      mh = __int_as_float(0x7f800000);
+      ml = mh;
+    }
+    worst = w;
+    max_lo = ml;
+    second_hi = sh;
+    b_lo = fminf(ml, cut_lo);
+    b_hi = fminf(mh, cut_hi);
+  }
+  __device__ __forceinline__ double exact_of(uint32_t r, bool in_chunk) const {
+    return exact_dist<M, D>(*q, data + static_cast<uint64_t>(r) * D, D, S_PACKED, in_chunk, 0.0);
+  }
+  __device__ __forceinline__ float slot_lo(int w) const {
+    float v = lo[0];
+#pragma unroll
+    for (int j = 1; j < K; ++j) v = (j == w) ? lo[j] : v;
+    return v;
+  }
+  __device__ __forceinline__ float slot_hi(int w) const {
+    float v = hi[0];
+#pragma unroll
+    for (int j = 1; j < K; ++j) v = (j == w) ? hi[j] : v;
+    return v;
+  }
+
+  // The worst slot exactly (full list): the largest (exact distance, index)
+  // among the slots whose enclosure reaches max_lo -- no other slot can be it.
+  __device__ void resolve_worst(double* wx, uint32_t* wid) {
+    const float ml = max_lo;
+    uint64_t best_bits = 0;
+    uint32_t best_id = 0;
+    int best_j = -1;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      if (hi[j] >= ml && row[j] != ROW_NONE) {
+        const double x = exact_of(row[j], (chunk >> j) & 1u);
+        const uint32_t id = indices[row[j]];
+        lo[j] = mag_dn32(dbits(x));  // keep the tighter enclosure
+        hi[j] = mag_up32(dbits(x));
+        const bool g = best_j < 0 || dbits(x) > best_bits || (dbits(x) == best_bits && id > best_id);
+        best_bits = g ? dbits(x) : best_bits;
+        best_id = g ? id : best_id;
+        best_j = g ? j : best_j;
+      }
+    }
+    rescan();
+    worst = best_j;
+    *wx = bitsd(best_bits);
+    *wid = best_id;
+  }
+
+  // exact bound min(k-th best, cutoff) as bits (query.rs:452-459)
+  __device__ uint64_t bound_exact() {
+    if (n_empty) return cut_bits;  // not full: the k-th best is +inf
+    double wx;
+    uint32_t wid;
+    resolve_worst(&wx, &wid);
+    const uint64_t kb = dbits(wx);
+    return kb < cut_bits ? kb : cut_bits;
+  }
+
+  // Offer the point at tree row r whose exact distance lies in [clo, chi].
+  __device__ __forceinline__ void offer(float clo, float chi, uint32_t r, bool in_chunk) {
+    double cx = 0.0;
+    bool have_x = false;
+    if (!(chi <= cut_lo)) {  // the cutoff test, unless clearly inside
+      if (clo > cut_hi) return;
+      cx = exact_of(r, in_chunk);
+      have_x = true;
+      if (dbits(cx) > cut_bits) return;
+    }
+    if (n_empty == 0) {
+      const float wlo = slot_lo(worst), whi = slot_hi(worst);
+      const bool definite = second_hi < wlo;  // no other enclosure reaches the worst's
+      if (definite && clo > whi) return;      // after the worst: not kept
+      if (chi < max_lo) {                     // before the worst, whichever slot it is
+        if (!definite) {
+          double wx;
+          uint32_t wid;
+          resolve_worst(&wx, &wid);
+        }
+      } else {  // too close to call on enclosures
+        double wx;
+        uint32_t wid;
+        resolve_worst(&wx, &wid);
+        if (!have_x) cx = exact_of(r, in_chunk);
+        const uint32_t cid = indices[r];
+        if (!(dbits(cx) < dbits(wx) || (dbits(cx) == dbits(wx) && cid < wid))) return;
+        clo = mag_dn32(dbits(cx));
+        chi = mag_up32(dbits(cx));
+      }
+    } else {
+      --n_empty;
+    }
+    const int w = worst;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const bool m = j == w;
+      lo[j] = m ? clo : lo[j];
+      hi[j] = m ? chi : hi[j];
+      row[j] = m ? r : row[j];
+    }
+    if (D == 8) chunk = (chunk & ~(1u << w)) | (static_cast<uint32_t>(in_chunk) << w);
+    rescan();
+  }
+
+  // write_results (query.rs:421-429, 483-493): the exact values sorted by
+  // (distance, index); empty slots after every real one.
+  __device__ __forceinline__ void write(double* od, int64_t* oi, uint64_t k, uint64_t n_points) const {
+    uint64_t xb[K];
+    uint32_t id[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      if (static_cast<uint64_t>(j) < K - k) {  // placeholder: sorts first
+        xb[j] = 0;
+        id[j] = 0;
+      } else if (row[j] == ROW_NONE) {  // empty: sorts last
+        xb[j] = ~0ull;
+        id[j] = NO_ID;
+      } else {
+        xb[j] = dbits(exact_of(row[j], (chunk >> j) & 1u)) + 1;
+        id[j] = indices[row[j]];
+      }
+    }
+#pragma unroll
+    for (int i = 1; i < K; ++i) {
+#pragma unroll
+      for (int j = i; j > 0; --j) {
+        const bool sw = xb[j] < xb[j - 1] || (xb[j] == xb[j - 1] && id[j] < id[j - 1]);
+        const uint64_t tx = xb[j];
+        const uint32_t ti = id[j];
+        xb[j] = sw ? xb[j - 1] : xb[j];
+        id[j] = sw ? id[j - 1] : id[j];
+        xb[j - 1] = sw ? tx : xb[j - 1];
+        id[j - 1] = sw ? ti : id[j - 1];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      if (static_cast<uint64_t>(j) >= K - k) {
+        const uint64_t o = j - (K - k);
+        if (xb[j] != ~0ull) {
+          od[o] = restore<M>(bitsd(xb[j] - 1), 0.0);
+          oi[o] = static_cast<int64_t>(id[j]);
+        } else {
+          od[o] = bitsd(INF_BITS);
+          oi[o] = static_cast<int64_t>(n_points);
+        }
+      }
+    }
+  }
+};

@@ -38,6 +38,7 @@ struct QArgs {
   const DNode* nodes;
   const double* boxes;    // [lo | hi] per node
   const float* boxes32;   // outward-rounded FP32 boxes
+  float coord_max;        // >= every |coordinate| of the tree, FP32
   const double* queries;  // nq * d
   double* out_d;          // nq * k
   int64_t* out_i;         // nq * k
@@ -817,6 +818,7 @@ int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, cons
   a.nodes = t->nodes;
   a.boxes = t->boxes;
   a.boxes32 = t->boxes32;
+  a.coord_max = t->coord_max32;
   a.queries = d_queries;
   a.out_d = d_out_d;
   a.out_i = d_out_i;
@@ -884,6 +886,7 @@ int query_on_device_scratch(const kd_tree* t, const double* d_queries, uint64_t 
   a.nodes = t->nodes;
   a.boxes = t->boxes;
   a.boxes32 = t->boxes32;
+  a.coord_max = t->coord_max32;
   a.queries = d_queries;
   a.out_d = d_out_d;
   a.out_i = d_out_i;

@@ -7,7 +7,7 @@
 // node is entered when at least one lane's rigorous FP32 lower bound of the
 // exact box distance does not exceed that lane's pruning bound; its children are
 // visited near side first by majority vote.  At a leaf every lane that needs it
-// offers each point to its own k-best list (LazyBest: FP32 enclosures of the
+// offers each point to its own k-best set (LazySet: FP32 enclosures of the
 // reference's exact FP64 distances, exact FP64 only when enclosures overlap).
 //
 // Each lane's result is the k smallest (exact FP64 reduced distance in the
@@ -22,6 +22,75 @@
 #pragma once
 
 constexpr int PACKET_STACK = 2 * KD_MAX_DEPTH;
+
+// Cheap rigorous point filter.  With a = p32 - q32 (exact reals) and every
+// coordinate within E = 2^-24 (|coordinate bound| + |q|) + 2^-148 of its FP32
+// copy, the triangle inequality gives |p - q| >= |a| - sqrt(d) E (L2; d E for L1,
+// E for L-inf), and the round-to-nearest FP32 sum s over-estimates |a| (squared
+// for L2) by at most (d + 3) 2^-24 relative.  So s > T(b) with
+//   T(b) = (1 + 2^-20) (sqrt(b) + sqrt(d) E)^2 + d 2^-148   (L2),
+//   T(b) = (1 + 2^-20) (b + d E) + d 2^-148                (L1),
+//   T(b) = (1 + 2^-20) (b + E) + 2^-148                    (L-inf),
+// all rounded up, proves the exact distance exceeds b.  NaN never rejects.
+template <int M, int D>
+struct PointFilter {
+  float q32[D];
+  float spread;
+  __device__ __forceinline__ void init(const QVec<D>& q, float coord_max) {
+    float qmax = 0.f;
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      q32[i] = __double2float_rn(q.v[i]);
+      qmax = fmaxf(qmax, fabsf(q32[i]));
+    }
+    const float e = __fmaf_ru(__fadd_ru(coord_max, qmax), TWO_M24, 2.9e-45f /* 2^-148 */);
+    spread = (M == M_L2) ? __fmul_ru(e, __fsqrt_ru(static_cast<float>(D)))
+                         : (M == M_L1 ? __fmul_ru(e, static_cast<float>(D)) : e);
+  }
+  __device__ __forceinline__ float threshold(float b) const {
+    constexpr float abs_slack = D * 2.9e-45f;
+    if (M == M_L2) {
+      const float r = __fadd_ru(__fsqrt_ru(b), spread);
+      return __fadd_ru(__fmul_ru(__fmul_ru(r, r), UB_GROW), abs_slack);
+    }
+    return __fadd_ru(__fmul_ru(__fadd_ru(b, spread), UB_GROW), abs_slack);
+  }
+  // Enclosure [clo, chi] of the exact FP64 distance from the same sum s: |a|
+  // within 2^-19 of s * rsqrt(s) (rsqrtf: 2 ulp; s: (d + 3) 2^-24), then the
+  // spread and the FP64 roundings, as above.
+  __device__ __forceinline__ void enclose(float s, float* clo, float* chi) const {
+    float lo, hi;
+    if (M == M_L2) {
+      const float r = s > 0.f ? s * rsqrtf(s) : 0.f;
+      if (!(r <= 3.4e38f)) {  // overflow or NaN: no information
+        *clo = 0.f;
+        *chi = __int_as_float(0x7f800000);
+        return;
+      }
+      lo = fmaxf(__fsub_rd(__fmul_rd(r, 0.99999809f /* 1 - 2^-19 */), spread), 0.f);
+      hi = __fadd_ru(__fmul_ru(r, 1.0000020f /* 1 + 2^-19 */), spread);
+      lo = __fmul_rd(lo, lo);
+      hi = __fmul_ru(hi, hi);
+    } else {
+      lo = fmaxf(__fsub_rd(__fmul_rd(s, 0.99999809f), spread), 0.f);
+      hi = __fadd_ru(__fmul_ru(s, 1.0000020f), spread);
+      if (!(s <= 3.4e38f)) hi = __int_as_float(0x7f800000);
+    }
+    *clo = __fmul_rd(lo, LB_SHRINK);
+    *chi = __fmul_ru(hi, UB_GROW);
+  }
+  __device__ __forceinline__ float sum(const float* p32) const {
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      const float t = __fsub_rn(p32[i], q32[i]);
+      if (M == M_L2) s = __fmaf_rn(t, t, s);
+      else if (M == M_L1) s = __fadd_rn(s, fabsf(t));
+      else s = fmaxf(s, fabsf(t));
+    }
+    return s;
+  }
+};
 
 template <int M, int D, int K>
 __global__ void __launch_bounds__(QUERY_THREADS) k_query_packet(QArgs a) {
@@ -45,15 +114,14 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query_packet(QArgs a) {
     for (int i = 0; i < D; ++i) q.v[i] = 0.0;
   }
   float qlo[D], qhi[D];
-  uint64_t qkey[D];
 #pragma unroll
-  for (int i = 0; i < D; ++i) {
-    rn_enclose(__double2float_rn(q.v[i]), &qlo[i], &qhi[i]);
-    qkey[i] = ieee_key(dbits(q.v[i]));
-  }
+  for (int i = 0; i < D; ++i) rn_enclose(__double2float_rn(q.v[i]), &qlo[i], &qhi[i]);
+  PointFilter<M, D> filt;
+  filt.init(q, a.coord_max);
 
-  LazyBest<M, D, K> best;
+  LazySet<M, D, K> best;
   best.init(a.k, a.cutoff, &q, a.data, a.indices);
+  float thr = filt.threshold(best.b_hi);
 
   uint32_t stack[PACKET_STACK];  // identical in every lane
   int sp = 0;
@@ -69,19 +137,39 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query_packet(QArgs a) {
       const uint64_t se = dbits(nd.split);
       const uint32_t start = static_cast<uint32_t>(se), end = static_cast<uint32_t>(se >> 32);
       const uint32_t chunk_end = (D == 8 && M != M_LINF) ? start + (end - start) / 8 * 8 : end;
-      for (uint32_t r = start; r < end; ++r) {
-        float clo, chi;
-        LazyBest<M, D, K>::point_enclosure(a.data32 + static_cast<uint64_t>(r) * D, qlo, qhi, &clo, &chi);
-        if (need && !(clo > best.b_hi)) best.offer(clo, chi, r, r < chunk_end);
+      for (uint32_t c0 = start; c0 < end; c0 += 32) {
+        const uint32_t c1 = min(end, c0 + 32);
+        // 1. which of these points can this lane's bound admit?
+        uint32_t pending = 0;
+        for (uint32_t r = c0; r < c1; ++r) {
+          const float s = filt.sum(a.data32 + static_cast<uint64_t>(r) * D);
+          if (need && !(s > thr)) pending |= 1u << (r - c0);
+        }
+        // 2. offer them, all lanes with a pending point together
+        while (__any_sync(0xffffffffu, pending != 0)) {
+          if (pending) {
+            const uint32_t r = c0 + __ffs(pending) - 1;
+            pending &= pending - 1;
+            const float sr = filt.sum(a.data32 + static_cast<uint64_t>(r) * D);
+            if (!(sr > thr)) {  // the bound may have tightened meanwhile
+              float clo, chi;
+              filt.enclose(sr, &clo, &chi);
+              if (!(clo > best.b_hi)) {
+                best.offer(clo, chi, r, r < chunk_end);
+                thr = filt.threshold(best.b_hi);
+              }
+            }
+          }
+        }
       }
       continue;
     }
     // near child first, by majority of the lanes that need this node
     const uint32_t dim = nd.meta & KD_NODE_DIM_MASK;
-    uint64_t qk = qkey[0];
+    double qd = q.v[0];
 #pragma unroll
-    for (int i = 1; i < D; ++i) qk = (static_cast<uint32_t>(i) == dim) ? qkey[i] : qk;
-    const bool left = qk <= ieee_key(dbits(nd.split));
+    for (int i = 1; i < D; ++i) qd = (static_cast<uint32_t>(i) == dim) ? q.v[i] : qd;
+    const bool left = ieee_key(dbits(qd)) <= ieee_key(dbits(nd.split));
     const uint32_t left_votes = __popc(__ballot_sync(0xffffffffu, need && left));
     const bool left_first = 2 * left_votes >= static_cast<uint32_t>(__popc(need_mask));
     stack[sp++] = left_first ? nd.right : node + 1;

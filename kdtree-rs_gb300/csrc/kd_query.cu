@@ -337,6 +337,41 @@ struct BestList {
   }
 };
 
+// k > 32: the same sorted list held in the query's own output row (distance
+// bits in the distance slots, indices in the index slots), shifted in memory.
+template <>
+struct BestList<0> {
+  uint64_t* dist;
+  int64_t* id;
+  uint64_t k;
+  __device__ __forceinline__ void bind(double* od, int64_t* oi, uint64_t kk) {
+    dist = reinterpret_cast<uint64_t*>(od);
+    id = oi;
+    k = kk;
+  }
+  __device__ __forceinline__ void reset(uint64_t) {
+    for (uint64_t j = 0; j < k; ++j) {
+      dist[j] = INF_BITS;
+      id[j] = NO_ID;
+    }
+  }
+  __device__ __forceinline__ uint64_t worst() const { return dist[k - 1]; }
+  __device__ __forceinline__ static bool lt(uint64_t da, uint32_t ia, uint64_t db, uint32_t ib) {
+    return da < db || (da == db && ia < ib);
+  }
+  __device__ void consider(uint64_t dd, uint32_t ii) {
+    if (!lt(dd, ii, dist[k - 1], static_cast<uint32_t>(id[k - 1]))) return;
+    uint64_t pos = k - 1;
+    while (pos > 0 && lt(dd, ii, dist[pos - 1], static_cast<uint32_t>(id[pos - 1]))) {
+      dist[pos] = dist[pos - 1];
+      id[pos] = id[pos - 1];
+      --pos;
+    }
+    dist[pos] = dd;
+    id[pos] = ii;
+  }
+};
+
 // Stack frames of the iterative descent.
 enum FrameKind : uint32_t { F_FAR = 0, F_RESTORE = 1, F_BOX_FAR = 2, F_BOX_NEAR = 3 };
 struct Frame {
@@ -430,6 +465,7 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query(QArgs a) {
 
   const uint64_t cutoff_bits = dbits(a.cutoff);
   BestList<K> best;
+  if constexpr (K == 0) best.bind(a.out_d + qi * a.k, a.out_i + qi * a.k, a.k);
   best.reset(a.k);
   auto bound_bits = [&]() -> uint64_t {
     uint64_t w = best.worst();
@@ -636,6 +672,17 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query(QArgs a) {
   // write_results (query.rs:421-429, 483-493)
   double* od = a.out_d + qi * a.k;
   int64_t* oi = a.out_i + qi * a.k;
+  if constexpr (K == 0) {
+    for (uint64_t j = 0; j < a.k; ++j) {  // convert the in-place list
+      if (oi[j] != static_cast<int64_t>(NO_ID)) {
+        od[j] = restore<M>(od[j], pexp);
+      } else {
+        od[j] = __longlong_as_double(0x7ff0000000000000ll);
+        oi[j] = static_cast<int64_t>(a.n_points);
+      }
+    }
+    return;
+  }
 #pragma unroll
   for (int j = 0; j < K; ++j) {
     if (static_cast<uint64_t>(j) >= K - a.k) {
@@ -769,7 +816,7 @@ bool force_reference_order() {
 template <int M, int D, int K>
 int launch(const QArgs& a, cudaStream_t st) {
   const unsigned blocks = static_cast<unsigned>((a.nq + QUERY_THREADS - 1) / QUERY_THREADS);
-  if constexpr (D > 0 && M != M_LP) {
+  if constexpr (D > 0 && M != M_LP && K > 0) {
     if (a.n_points < ROW_NONE) {
       if (!a.use_eps && !force_reference_order())
         k_query_packet<M, D, K><<<blocks, QUERY_THREADS, 0, st>>>(a);
@@ -791,7 +838,7 @@ int dispatch_k(const QArgs& a, cudaStream_t st) {
   if (a.k <= 8) return launch<M, D, 8>(a, st);
   if (a.k <= 16) return launch<M, D, 16>(a, st);
   if (a.k <= 32) return launch<M, D, 32>(a, st);
-  return fail(KD_ERR_INVALID_ARGUMENT, "k > 32 is not supported by this query path");
+  return launch<M, D, 0>(a, st);
 }
 
 template <int M>

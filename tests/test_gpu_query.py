@@ -117,3 +117,20 @@ def test_plain_scale_sampled(oracle, dist, k, p):
     sel = np.random.default_rng(9).choice(1_000_000, 20_000, replace=False)
     o = oracle.OracleKDTree(data, leafsize=16).query(q[sel], k=k, p=p, parallel=True)
     assert_bit_exact((gd[sel], gi[sel]), o)
+
+
+@pytest.mark.parametrize("d,p", [(3, 2.0), (5, 1.0), (8, np.inf), (17, 2.0)])
+@pytest.mark.parametrize("k", [33, 64, 150])
+def test_large_k(oracle, d, p, k):
+    """k beyond the register lists: the list lives in the query's output row."""
+    rng = np.random.default_rng(k + d)
+    data = rng.normal(size=(4000, d))
+    q = rng.normal(size=(300, d))
+    assert_bit_exact(*_both(oracle, data, q, 16, k=k, p=p))
+
+
+def test_k_far_beyond_n(oracle):
+    data = np.random.default_rng(3).normal(size=(40, 3))
+    g, o = _both(oracle, data, data[:10] + 0.01, 8, k=100)
+    assert_bit_exact(g, o)
+    assert (g[1][:, 40:] == 40).all()

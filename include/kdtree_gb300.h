@@ -86,6 +86,31 @@ int kd_query_device(const kd_tree* tree, const double* d_queries, uint64_t n_val
                     double p, int has_max_distance, double max_distance, double eps,
                     double* d_out_distances, int64_t* d_out_indices, void* stream);
 
+/* Query kernels kd_query_device_path can be asked for.  No reference
+ * counterpart: the reference has one CPU descent; these are the engine's
+ * implementations of it, for measurement and cross-checking.
+ *   KD_PATH_AUTO            what kd_query / kd_query_device run
+ *   KD_PATH_REFERENCE_ORDER one thread per query, the reference's depth-first
+ *                           order (FP64 decisions; the only order for eps > 0)
+ *   KD_PATH_PACKET          warp-shared traversal (d in {2, 3, 8}, eps = 0)
+ *   KD_PATH_TENSOR_CORE     tcgen05 BF16 distance filter + FP64 re-rank
+ *                           (L2, eps = 0, 16 <= d <= 128, k <= 32)
+ * A path that does not apply to a call falls back to the reference order. */
+enum kd_query_path {
+  KD_PATH_AUTO = 0,
+  KD_PATH_REFERENCE_ORDER = 1,
+  KD_PATH_PACKET = 2,
+  KD_PATH_TENSOR_CORE = 3
+};
+
+/* kd_query_device with the kernel chosen by `path` (see kd_query_path).
+ * `d_survivors`, when not NULL, is a device counter to which the
+ * tensor-core path adds the (query, point) pairs its filter could not reject. */
+int kd_query_device_path(const kd_tree* tree, const double* d_queries, uint64_t n_values, uint64_t k,
+                         double p, int has_max_distance, double max_distance, double eps,
+                         double* d_out_distances, int64_t* d_out_indices, void* stream, int path,
+                         unsigned long long* d_survivors);
+
 /* Largest n_values (n_queries * ndim) one kd_query_device_noalloc call takes. */
 #define KD_NOALLOC_MAX_VALUES 524256ull
 

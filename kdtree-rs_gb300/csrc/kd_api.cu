@@ -144,6 +144,10 @@ void free_tree(kd_tree* t) {
   cudaFree(t->boxes);
   cudaFree(t->data32);
   cudaFree(t->boxes32);
+  cudaFree(t->tc_points);
+  cudaFree(t->tc_w);
+  cudaFree(t->tc_v);
+  cudaFree(t->tc_centre);
   delete t;
 }
 
@@ -167,7 +171,7 @@ struct DevMem {
 
 int query_common(const kd_tree* t, const double* queries, bool on_device, uint64_t n_values, uint64_t k,
                  double p, int has_max, double max_distance, double eps, double* out_d, int64_t* out_i,
-                 cudaStream_t st) {
+                 cudaStream_t st, int path = PATH_AUTO, unsigned long long* d_survivors = nullptr) {
   if (!t) return fail(KD_ERR_INVALID_ARGUMENT, "tree is NULL");
   if (k == 0) return fail(KD_ERR_INVALID_K, "k must be greater than zero");
   if (n_values == 0 || n_values % t->ndim)
@@ -199,6 +203,7 @@ int query_common(const kd_tree* t, const double* queries, bool on_device, uint64
     return fail(scalar, msg);
   }
   if (k > (~0ull / sizeof(double)) / nq) return fail(KD_ERR_OUT_OF_MEMORY, "output would not fit in memory");
+  qp.path = path;
   const double* dq = queries;
   double* dd = out_d;
   int64_t* di = out_i;
@@ -212,7 +217,7 @@ int query_common(const kd_tree* t, const double* queries, bool on_device, uint64
     dd = static_cast<double*>(md.p);
     di = static_cast<int64_t*>(mi.p);
   }
-  if ((rc = query_on_device(t, dq, nq, qp, dd, di, st, static_cast<uint32_t*>(status.p)))) return rc;
+  if ((rc = query_on_device(t, dq, nq, qp, dd, di, st, static_cast<uint32_t*>(status.p), d_survivors))) return rc;
   uint32_t h = 0;
   KD_TRY_CUDA(cudaMemcpyAsync(&h, status.p, sizeof h, cudaMemcpyDeviceToHost, st));
   if (!on_device) {
@@ -220,6 +225,7 @@ int query_common(const kd_tree* t, const double* queries, bool on_device, uint64
     KD_TRY_CUDA(cudaMemcpyAsync(out_i, di, nq * k * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   }
   KD_TRY_CUDA(cudaStreamSynchronize(st));
+  if (h & 2u) return fail(KD_ERR_CUDA, "the tensor-core pipeline timed out waiting on a barrier");
   if (h) return fail(KD_ERR_NONFINITE_DATA, "all coordinates must be finite");
   return KD_OK;
 }
@@ -366,6 +372,14 @@ int kd_query_device(const kd_tree* tree, const double* d_queries, uint64_t n_val
                     int64_t* d_out_indices, void* stream) {
   return query_common(tree, d_queries, true, n_values, k, p, has_max_distance, max_distance, eps,
                       d_out_distances, d_out_indices, static_cast<cudaStream_t>(stream));
+}
+
+int kd_query_device_path(const kd_tree* tree, const double* d_queries, uint64_t n_values, uint64_t k, double p,
+                         int has_max_distance, double max_distance, double eps, double* d_out_distances,
+                         int64_t* d_out_indices, void* stream, int path, unsigned long long* d_survivors) {
+  if (path < KD_PATH_AUTO || path > KD_PATH_TENSOR_CORE) return fail(KD_ERR_INVALID_ARGUMENT, "unknown query path");
+  return query_common(tree, d_queries, true, n_values, k, p, has_max_distance, max_distance, eps, d_out_distances,
+                      d_out_indices, static_cast<cudaStream_t>(stream), path, d_survivors);
 }
 
 uint64_t kd_ndim(const kd_tree* t) { return t ? t->ndim : 0; }

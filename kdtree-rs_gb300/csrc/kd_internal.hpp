@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstdint>
+#include <mutex>
 #include <string>
 
 #include <cuda_runtime.h>
@@ -24,6 +25,14 @@ struct kd_tree {
   float* data32 = nullptr;      // n_points * ndim, round-to-nearest FP32 copy (filters)
   float* boxes32 = nullptr;     // n_nodes * 2 * ndim, [lo rounded down | hi rounded up]
   float coord_max32 = 0.f;      // FP32 upper bound of every |coordinate| (the root box)
+  // Tensor-core filter inputs, made on first use (guarded by tc_mutex):
+  // centred BF16 rows padded to tc_dpad, and the per-point filter terms.
+  std::mutex tc_mutex;
+  uint16_t* tc_points = nullptr;  // n_points x tc_dpad BF16 of (p - centre)
+  float* tc_w = nullptr;          // per point: |p_b|^2 (1 - 2^-12) - v^2, rounded down
+  float* tc_v = nullptr;          // per point: 2^-8 |p_b|, rounded up
+  double* tc_centre = nullptr;    // ndim, the root box centre
+  uint32_t tc_dpad = 0;
 };
 
 namespace kd {
@@ -47,7 +56,12 @@ int build_on_device(const double* d_src, uint64_t n_points, uint64_t ndim, uint6
                     cudaStream_t stream, kd_tree* t);
 
 // Parameters of one query call after validation (src/query.rs:38-62).
+// Which query kernel runs (kd_query_device_path): the automatic choice, the
+// reference-order descent, the packet traversal, or the tensor-core filter.
+enum QueryPath : int { PATH_AUTO = 0, PATH_REFERENCE_ORDER = 1, PATH_PACKET = 2, PATH_TENSOR_CORE = 3 };
+
 struct QueryParams {
+  int path = PATH_AUTO;
   int metric;         // MetricKind
   double p;           // exponent (LP only)
   double cutoff;      // reduce(max_distance), -0 normalised to +0
@@ -67,12 +81,21 @@ __global__ void k_check_finite(const double* v, uint64_t n, uint32_t* status);
 // when a query is non-finite.  Work is ordered on `stream`.
 int query_on_device(const kd_tree* t, const double* d_queries, uint64_t n_queries,
                     const QueryParams& qp, double* d_out_d, int64_t* d_out_i,
-                    cudaStream_t stream, uint32_t* d_status);
+                    cudaStream_t stream, uint32_t* d_status, unsigned long long* d_survivors = nullptr);
 
 // Same as query_on_device with the dynamic-width CellBound scratch supplied by
 // the caller (n_queries * ndim doubles); allocates nothing.
 int query_on_device_scratch(const kd_tree* t, const double* d_queries, uint64_t n_queries,
                             const QueryParams& qp, double* d_out_d, int64_t* d_out_i,
                             cudaStream_t stream, uint32_t* d_status, double* d_axes_scratch);
+
+// Exact k-NN through the tensor-core filter (L2, eps = 0, 16 <= d <= 128,
+// k <= 32).  Returns KD_OK, or KD_ERR_INVALID_ARGUMENT without doing anything
+// when the case is outside that envelope.  `d_survivors`, if not NULL,
+// accumulates the number of (query, point) pairs the filter could not reject.
+int query_tc_on_device(kd_tree* t, const double* d_queries, uint64_t n_queries, const QueryParams& qp,
+                       double* d_out_d, int64_t* d_out_i, cudaStream_t stream, uint32_t* d_status,
+                       unsigned long long* d_survivors);
+bool tc_applicable(const kd_tree* t, const QueryParams& qp);
 
 }  // namespace kd

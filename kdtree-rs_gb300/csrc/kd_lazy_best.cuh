@@ -416,3 +416,194 @@ struct LazySet {
     }
   }
 };
+
+// ---------------------------------------------------------------------------
+// Runtime-width variants (the tensor-core filter path, 16 <= d <= 128):
+// the exact FP64 value follows the reference's Folded (d <= 16) or Streamed
+// (d > 16) L2 order (kernel.rs:343-354, 177-188) from the query in memory.
+// ---------------------------------------------------------------------------
+struct DynPoint {
+  const double* q;     // the query, FP64
+  const double* data;  // tree-ordered points, FP64
+  uint64_t d;
+  int strat;
+  __device__ __forceinline__ double exact(uint32_t r) const {
+    QVec<0> qv;
+    qv.g = q;
+    return exact_dist<M_L2, 0>(qv, data + static_cast<uint64_t>(r) * d, d, strat, false, 0.0);
+  }
+};
+
+template <int K>
+struct LazySetDyn {
+  float lo[K], hi[K];
+  uint32_t row[K];
+  uint32_t n_empty;
+  int worst;
+  float max_lo, second_hi;
+  float b_lo, b_hi;
+  float cut_lo, cut_hi;
+  uint64_t cut_bits;
+  DynPoint pt;
+  const uint32_t* indices;
+
+  __device__ __forceinline__ void init(uint64_t k, double cutoff, DynPoint p, const uint32_t* indices_) {
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const bool pad = static_cast<uint64_t>(j) < K - k;
+      lo[j] = pad ? __int_as_float(0xff800000) : __int_as_float(0x7f800000);
+      hi[j] = lo[j];
+      row[j] = ROW_NONE;
+    }
+    n_empty = static_cast<uint32_t>(k);
+    cut_bits = dbits(cutoff);
+    cut_lo = mag_dn32(cut_bits);
+    cut_hi = mag_up32(cut_bits);
+    pt = p;
+    indices = indices_;
+    rescan();
+  }
+  __device__ __forceinline__ bool is_empty(int j) const { return row[j] == ROW_NONE && lo[j] > 0.f; }
+  __device__ __forceinline__ void rescan() {
+    float mh = __int_as_float(0xff800000), sh = mh, ml = mh;
+    int w = 0, first_empty = -1;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const bool g = hi[j] > mh || (j == 0);
+      sh = g ? mh : fmaxf(sh, hi[j]);
+      mh = g ? hi[j] : mh;
+      w = g ? j : w;
+      ml = fmaxf(ml, lo[j]);
+      first_empty = (first_empty < 0 && is_empty(j)) ? j : first_empty;
+    }
+    if (n_empty) {
+      w = first_empty;
+      mh = __int_as_float(0x7f800000);
+      ml = mh;
+    }
+    worst = w;
+    max_lo = ml;
+    second_hi = sh;
+    b_lo = fminf(ml, cut_lo);
+    b_hi = fminf(mh, cut_hi);
+  }
+  __device__ __forceinline__ float slot_lo(int w) const {
+    float v = lo[0];
+#pragma unroll
+    for (int j = 1; j < K; ++j) v = (j == w) ? lo[j] : v;
+    return v;
+  }
+  __device__ __forceinline__ float slot_hi(int w) const {
+    float v = hi[0];
+#pragma unroll
+    for (int j = 1; j < K; ++j) v = (j == w) ? hi[j] : v;
+    return v;
+  }
+  __device__ void resolve_worst(double* wx, uint32_t* wid) {
+    const float ml = max_lo;
+    uint64_t best_bits = 0;
+    uint32_t best_id = 0;
+    int best_j = -1;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {  // static indices keep the slots in registers
+      if (hi[j] >= ml && row[j] != ROW_NONE) {
+        const double x = pt.exact(row[j]);
+        const uint32_t id = indices[row[j]];
+        lo[j] = mag_dn32(dbits(x));
+        hi[j] = mag_up32(dbits(x));
+        const bool g = best_j < 0 || dbits(x) > best_bits || (dbits(x) == best_bits && id > best_id);
+        best_bits = g ? dbits(x) : best_bits;
+        best_id = g ? id : best_id;
+        best_j = g ? j : best_j;
+      }
+    }
+    rescan();
+    worst = best_j;
+    *wx = bitsd(best_bits);
+    *wid = best_id;
+  }
+  __device__ void offer(float clo, float chi, uint32_t r) {
+    double cx = 0.0;
+    bool have_x = false;
+    if (!(chi <= cut_lo)) {
+      if (clo > cut_hi) return;
+      cx = pt.exact(r);
+      have_x = true;
+      if (dbits(cx) > cut_bits) return;
+    }
+    if (n_empty == 0) {
+      const float wlo = slot_lo(worst), whi = slot_hi(worst);
+      const bool definite = second_hi < wlo;
+      if (definite && clo > whi) return;
+      if (chi < max_lo) {
+        if (!definite) {
+          double wx;
+          uint32_t wid;
+          resolve_worst(&wx, &wid);
+        }
+      } else {
+        double wx;
+        uint32_t wid;
+        resolve_worst(&wx, &wid);
+        if (!have_x) cx = pt.exact(r);
+        const uint32_t cid = indices[r];
+        if (!(dbits(cx) < dbits(wx) || (dbits(cx) == dbits(wx) && cid < wid))) return;
+        clo = mag_dn32(dbits(cx));
+        chi = mag_up32(dbits(cx));
+      }
+    } else {
+      --n_empty;
+    }
+    const int w = worst;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const bool m = j == w;
+      lo[j] = m ? clo : lo[j];
+      hi[j] = m ? chi : hi[j];
+      row[j] = m ? r : row[j];
+    }
+    rescan();
+  }
+  // exact values of the k best, sorted by (distance, index), written out
+  __device__ void write(double* od, int64_t* oi, uint64_t k, uint64_t n_points) const {
+    uint64_t xb[K];
+    uint32_t id[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      if (static_cast<uint64_t>(j) < K - k) {
+        xb[j] = 0;
+        id[j] = 0;
+      } else if (row[j] == ROW_NONE) {
+        xb[j] = ~0ull;
+        id[j] = NO_ID;
+      } else {
+        xb[j] = dbits(pt.exact(row[j])) + 1;
+        id[j] = indices[row[j]];
+      }
+    }
+    for (int i = 1; i < K; ++i) {
+      const uint64_t tx = xb[i];
+      const uint32_t ti = id[i];
+      int j = i;
+      while (j > 0 && (tx < xb[j - 1] || (tx == xb[j - 1] && ti < id[j - 1]))) {
+        xb[j] = xb[j - 1];
+        id[j] = id[j - 1];
+        --j;
+      }
+      xb[j] = tx;
+      id[j] = ti;
+    }
+    for (int j = 0; j < K; ++j) {
+      if (static_cast<uint64_t>(j) >= K - k) {
+        const uint64_t o = j - (K - k);
+        if (xb[j] != ~0ull) {
+          od[o] = __dsqrt_rn(bitsd(xb[j] - 1));
+          oi[o] = static_cast<int64_t>(id[j]);
+        } else {
+          od[o] = bitsd(INF_BITS);
+          oi[o] = static_cast<int64_t>(n_points);
+        }
+      }
+    }
+  }
+};

@@ -27,275 +27,7 @@ namespace kd {
 
 namespace {
 
-constexpr uint32_t NO_ID = 0xffffffffu;
-constexpr uint64_t INF_BITS = 0x7ff0000000000000ull;
-constexpr int QUERY_THREADS = 128;
-
-struct QArgs {
-  const double* data;     // tree order, n * d
-  const float* data32;    // FP32 copy
-  const uint32_t* indices;
-  const DNode* nodes;
-  const double* boxes;    // [lo | hi] per node
-  const float* boxes32;   // outward-rounded FP32 boxes
-  float coord_max;        // >= every |coordinate| of the tree, FP32
-  const double* queries;  // nq * d
-  double* out_d;          // nq * k
-  int64_t* out_i;         // nq * k
-  double* axes_scratch;   // nq * d, dynamic-d CellBound (unused for static d)
-  uint32_t* status;       // bit 0: non-finite query
-  const uint32_t* order;  // optional: thread t runs query order[t] (spatially sorted)
-  uint64_t nq;
-  uint64_t d;
-  uint64_t k;
-  uint64_t n_points;
-  double p;               // LP exponent
-  double cutoff;          // reduced max_distance, >= +0
-  double eps_factor;
-  int use_eps;            // eps_factor != 1
-};
-
-// ---------------------------------------------------------------------------
-// Metric algebra (src/metric.rs:64-98), exact.
-// ---------------------------------------------------------------------------
-template <int M>
-__device__ __forceinline__ double reduce(double x, double p) {
-  if (M == M_L2) return dmul(x, x);
-  if (M == M_LP) return pow(x, p);
-  return x;
-}
-template <int M>
-__device__ __forceinline__ double restore(double x, double p) {
-  if (M == M_L2) return __dsqrt_rn(x);
-  if (M == M_LP) return pow(x, 1.0 / p);
-  return x;
-}
-template <int M>
-__device__ __forceinline__ double axis_of(double delta) {  // axes_lanes (kernel.rs:22-29)
-  return M == M_L2 ? dmul(delta, delta) : fabs(delta);
-}
-__device__ __forceinline__ double hsum8(const double* v) {  // src/simd.rs:26-30
-  return dadd(dadd(dadd(v[0], v[4]), dadd(v[2], v[6])), dadd(dadd(v[1], v[5]), dadd(v[3], v[7])));
-}
-__device__ __forceinline__ double max_nn(double a, double b) { return b > a ? b : a; }
-// axis_offset (src/layout.rs:147-149)
-__device__ __forceinline__ double axis_offset(double q, double lo, double hi) {
-  double a = dsub(lo, q), b = dsub(q, hi);
-  double m = a > b ? a : b;
-  return m > 0.0 ? m : 0.0;
-}
-
-// Query coordinates: registers for a compile-time width, global otherwise.
-template <int D>
-struct QVec {
-  double v[D > 0 ? D : 1];
-  const double* g;
-  __device__ __forceinline__ double operator[](uint64_t i) const {
-    if (D > 0) return v[i];
-    return g[i];
-  }
-};
-
-// ---------------------------------------------------------------------------
-// Exact reduced point distance (src/kernel.rs:163-218, 343-354, 411-562).
-// `in_chunk`: the point lies inside a full Packed chunk of its leaf (d4: pairs,
-// d8: groups of 8); only then do d4 / d8 use their pairwise orders.
-// ---------------------------------------------------------------------------
-template <int M, int D>
-__device__ __forceinline__ double exact_dist(const QVec<D>& q, const double* p, uint64_t d, int strat, bool in_chunk,
-                                             double pexp) {
-  if (M == M_LP) {
-    double dist = 0.0;
-    for (uint64_t i = 0; i < d; ++i) dist = dadd(dist, pow(fabs(dsub(q[i], p[i])), pexp));
-    return dist;
-  }
-  if (M == M_LINF) {
-    double dist = 0.0;
-    if (D > 0) {
-#pragma unroll
-      for (int i = 0; i < D; ++i) dist = max_nn(dist, fabs(dsub(q[i], p[i])));
-    } else {
-      for (uint64_t i = 0; i < d; ++i) dist = max_nn(dist, fabs(dsub(q[i], p[i])));
-    }
-    return dist;
-  }
-  if (D > 0) {
-    if (D == 4 && in_chunk) {
-      double a0 = axis_of<M>(dsub(p[0], q[0])), a1 = axis_of<M>(dsub(p[1], q[1]));
-      double a2 = axis_of<M>(dsub(p[2], q[2])), a3 = axis_of<M>(dsub(p[3], q[3]));
-      return dadd(dadd(a0, a2), dadd(a1, a3));
-    }
-    if (D == 8 && in_chunk) {
-      double a[8];
-#pragma unroll
-      for (int i = 0; i < 8; ++i) a[i] = axis_of<M>(dsub(p[i], q[i]));
-      return dadd(dadd(dadd(a[0], a[1]), dadd(a[2], a[3])), dadd(dadd(a[4], a[5]), dadd(a[6], a[7])));
-    }
-    double dist = 0.0;
-#pragma unroll
-    for (int i = 0; i < D; ++i) dist = dadd(dist, axis_of<M>(dsub(q[i], p[i])));
-    return dist;
-  }
-  if (strat == S_PACKED) {
-    if (d == 4 && in_chunk) {
-      double a0 = axis_of<M>(dsub(p[0], q[0])), a1 = axis_of<M>(dsub(p[1], q[1]));
-      double a2 = axis_of<M>(dsub(p[2], q[2])), a3 = axis_of<M>(dsub(p[3], q[3]));
-      return dadd(dadd(a0, a2), dadd(a1, a3));
-    }
-    if (d == 8 && in_chunk) {
-      double a[8];
-#pragma unroll
-      for (int i = 0; i < 8; ++i) a[i] = axis_of<M>(dsub(p[i], q[i]));
-      return dadd(dadd(dadd(a[0], a[1]), dadd(a[2], a[3])), dadd(dadd(a[4], a[5]), dadd(a[6], a[7])));
-    }
-    double dist = 0.0;
-    for (uint64_t i = 0; i < d; ++i) dist = dadd(dist, axis_of<M>(dsub(q[i], p[i])));
-    return dist;
-  }
-  const uint64_t nch = d / LANES;
-  double dist = 0.0;
-  if (strat == S_FOLDED) {
-    double acc[LANES] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (uint64_t c = 0; c < nch; ++c)
-#pragma unroll
-      for (int j = 0; j < LANES; ++j) acc[j] = dadd(acc[j], axis_of<M>(dsub(q[c * LANES + j], p[c * LANES + j])));
-    dist = nch ? hsum8(acc) : 0.0;
-  } else {
-    for (uint64_t c = 0; c < nch; ++c) {
-      double v[LANES];
-#pragma unroll
-      for (int j = 0; j < LANES; ++j) v[j] = axis_of<M>(dsub(q[c * LANES + j], p[c * LANES + j]));
-      dist = dadd(dist, hsum8(v));
-    }
-  }
-  for (uint64_t i = nch * LANES; i < d; ++i) dist = dadd(dist, axis_of<M>(dsub(q[i], p[i])));
-  return dist;
-}
-
-// Exact box distance (src/kernel.rs:565-616).
-template <int M, int D>
-__device__ __forceinline__ double exact_box_dist(const QVec<D>& q, const double* box, uint64_t d, double pexp) {
-  const double* lo = box;
-  const double* hi = box + d;
-  if (M == M_LINF) {
-    double worst = 0.0;
-    for (uint64_t i = 0; i < d; ++i) worst = max_nn(worst, axis_offset(q[i], lo[i], hi[i]));
-    return worst;
-  }
-  if (M == M_LP) {
-    double dist = 0.0;
-    for (uint64_t i = 0; i < d; ++i) {
-      double off = axis_offset(q[i], lo[i], hi[i]);
-      if (off > 0.0) dist = dadd(dist, pow(off, pexp));
-    }
-    return dist;
-  }
-  const uint64_t nch = d / LANES;
-  double dist = 0.0;
-  if (nch) {
-    double acc[LANES] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (uint64_t c = 0; c < nch; ++c)
-#pragma unroll
-      for (int j = 0; j < LANES; ++j) {
-        uint64_t i = c * LANES + j;
-        double off = max_nn(max_nn(dsub(lo[i], q[i]), dsub(q[i], hi[i])), 0.0);
-        acc[j] = dadd(acc[j], axis_of<M>(off));
-      }
-    dist = hsum8(acc);
-  }
-  for (uint64_t i = nch * LANES; i < d; ++i) dist = dadd(dist, reduce<M>(axis_offset(q[i], lo[i], hi[i]), pexp));
-  return dist;
-}
-
-// ---------------------------------------------------------------------------
-// FP32 interval bounds with directed rounding.
-//
-// A double x is enclosed by FP32 values: q32 = RN(q) gives
-// q in [q32 - e, q32 + e], e = 2^-24 |q32| + 2^-149 (likewise the RN copies of
-// the points); a double converted through its bits (mag_dn32 / mag_up32) is
-// bracketed directly.  Interval sums, differences and squares rounded toward
-// the safe side give an FP32 lower bound lb and upper bound ub of the exact real
-// distance.  The FP64 value the reference computes from the same inputs is
-// within (d + 3) relative roundings of 2^-53 of that real value, so with the
-// FP64 pruning bound b enclosed as [b_lo, b_hi] = [b (1 - 2^-20), b (1 + 2^-20)]
-// (rounded outward):
-//   lb > b_hi  implies  exact > b   (the reference rejects: skip it),
-//   ub < b_lo  implies  exact <= b  (the reference admits: no FP64 needed),
-// and only the remaining cases compute the exact FP64 value.  Non-finite FP32
-// values (inputs beyond FP32 range) make lb 0 and ub inf, deciding nothing.
-// ---------------------------------------------------------------------------
-constexpr float TWO_M24 = 5.9604645e-08f;  // 2^-24
-constexpr float TWO_M23 = 1.1920929e-07f;  // 2^-23
-constexpr float TINY32 = 1.4e-45f;         // 2^-149
-constexpr float LB_SHRINK = 0.99999905f;   // 1 - 2^-20 (exact in FP32)
-constexpr float UB_GROW = 1.0000010f;      // 1 + 2^-20 (exact in FP32)
-
-// |x| of a double given by its bits, rounded down / up to FP32.
-__device__ __forceinline__ float mag_dn32(uint64_t b) {
-  b &= 0x7fffffffffffffffull;
-  const int e = static_cast<int>(b >> 52) - 896;  // FP32 biased exponent
-  if ((b >> 52) == 0x7ff) return (b & 0xfffffffffffffull) ? 0.f : __int_as_float(0x7f800000);
-  if (e >= 255) return 3.40282347e38f;
-  if (e <= 0) return 0.f;
-  return __uint_as_float((static_cast<uint32_t>(e) << 23) | static_cast<uint32_t>((b >> 29) & 0x7fffffu));
-}
-__device__ __forceinline__ float mag_up32(uint64_t b) {
-  b &= 0x7fffffffffffffffull;
-  if (b == 0) return 0.f;
-  const int e = static_cast<int>(b >> 52) - 896;
-  if (e >= 255) return __int_as_float(0x7f800000);
-  if (e <= 0) return 1.17549435e-38f;  // FLT_MIN bounds everything below it
-  uint32_t r = (static_cast<uint32_t>(e) << 23) | static_cast<uint32_t>((b >> 29) & 0x7fffffu);
-  if (b & 0x1fffffffull) r += 1;  // carries into the exponent (or to +inf) correctly
-  return __uint_as_float(r);
-}
-// Signed double (bits) rounded down / up to FP32.
-__device__ __forceinline__ float rd32(uint64_t b) { return (b >> 63) ? -mag_up32(b) : mag_dn32(b); }
-__device__ __forceinline__ float ru32(uint64_t b) { return (b >> 63) ? -mag_dn32(b) : mag_up32(b); }
-
-// Enclosure [lo, hi] of a double whose FP32 round-to-nearest copy is x32.
-__device__ __forceinline__ void rn_enclose(float x32, float* lo, float* hi) {
-  const float e = __fmaf_ru(fabsf(x32), TWO_M24, TINY32);
-  *lo = __fsub_rd(x32, e);
-  *hi = __fadd_ru(x32, e);
-}
-// Lower / upper bound of |x - y| for x in [xl, xh], y in [yl, yh].
-__device__ __forceinline__ float absdiff_lb(float xl, float xh, float yl, float yh) {
-  const float a = __fsub_rd(xl, yh), b = __fsub_rd(yl, xh);
-  const float m = a > b ? a : b;
-  return m > 0.f ? m : 0.f;  // NaN lands on 0
-}
-__device__ __forceinline__ float absdiff_ub(float xl, float xh, float yl, float yh) {
-  const float a = __fsub_ru(xh, yl), b = __fsub_ru(yh, xl);
-  return fmaxf(fmaxf(a, b), 0.f);
-}
-template <int M>
-__device__ __forceinline__ float red_lb(float t) {  // reduce(), rounded down
-  return M == M_L2 ? __fmul_rd(t, t) : t;
-}
-template <int M>
-__device__ __forceinline__ float red_ub(float t) {
-  return M == M_L2 ? __fmul_ru(t, t) : t;
-}
-template <int M>
-__device__ __forceinline__ float fold_lb(float acc, float t) {  // fold(), rounded down
-  if (M == M_LINF) return acc > t ? acc : t;
-  return __fadd_rd(acc, t);
-}
-template <int M>
-__device__ __forceinline__ float fold_ub(float acc, float t) {
-  if (M == M_LINF) return fmaxf(acc, t);
-  return __fadd_ru(acc, t);
-}
-
-// dist <= bound for a non-negative bound given by its bits, with dist of any
-// sign: a cell bound fl(fl(cell - old) + far_axis) can round slightly below
-// zero, which f64 '<=' admits; NaN never is.
-__device__ __forceinline__ bool leq_bound(double dist, uint64_t bound_bits) {
-  const uint64_t b = dbits(dist);
-  if (b >> 63) return (b & 0x7fffffffffffffffull) <= INF_BITS;
-  return b <= bound_bits;
-}
+#include "kd_query_common.cuh"
 
 // ---------------------------------------------------------------------------
 // The k best so far, sorted by (reduced distance, original index): K register
@@ -380,13 +112,6 @@ struct Frame {
   double x;       // parent cell_dist, or the saved axis value
   double y;       // the pending child's box distance (F_BOX_*)
 };
-
-// The IEEE order of finite doubles as an unsigned key (-0 folded onto +0), so
-// the near-child test q[dim] <= split (query.rs:263-268) is an integer compare.
-__device__ __forceinline__ uint64_t ieee_key(uint64_t b) {
-  uint64_t k = total_key_bits(b);
-  return k == 0x7fffffffffffffffull ? 0x8000000000000000ull : k;
-}
 
 template <int M, int D, int K>
 __global__ void __launch_bounds__(QUERY_THREADS) k_query(QArgs a) {
@@ -818,7 +543,7 @@ int launch(const QArgs& a, cudaStream_t st) {
   const unsigned blocks = static_cast<unsigned>((a.nq + QUERY_THREADS - 1) / QUERY_THREADS);
   if constexpr (D > 0 && M != M_LP && K > 0) {
     if (a.n_points < ROW_NONE) {
-      if (!a.use_eps && !force_reference_order())
+      if (!a.use_eps && !a.reference_order && !force_reference_order())
         k_query_packet<M, D, K><<<blocks, QUERY_THREADS, 0, st>>>(a);
       else
         k_query_fast<M, D, K><<<blocks, QUERY_THREADS, 0, st>>>(a);
@@ -857,8 +582,15 @@ int dispatch_d(const QArgs& a, cudaStream_t st) {
 }  // namespace
 
 int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, const QueryParams& qp,
-                    double* d_out_d, int64_t* d_out_i, cudaStream_t st, uint32_t* d_status) {
+                    double* d_out_d, int64_t* d_out_i, cudaStream_t st, uint32_t* d_status,
+                    unsigned long long* d_survivors) {
+  // d >= 16, L2, eps = 0: the tensor-core filter (the tree stops pruning there)
+  const bool tc_allowed = qp.path == PATH_TENSOR_CORE || (qp.path == PATH_AUTO && !force_reference_order());
+  if (tc_allowed && tc_applicable(t, qp))
+    return query_tc_on_device(const_cast<kd_tree*>(t), d_queries, nq, qp, d_out_d, d_out_i, st, d_status,
+                              d_survivors);
   QArgs a{};
+  a.reference_order = qp.path == PATH_REFERENCE_ORDER;
   a.data = t->data;
   a.data32 = t->data32;
   a.indices = t->indices;

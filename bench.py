@@ -193,6 +193,145 @@ def run_reference(args):
     return 0
 
 
+PATH_AUTO, PATH_REFERENCE_ORDER, PATH_TENSOR_CORE = 0, 1, 3
+# kernels one kd_query_device call launches for d=3, k=16 (queries sorted by
+# landing leaf: k_landing_leaf, 3 scan kernels, k_scatter_order; k_query_packet)
+LAUNCHES_PER_STEP = 6
+
+
+def gmm_points(rng, centres, n, sigma=0.01):
+    return centres[rng.integers(0, len(centres), n)] + sigma * rng.standard_normal((n, centres.shape[1]))
+
+
+def time_path(lib, tree, dq, k, p, path, reps, torch, stream, survivors=None):
+    """Mean ms of kd_query_device_path over `reps` calls (events on `stream`)."""
+    n = dq.shape[0]
+    od = torch.empty((n, k), dtype=torch.float64, device=dq.device)
+    oi = torch.empty((n, k), dtype=torch.int64, device=dq.device)
+    P = ctypes.c_void_p
+
+    def call():
+        st = lib.kd_query_device_path(tree._h, P(dq.data_ptr()), dq.numel(), k, p, 0, 0.0, 0.0, P(od.data_ptr()),
+                                      P(oi.data_ptr()), P(stream.cuda_stream), path,
+                                      P(survivors.data_ptr()) if survivors is not None else None)
+        if st:
+            raise RuntimeError(f"kd_query_device_path failed: {st}")
+
+    call()  # warm-up (and, for the tensor-core path, the one-time BF16 copy of the tree)
+    if survivors is not None:
+        survivors.zero_()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        call()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps, (od, oi)
+
+
+def plain_scale_cases(lib, torch, stream, dev):
+    """Config 2: N=1M, d=3, leafsize 16, 1M queries; k in {1, 16}, p in {1, 2, inf},
+    uniform and a 64-component Gaussian mixture (sigma 0.01)."""
+    from kdtree import KDTree
+
+    out = {}
+    rd, rq = np.random.default_rng(2), np.random.default_rng(3)
+    centres = np.random.default_rng(4).uniform(size=(64, DIM))
+    sets = {"uniform": (rd.uniform(size=(N_POINTS, DIM)), rq.uniform(size=(N_QUERIES, DIM))),
+            "gmm": (gmm_points(rd, centres, N_POINTS), gmm_points(rq, centres, N_QUERIES))}
+    for name, (data, q) in sets.items():
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tree = KDTree(data, leafsize=LEAFSIZE)
+        build_s = time.perf_counter() - t0
+        dq = torch.from_numpy(q).to(dev)
+        for k in (1, 16):
+            for p in (1.0, 2.0, float("inf")):
+                ms, _ = time_path(lib, tree, dq, k, p, PATH_AUTO, 3, torch, stream)
+                out[f"{name}-k{k}-p{'inf' if p == float('inf') else int(p)}"] = {"qps": N_QUERIES / ms * 1e3,
+                                                                               "ms": ms}
+        out[f"{name}-build_s"] = build_s
+        del tree
+    return out
+
+
+def precision_cases(lib, torch, stream, dev, cpu_threads):
+    """Config 3: N=1M, d in {16, 64}, standard normal x per-dimension scale
+    log-uniform in [0.1, 10], 100k queries, k=32, L2: the tensor-core filter path
+    against the reference-order FP64 path (on a 1,000-query sample), the filter's
+    survivors per pair, and the BF16 score's error against FP64."""
+    from kdtree import KDTree
+
+    out = {}
+    for d in (16, 64):
+        rng = np.random.default_rng(300 + d)
+        scale = np.exp(rng.uniform(np.log(0.1), np.log(10), d))
+        data = rng.standard_normal((1_000_000, d)) * scale
+        q = rng.standard_normal((100_000, d)) * scale
+        t0 = time.perf_counter()
+        tree = KDTree(data, leafsize=16)
+        build_s = time.perf_counter() - t0
+        dq = torch.from_numpy(q).to(dev)
+        surv = torch.zeros(1, dtype=torch.int64, device=dev)
+        ms_tc, (od, oi) = time_path(lib, tree, dq, 32, 2.0, PATH_TENSOR_CORE, 3, torch, stream, surv)
+        pairs = 3 * q.shape[0] * data.shape[0]
+        sample = dq[:1000].contiguous()
+        ms_ref, (rd_, ri_) = time_path(lib, tree, sample, 32, 2.0, PATH_REFERENCE_ORDER, 1, torch, stream)
+        same = bool(torch.equal(oi[:1000], ri_) and torch.equal(od[:1000], rd_))
+        # BF16 score error against FP64 on the true neighbours of 200 queries
+        c = (data.min(0) + data.max(0)) / 2
+        qi = np.repeat(np.arange(200), 32)
+        pi = oi[:200].cpu().numpy().reshape(-1)
+        qb = torch.from_numpy(q[:200] - c).float().bfloat16().double().numpy()
+        pb = torch.from_numpy(data[pi] - c).float().bfloat16().double().numpy()
+        approx = (qb[qi] ** 2).sum(1) + (pb ** 2).sum(1) - 2 * (qb[qi] * pb).sum(1)
+        exact = ((q[qi] - data[pi]) ** 2).sum(1)
+        rel = np.abs(approx - exact) / exact
+        case = {"build_s": build_s, "tc_qps": q.shape[0] / ms_tc * 1e3, "tc_ms_100k": ms_tc,
+                "reference_order_fp64_qps": 1000 / ms_ref * 1e3, "reference_order_sample": 1000,
+                "speedup_tc_vs_fp64_path": (q.shape[0] / ms_tc) / (1000 / ms_ref),
+                "sample_identical": same, "rerank_fraction": int(surv.item()) / pairs,
+                "filter_rel_err_max": float(rel.max()), "filter_rel_err_median": float(np.median(rel))}
+        if cpu_threads:
+            sys.path.insert(0, str(ROOT / "oracle"))
+            import kdtree_oracle
+
+            ot = kdtree_oracle.OracleKDTree(data, leafsize=16, parallel=True)
+            ns = 2000 if d == 16 else 200
+            t0 = time.perf_counter()
+            ot.query(q[:ns], k=32, threads=cpu_threads)
+            case["cpu_oracle_qps"] = ns / (time.perf_counter() - t0)
+            case["cpu_sample"] = ns
+        out[f"d{d}"] = case
+        del tree
+    return out
+
+
+def run_profile_tc():
+    """A tensor-core-path case small enough for an ncu capture: one CTA-filling
+    batch (152 x 128 queries) against 100,000 points, d=64, k=32."""
+    import torch
+
+    from kdtree import KDTree
+    from kdtree import _core
+
+    lib = _core._lib
+    P_, u64_, d_ = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double
+    lib.kd_query_device_path.argtypes = [P_, P_, u64_, u64_, d_, ctypes.c_int, d_, d_, P_, P_, P_, ctypes.c_int, P_]
+    lib.kd_query_device_path.restype = ctypes.c_int
+    rng = np.random.default_rng(364)
+    scale = np.exp(rng.uniform(np.log(0.1), np.log(10), 64))
+    data = rng.standard_normal((100_000, 64)) * scale
+    q = rng.standard_normal((152 * 128, 64)) * scale
+    tree = KDTree(data, leafsize=16)
+    stream = torch.cuda.Stream()
+    dq = torch.from_numpy(q).cuda()
+    ms, _ = time_path(lib, tree, dq, 32, 2.0, PATH_TENSOR_CORE, 3, torch, stream)
+    print(json.dumps({"profile_tc_ms": ms, "queries": q.shape[0], "points": data.shape[0], "d": 64, "k": 32}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -200,9 +339,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-cases", action="store_true", help="skip the secondary workloads")
+    ap.add_argument("--profile-tc", action="store_true",
+                    help="only run the tensor-core path on a profiling-sized case (N=100k, d=64, "
+                         "19,456 queries, k=32), 3 calls")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_tc:
+        return run_profile_tc()
 
     import torch
 
@@ -216,6 +361,9 @@ def main():
     from kdtree import _core
 
     lib = _core._lib
+    P_, u64_, d_ = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double
+    lib.kd_query_device_path.argtypes = [P_, P_, u64_, u64_, d_, ctypes.c_int, d_, d_, P_, P_, P_, ctypes.c_int, P_]
+    lib.kd_query_device_path.restype = ctypes.c_int
     data, q = workload(rank)
 
     # build (GPU), timed on the host around the synchronous call
@@ -338,7 +486,7 @@ def main():
         "config": {"workload": WORKLOAD, "n_points": N_POINTS, "queries_per_step": N_QUERIES, "d": DIM, "k": K,
                    "p": P, "leafsize": LEAFSIZE, "l2": "flushed (256 MiB write) before every timed step",
                    "parallelism": f"replicas x{ws}"},
-        "gpu_launches": args.steps,
+        "gpu_launches": LAUNCHES_PER_STEP * args.steps,
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),
                 "d2h_bytes_per_step": int(N_QUERIES * K * 16)},
@@ -350,6 +498,12 @@ def main():
             "sample": "the full 1,000,000-query step, best of 3 runs (oracle restatement of the reference)"},
         "wall_s_timed_region": t_wall,
     }
+    if not args.no_cases and ws == 1:
+        ct = None
+        if not args.no_cpu:
+            ct = kdtree_oracle.max_threads()
+        line["cases"] = {"plain_scale": plain_scale_cases(lib, torch, stream, dev),
+                         "precision": precision_cases(lib, torch, stream, dev, ct)}
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()

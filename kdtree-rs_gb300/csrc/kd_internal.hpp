@@ -89,6 +89,13 @@ int query_on_device_scratch(const kd_tree* t, const double* d_queries, uint64_t 
                             const QueryParams& qp, double* d_out_d, int64_t* d_out_i,
                             cudaStream_t stream, uint32_t* d_status, double* d_axes_scratch);
 
+// Sort a batch by landing leaf (the leaf each query's descent reaches first):
+// leaf_of[i] = that leaf's node id, order = query indices grouped by leaf in
+// preorder.  `scratch` holds order_scratch_words(t) u32.  Work on `stream`.
+uint64_t order_scratch_words(const kd_tree* t);
+void order_by_landing_leaf(const kd_tree* t, const double* d_queries, uint64_t nq, uint32_t* leaf_of,
+                           uint32_t* order, uint32_t* scratch, cudaStream_t stream);
+
 // Exact k-NN through the tensor-core filter (L2, eps = 0, 16 <= d <= 128,
 // k <= 32).  Returns KD_OK, or KD_ERR_INVALID_ARGUMENT without doing anything
 // when the case is outside that envelope.  `d_survivors`, if not NULL,

@@ -581,6 +581,24 @@ int dispatch_d(const QArgs& a, cudaStream_t st) {
 
 }  // namespace
 
+uint64_t order_scratch_words(const kd_tree* t) {
+  return t->n_nodes + (t->n_nodes + SCAN_TILE - 1) / SCAN_TILE;
+}
+
+void order_by_landing_leaf(const kd_tree* t, const double* d_queries, uint64_t nq, uint32_t* leaf_of,
+                           uint32_t* order, uint32_t* scratch, cudaStream_t st) {
+  const uint64_t n_tiles = (t->n_nodes + SCAN_TILE - 1) / SCAN_TILE;
+  uint32_t* counts = scratch;
+  uint32_t* tile_sums = counts + t->n_nodes;
+  cudaMemsetAsync(counts, 0, t->n_nodes * sizeof(uint32_t), st);
+  const unsigned qb = static_cast<unsigned>((nq + 255) / 256);
+  k_landing_leaf<<<qb, 256, 0, st>>>(t->nodes, d_queries, nq, t->ndim, leaf_of, counts);
+  k_scan_tiles<<<static_cast<unsigned>(n_tiles), SCAN_THREADS, 0, st>>>(counts, t->n_nodes, tile_sums);
+  k_scan_sums<<<1, SCAN_THREADS, 0, st>>>(tile_sums, n_tiles);
+  k_scan_add<<<static_cast<unsigned>((t->n_nodes + 255) / 256), 256, 0, st>>>(counts, t->n_nodes, tile_sums);
+  k_scatter_order<<<qb, 256, 0, st>>>(leaf_of, counts, nq, order);
+}
+
 int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, const QueryParams& qp,
                     double* d_out_d, int64_t* d_out_i, cudaStream_t st, uint32_t* d_status,
                     unsigned long long* d_survivors) {
@@ -622,21 +640,12 @@ int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, cons
   }
   void* sort_mem = nullptr;
   if (nq >= ORDER_MIN_QUERIES && nq < 0xffffffffull) {
-    const uint64_t n_tiles = (t->n_nodes + SCAN_TILE - 1) / SCAN_TILE;
-    const uint64_t words = 2 * nq + t->n_nodes + n_tiles;
+    const uint64_t words = 2 * nq + order_scratch_words(t);
     cudaError_t e = cudaMallocAsync(&sort_mem, words * sizeof(uint32_t), st);
     if (e == cudaSuccess) {
       uint32_t* leaf_of = static_cast<uint32_t*>(sort_mem);
       uint32_t* order = leaf_of + nq;
-      uint32_t* counts = order + nq;
-      uint32_t* tile_sums = counts + t->n_nodes;
-      cudaMemsetAsync(counts, 0, t->n_nodes * sizeof(uint32_t), st);
-      const unsigned qb = static_cast<unsigned>((nq + 255) / 256);
-      k_landing_leaf<<<qb, 256, 0, st>>>(t->nodes, d_queries, nq, t->ndim, leaf_of, counts);
-      k_scan_tiles<<<static_cast<unsigned>(n_tiles), SCAN_THREADS, 0, st>>>(counts, t->n_nodes, tile_sums);
-      k_scan_sums<<<1, SCAN_THREADS, 0, st>>>(tile_sums, n_tiles);
-      k_scan_add<<<static_cast<unsigned>((t->n_nodes + 255) / 256), 256, 0, st>>>(counts, t->n_nodes, tile_sums);
-      k_scatter_order<<<qb, 256, 0, st>>>(leaf_of, counts, nq, order);
+      order_by_landing_leaf(t, d_queries, nq, leaf_of, order, order + nq, st);
       a.order = order;
     } else {
       cudaGetLastError();  // run unordered: same results, less coherence

@@ -57,7 +57,9 @@ struct TcArgs {
   const double* data;     // tree-ordered points, FP64
   const float* data32;    // tree-ordered points, FP32
   const uint32_t* indices;
-  const float* q32;       // nq x d, FP32 copies of the queries
+  const uint32_t* order;  // sorted row -> query index (rows are grouped by landing leaf)
+  const uint32_t* tile_start;  // per query tile: the point tile holding its landing leaf
+  const float* q32;       // nq x d, FP32 copies of the queries, in sorted row order
   const float* qn2;       // |q_b|^2, FP32 sum
   const float* qnorm;     // |q_b| rounded up
   const float* pw;        // per point w (padded to whole tiles with +inf)
@@ -140,6 +142,20 @@ __device__ __forceinline__ void tc_threshold(float b, float qn2, float qnorm, fl
   *thr = __fsub_ru(__fmul_ru(r, r), __fmul_rd(qn2, 0.99975586f /* 1 - 2^-12 */));
 }
 
+// The i-th point tile a query tile visits: its own tile s first, then
+// alternately the next and previous ones (s, s+1, s-1, s+2, ...) -- rows are in
+// tree order, so nearby tiles hold nearby points and bounds tighten early.
+__device__ __forceinline__ uint32_t zigzag(uint32_t s, uint32_t i, uint32_t n) {
+  const uint32_t left = s, right = n - 1 - s, m = left < right ? left : right;
+  if (i == 0) return s;
+  if (i <= 2 * m) {
+    const uint32_t j = (i + 1) / 2;
+    return (i & 1) ? s + j : s - j;
+  }
+  const uint32_t off = i - 2 * m;
+  return right > left ? s + m + off : s - m - off;
+}
+
 template <int K>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_query_tc(const __grid_constant__ CUtensorMap tmap_q, const __grid_constant__ CUtensorMap tmap_p, TcArgs a) {
@@ -211,7 +227,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           unsigned char* dst = s_p + s * p_bytes;
           mbar_expect_tx(smem_u32(&full[s]), p_bytes);
           for (uint32_t kc = 0; kc < kch; ++kc)
-            tma_load_2d(smem_u32(dst + kc * TC_N * 128), &tmap_p, kc * TC_KC, pt * TC_N, smem_u32(&full[s]));
+            tma_load_2d(smem_u32(dst + kc * TC_N * 128), &tmap_p, kc * TC_KC,
+                        zigzag(a.tile_start[qt], pt, a.n_pt) * TC_N, smem_u32(&full[s]));
           last_use[s] = u + 1;
         }
         if (!ok) break;
@@ -265,11 +282,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     unsigned long long surv = 0;
     bool ok = true;
     for (uint32_t qt = blockIdx.x; qt < a.n_qt && ok; qt += gridDim.x) {
-      const uint64_t qi = static_cast<uint64_t>(qt) * TC_M + row;
-      const bool active = qi < a.nq;
-      const uint64_t qrow = active ? qi : 0;
+      const uint64_t srow = static_cast<uint64_t>(qt) * TC_M + row;  // sorted row
+      const bool active = srow < a.nq;
+      const uint64_t qrow = active ? srow : 0;
+      const uint64_t qi = a.order[qrow];  // the query's own index
       LazySetDyn<K> set;
-      set.init(a.k, a.cutoff, DynPoint{a.queries + qrow * a.d, a.data, a.d, a.strat}, a.indices);
+      set.init(a.k, a.cutoff, DynPoint{a.queries + qi * a.d, a.data, a.d, a.strat}, a.indices);
       const float* q32 = a.q32 + qrow * a.d;
       float qmax = 0.f;
       for (uint64_t i = 0; i < a.d; ++i) qmax = fmaxf(qmax, fabsf(q32[i]));
@@ -286,7 +304,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
-        const uint32_t base = pt * TC_N;
+        const uint32_t base = zigzag(a.tile_start[qt], pt, a.n_pt) * TC_N;
         for (uint32_t c = 0; c < TC_N; c += 32) {
           uint32_t r[32];
           tmem_ld32(tmem + ((quarter * 32) << 16) + b * TC_N + c, r);
@@ -362,15 +380,17 @@ __device__ __forceinline__ uint16_t bf16_rn_bits(float x) {
 }
 
 // Centred BF16 rows (zero padded to dpad) and the per-row norm terms.
-__global__ void k_tc_rows(const double* src, uint64_t n, uint64_t d, uint32_t dpad, const double* centre,
-                          uint16_t* dst, float* n2_out, float* norm_out, float* w_out, float* v_out) {
+__global__ void k_tc_rows(const double* src, const uint32_t* order, uint64_t n, uint64_t d, uint32_t dpad,
+                          const double* centre, uint16_t* dst, float* n2_out, float* norm_out, float* w_out,
+                          float* v_out) {
   const uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
   if (i >= n) return;
+  const uint64_t from = order ? order[i] : i;  // row i of the output holds source row `from`
   float n2 = 0.f;
   for (uint32_t j = 0; j < dpad; ++j) {
     uint16_t h = 0;
     if (j < d) {
-      const double c = __dsub_rn(src[i * d + j], centre[j]);
+      const double c = __dsub_rn(src[from * d + j], centre[j]);
       h = bf16_rn_bits(__double2float_rn(c));
       const float f = __bfloat162float(__ushort_as_bfloat16(h));
       n2 = __fmaf_rn(f, f, n2);  // BF16 squares are exact in FP32
@@ -395,9 +415,22 @@ __global__ void k_tc_pad(float* w, float* v, uint64_t from, uint64_t to) {
   }
 }
 
-__global__ void k_f32_copy(const double* src, float* dst, uint64_t n) {
-  const uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
-  if (i < n) dst[i] = __double2float_rn(src[i]);
+__global__ void k_f32_gather(const double* src, const uint32_t* order, uint64_t n, uint64_t d, float* dst) {
+  const uint64_t f = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  if (f >= n * d) return;
+  const uint64_t r = f / d, j = f - r * d;
+  dst[f] = __double2float_rn(src[static_cast<uint64_t>(order[r]) * d + j]);
+}
+
+// Point tile of each query tile's middle query's landing leaf.
+__global__ void k_tile_start(const DNode* nodes, const uint32_t* leaf_of, const uint32_t* order, uint64_t nq,
+                             uint32_t n_qt, uint32_t* tile_start) {
+  const uint32_t qt = blockIdx.x * blockDim.x + threadIdx.x;
+  if (qt >= n_qt) return;
+  uint64_t r = static_cast<uint64_t>(qt) * TC_M + TC_M / 2;
+  if (r >= nq) r = nq - 1;
+  const uint64_t se = static_cast<uint64_t>(__double_as_longlong(nodes[leaf_of[order[r]]].split));
+  tile_start[qt] = static_cast<uint32_t>(se) / TC_N;  // the leaf's first row
 }
 
 __global__ void k_centre(const double* root_box, uint64_t d, double* centre) {
@@ -459,8 +492,8 @@ int ensure_tc_points(kd_tree* t, cudaStream_t st) {
     return fail(KD_ERR_OUT_OF_MEMORY, "device allocation failed");
   }
   k_centre<<<static_cast<unsigned>((d + 127) / 128), 128, 0, st>>>(t->boxes, d, centre);
-  k_tc_rows<<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(t->data, n, d, dpad, centre, pts, nullptr,
-                                                                     nullptr, w, v);
+  k_tc_rows<<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(t->data, nullptr, n, d, dpad, centre, pts,
+                                                                     nullptr, nullptr, w, v);
   if (n_pad > n) k_tc_pad<<<1, 256, 0, st>>>(w, v, n, n_pad);
   KD_TRY_CUDA(cudaGetLastError());
   KD_TRY_CUDA(cudaStreamSynchronize(st));
@@ -486,11 +519,13 @@ int query_tc_on_device(kd_tree* t, const double* d_queries, uint64_t nq, const Q
   if ((rc = ensure_tc_points(t, st))) return rc;
   const uint64_t d = t->ndim;
   const uint32_t dpad = t->tc_dpad;
-  // query-side inputs
+  // query-side inputs, rows sorted by landing leaf
+  const uint32_t n_qt = static_cast<uint32_t>((nq + TC_M - 1) / TC_M);
   void* mem = nullptr;
   const uint64_t qbytes = nq * dpad * sizeof(uint16_t), fbytes = nq * sizeof(float);
   const uint64_t q32_bytes = nq * d * sizeof(float);
-  const uint64_t total = qbytes + 2 * fbytes + q32_bytes + 256;
+  const uint64_t sort_words = 2 * nq + order_scratch_words(t) + n_qt;
+  const uint64_t total = qbytes + 2 * fbytes + q32_bytes + sort_words * sizeof(uint32_t) + 256;
   if (cudaMallocAsync(&mem, total, st) != cudaSuccess) {
     cudaGetLastError();
     return fail(KD_ERR_OUT_OF_MEMORY, "device allocation failed");
@@ -499,9 +534,15 @@ int query_tc_on_device(kd_tree* t, const double* d_queries, uint64_t nq, const Q
   float* qn2 = reinterpret_cast<float*>(static_cast<unsigned char*>(mem) + qbytes);
   float* qnorm = qn2 + nq;
   float* q32 = qnorm + nq;
-  k_tc_rows<<<static_cast<unsigned>((nq + 255) / 256), 256, 0, st>>>(d_queries, nq, d, dpad, t->tc_centre, qb, qn2,
-                                                                      qnorm, nullptr, nullptr);
-  k_f32_copy<<<static_cast<unsigned>((nq * d + 255) / 256), 256, 0, st>>>(d_queries, q32, nq * d);
+  uint32_t* leaf_of = reinterpret_cast<uint32_t*>(q32 + nq * d);
+  uint32_t* order = leaf_of + nq;
+  uint32_t* tile_start = order + nq;
+  uint32_t* scratch = tile_start + n_qt;
+  order_by_landing_leaf(t, d_queries, nq, leaf_of, order, scratch, st);
+  k_tile_start<<<(n_qt + 127) / 128, 128, 0, st>>>(t->nodes, leaf_of, order, nq, n_qt, tile_start);
+  k_tc_rows<<<static_cast<unsigned>((nq + 255) / 256), 256, 0, st>>>(d_queries, order, nq, d, dpad, t->tc_centre, qb,
+                                                                      qn2, qnorm, nullptr, nullptr);
+  k_f32_gather<<<static_cast<unsigned>((nq * d + 255) / 256), 256, 0, st>>>(d_queries, order, nq, d, q32);
   CUtensorMap mq, mp;
   if ((rc = make_rows_map(&mq, qb, nq, dpad, TC_M)) || (rc = make_rows_map(&mp, t->tc_points, t->n_points, dpad, TC_N))) {
     cudaFreeAsync(mem, st);
@@ -512,6 +553,8 @@ int query_tc_on_device(kd_tree* t, const double* d_queries, uint64_t nq, const Q
   a.data = t->data;
   a.data32 = t->data32;
   a.indices = t->indices;
+  a.order = order;
+  a.tile_start = tile_start;
   a.q32 = q32;
   a.qn2 = qn2;
   a.qnorm = qnorm;
@@ -528,7 +571,7 @@ int query_tc_on_device(kd_tree* t, const double* d_queries, uint64_t nq, const Q
   a.cutoff = qp.cutoff;
   a.coord_max = t->coord_max32;
   a.strat = d <= 16 ? S_FOLDED : S_STREAMED;
-  a.n_qt = static_cast<uint32_t>((nq + TC_M - 1) / TC_M);
+  a.n_qt = n_qt;
   a.n_pt = static_cast<uint32_t>((t->n_points + TC_N - 1) / TC_N);
   a.kch = dpad / TC_KC;
   a.nst = a.kch == 1 ? 4 : 2;

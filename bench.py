@@ -308,6 +308,52 @@ def precision_cases(lib, torch, stream, dev, cpu_threads):
     return out
 
 
+def batched_case(torch, dev, stream, reps=5):
+    """Config 4: 256 trees, N log-uniform in [1e3, 5e5], d in {2, 3, 8}, uniform
+    [0,1)^d points, leafsize 32 (the reference's default); per tree Q queries,
+    Q log-uniform in [1, 5e4], k in {1, 4, 32}, L2; one seed (400) for the whole
+    draw.  Total queries/s of the batch plan: one CUDA graph holding the sort
+    and ONE persistent query launch, the same launches without the graph, and
+    per-tree launches (one kd_query_device launch sequence per tree)."""
+    from kdtree import BatchQuery, KDTree, _core
+
+    rng = np.random.default_rng(400)
+    n_trees = 256
+    ns = np.exp(rng.uniform(np.log(1e3), np.log(5e5), n_trees)).astype(np.int64)
+    ds = rng.choice([2, 3, 8], n_trees)
+    qs = np.exp(rng.uniform(np.log(1.0), np.log(5e4), n_trees)).astype(np.int64)
+    ks = rng.choice([1, 4, 32], n_trees)
+    jobs = []
+    t0 = time.perf_counter()
+    for n, d, nq, k in zip(ns, ds, qs, ks):
+        tree = KDTree(rng.uniform(size=(int(n), int(d))))
+        dq = torch.from_numpy(rng.uniform(size=(int(nq), int(d)))).to(dev)
+        jobs.append((tree, dq, int(k), torch.empty((int(nq), int(k)), dtype=torch.float64, device=dev),
+                     torch.empty((int(nq), int(k)), dtype=torch.int64, device=dev)))
+    build_s = time.perf_counter() - t0
+    plan = BatchQuery(jobs)
+    total_q = int(qs.sum())
+    out = {"trees": n_trees, "points": int(ns.sum()), "queries": total_q, "build_all_s": build_s}
+    results = {}
+    for name, mode in (("graph", _core.BATCH_GRAPH), ("fused_no_graph", _core.BATCH_FUSED),
+                       ("per_tree_launches", _core.BATCH_PER_JOB)):
+        for _ in range(2):
+            plan.run(stream, mode)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            plan.run(stream, mode)
+        s = (time.perf_counter() - t0) / reps
+        out[name] = {"qps": total_q / s, "ms": s * 1e3}
+        results[name] = [(j[3].clone(), j[4].clone()) for j in jobs[:16]]
+    out["identical_across_modes"] = all(
+        torch.equal(a[0], b[0]) and torch.equal(a[1], b[1])
+        for other in ("fused_no_graph", "per_tree_launches") for a, b in zip(results["graph"], results[other]))
+    out["speedup_graph_vs_per_tree"] = out["graph"]["qps"] / out["per_tree_launches"]["qps"]
+    del plan, jobs
+    return out
+
+
 def run_profile_tc():
     """A tensor-core-path case small enough for an ncu capture: one CTA-filling
     batch (152 x 128 queries) against 100,000 points, d=64, k=32."""
@@ -340,6 +386,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-cases", action="store_true", help="skip the secondary workloads")
+    ap.add_argument("--batched-only", action="store_true", help="only run the batched multi-tree case")
     ap.add_argument("--profile-tc", action="store_true",
                     help="only run the tensor-core path on a profiling-sized case (N=100k, d=64, "
                          "19,456 queries, k=32), 3 calls")
@@ -348,6 +395,12 @@ def main():
         return run_reference(args)
     if args.profile_tc:
         return run_profile_tc()
+    if args.batched_only:
+        import torch
+
+        stream = torch.cuda.Stream()
+        print(json.dumps({"batched": batched_case(torch, torch.device("cuda", 0), stream)}), flush=True)
+        return 0
 
     import torch
 
@@ -503,7 +556,8 @@ def main():
         if not args.no_cpu:
             ct = kdtree_oracle.max_threads()
         line["cases"] = {"plain_scale": plain_scale_cases(lib, torch, stream, dev),
-                         "precision": precision_cases(lib, torch, stream, dev, ct)}
+                         "precision": precision_cases(lib, torch, stream, dev, ct),
+                         "batched": batched_case(torch, dev, stream)}
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()

@@ -137,6 +137,51 @@ int kd_query_device_noalloc(const kd_tree* tree, const double* d_queries, uint64
                             double p, int has_max_distance, double max_distance, double eps,
                             double* d_out_distances, int64_t* d_out_indices, void* stream);
 
+/* ---- Batched queries over many trees -------------------------------------
+ * No reference counterpart: the reference answers one `Tree::query` call at a
+ * time (src/query.rs:29-78); a batch is its caller's loop over many trees,
+ * fused into one pass on the device.  Each job's results are exactly those of
+ * kd_query_device on the same job. */
+
+/* One job: a tree, its queries and its outputs, all in device memory with the
+ * layout of kd_query_device (n_queries * ndim values in, n_queries * k out). */
+typedef struct kd_batch_job {
+  const kd_tree* tree;
+  const double* d_queries;
+  uint64_t n_queries;
+  uint64_t k;
+  double* d_out_distances;
+  int64_t* d_out_indices;
+} kd_batch_job;
+
+typedef struct kd_batch kd_batch;
+
+/* Plan a fixed set of jobs: trees, sizes, k and buffer addresses are recorded
+ * (the buffers must stay valid while the plan is used; their contents may
+ * change between runs).  p, max_distance and eps apply to every job and are
+ * validated as kd_query validates them; each job as a kd_query_device call
+ * (k > 0, n_queries > 0, buffers not NULL); every tree must live on the current
+ * device.  Device scratch for the plan is allocated here. */
+int kd_batch_create(const kd_batch_job* jobs, uint64_t n_jobs, double p, int has_max_distance,
+                    double max_distance, double eps, kd_batch** out);
+
+/* How kd_batch_run_mode executes a plan. */
+enum kd_batch_mode {
+  KD_BATCH_GRAPH = 0,   /* one CUDA graph: the sort and ONE persistent kernel launch
+                           for every job the packet traversal serves (what
+                           kd_batch_run does); the first run tunes the launch */
+  KD_BATCH_FUSED = 1,   /* the same launches issued one by one (no graph) */
+  KD_BATCH_PER_JOB = 2  /* one kd_query_device-style launch sequence per job */
+};
+
+/* Run every job of the plan on `stream` and return once the work has finished
+ * (a non-finite query in any job: KD_ERR_NONFINITE_DATA after all jobs ran). */
+int kd_batch_run(kd_batch* batch, void* stream);
+int kd_batch_run_mode(kd_batch* batch, void* stream, int mode);
+
+/* Release a plan (NULL is ignored). */
+void kd_batch_free(kd_batch* batch);
+
 /* Getters: `Tree::ndim`, `Tree::n_points`, `Tree::leafsize`
  * (src/tree.rs:48-58).  kd_n_nodes has no Python getter in the reference. */
 uint64_t kd_ndim(const kd_tree* tree);

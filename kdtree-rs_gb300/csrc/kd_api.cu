@@ -5,12 +5,15 @@
 // (metric), with the messages of src/error.rs:18-51.  The compute runs on the
 // GPU; there is no CPU fallback -- without a device every call fails with
 // KD_ERR_NO_DEVICE.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "kd_internal.hpp"
 
@@ -159,7 +162,7 @@ struct DevMem {
   }
   int alloc(size_t bytes, cudaStream_t s) {
     st = s;
-    cudaError_t e = cudaMallocAsync(&p, bytes ? bytes : 1, s);
+    cudaError_t e = dev_alloc(&p, bytes, s);
     if (e != cudaSuccess) {
       cudaGetLastError();
       p = nullptr;
@@ -168,6 +171,14 @@ struct DevMem {
     return KD_OK;
   }
 };
+
+// Error carried by a query's device status word: bit 0 a non-finite query
+// coordinate, bit 1 a tensor-core pipeline wait that ran out.
+int status_word(uint32_t h) {
+  if (h & 2u) return fail(KD_ERR_CUDA, "the tensor-core pipeline timed out waiting on a barrier");
+  if (h) return fail(KD_ERR_NONFINITE_DATA, "all coordinates must be finite");
+  return KD_OK;
+}
 
 int query_common(const kd_tree* t, const double* queries, bool on_device, uint64_t n_values, uint64_t k,
                  double p, int has_max, double max_distance, double eps, double* out_d, int64_t* out_i,
@@ -204,30 +215,34 @@ int query_common(const kd_tree* t, const double* queries, bool on_device, uint64
   }
   if (k > (~0ull / sizeof(double)) / nq) return fail(KD_ERR_OUT_OF_MEMORY, "output would not fit in memory");
   qp.path = path;
-  const double* dq = queries;
-  double* dd = out_d;
-  int64_t* di = out_i;
-  DevMem mq, md, mi;
-  if (!on_device) {
-    if ((rc = mq.alloc(n_values * sizeof(double), st)) || (rc = md.alloc(nq * k * sizeof(double), st)) ||
-        (rc = mi.alloc(nq * k * sizeof(int64_t), st)))
+  if (on_device) {
+    if ((rc = query_on_device(t, queries, nq, qp, out_d, out_i, st, static_cast<uint32_t*>(status.p), d_survivors)))
       return rc;
-    KD_TRY_CUDA(cudaMemcpyAsync(mq.p, queries, n_values * sizeof(double), cudaMemcpyHostToDevice, st));
-    dq = static_cast<const double*>(mq.p);
-    dd = static_cast<double*>(md.p);
-    di = static_cast<int64_t*>(mi.p);
+    uint32_t h = 0;
+    KD_TRY_CUDA(cudaMemcpyAsync(&h, status.p, sizeof h, cudaMemcpyDeviceToHost, st));
+    KD_TRY_CUDA(cudaStreamSynchronize(st));
+    return status_word(h);
   }
-  if ((rc = query_on_device(t, dq, nq, qp, dd, di, st, static_cast<uint32_t*>(status.p), d_survivors))) return rc;
+  // Host buffers: device staging for the queries and the results.
+  DevMem mq, md, mi;
+  if ((rc = mq.alloc(n_values * sizeof(double), st)) || (rc = md.alloc(nq * k * sizeof(double), st)) ||
+      (rc = mi.alloc(nq * k * sizeof(int64_t), st)))
+    return rc;
+  double* dq = static_cast<double*>(mq.p);
+  double* dd = static_cast<double*>(md.p);
+  int64_t* di = static_cast<int64_t*>(mi.p);
+  uint32_t* ds = static_cast<uint32_t*>(status.p);
+  // One batch: splitting it into concurrent pieces to overlap the download
+  // measured slower (each piece sorts fewer queries, so its warps are less
+  // coherent), and so did kernels writing page-locked outputs directly.
+  KD_TRY_CUDA(cudaMemcpyAsync(dq, queries, n_values * sizeof(double), cudaMemcpyHostToDevice, st));
+  if ((rc = query_on_device(t, dq, nq, qp, dd, di, st, ds, d_survivors))) return rc;
+  KD_TRY_CUDA(cudaMemcpyAsync(out_d, dd, nq * k * sizeof(double), cudaMemcpyDeviceToHost, st));
+  KD_TRY_CUDA(cudaMemcpyAsync(out_i, di, nq * k * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   uint32_t h = 0;
   KD_TRY_CUDA(cudaMemcpyAsync(&h, status.p, sizeof h, cudaMemcpyDeviceToHost, st));
-  if (!on_device) {
-    KD_TRY_CUDA(cudaMemcpyAsync(out_d, dd, nq * k * sizeof(double), cudaMemcpyDeviceToHost, st));
-    KD_TRY_CUDA(cudaMemcpyAsync(out_i, di, nq * k * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-  }
   KD_TRY_CUDA(cudaStreamSynchronize(st));
-  if (h & 2u) return fail(KD_ERR_CUDA, "the tensor-core pipeline timed out waiting on a barrier");
-  if (h) return fail(KD_ERR_NONFINITE_DATA, "all coordinates must be finite");
-  return KD_OK;
+  return status_word(h);
 }
 
 }  // namespace
@@ -291,6 +306,33 @@ int cuda_fail(cudaError_t err, const char* what) {
   return fail(err == cudaErrorMemoryAllocation ? KD_ERR_OUT_OF_MEMORY : KD_ERR_CUDA, m);
 }
 
+cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t st) {
+  constexpr int MAX_DEV = 64;
+  static std::mutex mu;
+  static cudaMemPool_t pools[MAX_DEV] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= MAX_DEV) return cudaMallocAsync(p, bytes, st);
+  cudaMemPool_t pool;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!pools[dev]) {
+      cudaMemPoolProps props{};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      cudaMemPool_t fresh;
+      if ((e = cudaMemPoolCreate(&fresh, &props)) != cudaSuccess) return e;
+      uint64_t keep = KD_POOL_KEEP_BYTES;
+      cudaMemPoolSetAttribute(fresh, cudaMemPoolAttrReleaseThreshold, &keep);
+      pools[dev] = fresh;
+    }
+    pool = pools[dev];
+  }
+  return cudaMallocFromPoolAsync(p, bytes ? bytes : 1, pool, st);
+}
+
 }  // namespace kd
 
 using namespace kd;
@@ -310,7 +352,7 @@ int kd_build(const double* data, uint64_t n_values, uint64_t ndim, uint64_t leaf
   if ((rc = ensure_device(&dev))) return rc;
   cudaStream_t st = thread_stream();
   void* src = nullptr;
-  KD_TRY_CUDA(cudaMallocAsync(&src, n_values * sizeof(double), st));
+  KD_TRY_CUDA(dev_alloc(&src, n_values * sizeof(double), st));
   cudaError_t ce = cudaMemcpyAsync(src, data, n_values * sizeof(double), cudaMemcpyHostToDevice, st);
   if (ce != cudaSuccess) {
     cudaFreeAsync(src, st);

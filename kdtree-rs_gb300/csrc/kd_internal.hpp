@@ -42,6 +42,13 @@ void set_error(const std::string& msg);
 int fail(int status, const std::string& msg);
 int cuda_fail(cudaError_t err, const char* what);
 
+// Stream-ordered device allocation from the library's own memory pool on the
+// current device.  The pool keeps up to KD_POOL_KEEP_BYTES of freed blocks for
+// later calls, so a steady query loop maps no new memory; freed with
+// cudaFreeAsync.
+constexpr uint64_t KD_POOL_KEEP_BYTES = 1ull << 30;
+cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t st);
+
 #define KD_TRY_CUDA(call)                                   \
   do {                                                      \
     cudaError_t kd_err_ = (call);                           \

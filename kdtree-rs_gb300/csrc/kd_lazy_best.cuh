@@ -418,6 +418,202 @@ struct LazySet {
 };
 
 // ---------------------------------------------------------------------------
+// LazyHeap: the same k best as LazySet, as a binary max-heap on the upper
+// enclosure `hi`, in shared memory (slot j of a thread at [j * QUERY_THREADS]:
+// the 32 lanes of a warp touch 32 consecutive words, one per bank, whatever
+// slot each lane is at).  Replacing the worst costs one sift-down, log2(k)
+// levels, instead of a scan of all K register slots.
+//
+// The root has the largest hi, so its exact distance is at most hi[0] and the
+// k-th best (the largest exact distance kept) is at least lo[0]:
+//  - a candidate with clo > hi[0] is after every kept point: rejected;
+//  - a candidate with chi < lo[0] is before the worst, and when no other slot
+//    reaches lo[0] (both children's hi < lo[0]) the root IS the worst:
+//    the candidate replaces it;
+//  - otherwise (enclosures too close to call) the exact FP64 values decide, by
+//    (distance, original index) as BestK does (query.rs:461-481), and the heap
+//    is rebuilt.
+// In a full Packed d8 chunk (kernel.rs:540-562) the summation order differs;
+// that flag rides in the sign bit of lo (lo >= 0 otherwise).
+// ---------------------------------------------------------------------------
+template <int M, int D, int K>
+struct LazyHeap {
+  static constexpr int S = QUERY_THREADS;
+  float* lo;
+  float* hi;
+  uint32_t* row;
+  uint32_t n, k;
+  float b_hi;  // upper bound of the pruning bound min(k-th best, cutoff)
+  float cut_lo, cut_hi;
+  uint64_t cut_bits;
+  const QVec<D>* q;
+  const double* data;
+  const uint32_t* indices;
+
+  __device__ __forceinline__ void init(uint64_t k_, double cutoff, const QVec<D>* qv, const double* data_,
+                                       const uint32_t* indices_, float* s_lo, float* s_hi, uint32_t* s_row) {
+    lo = s_lo + threadIdx.x;
+    hi = s_hi + threadIdx.x;
+    row = s_row + threadIdx.x;
+    n = 0;
+    k = static_cast<uint32_t>(k_);
+    cut_bits = dbits(cutoff);
+    cut_lo = mag_dn32(cut_bits);
+    cut_hi = mag_up32(cut_bits);
+    q = qv;
+    data = data_;
+    indices = indices_;
+    b_hi = cut_hi;
+  }
+  static __device__ __forceinline__ float tag(float l, bool in_chunk) {
+    return __uint_as_float(__float_as_uint(l) | (static_cast<uint32_t>(in_chunk) << 31));
+  }
+  static __device__ __forceinline__ bool chunk_of(float tagged) { return __float_as_uint(tagged) >> 31; }
+  __device__ __forceinline__ double exact_of(uint32_t r, bool in_chunk) const {
+    return exact_dist<M, D>(*q, data + static_cast<uint64_t>(r) * D, D, S_PACKED, in_chunk, 0.0);
+  }
+  __device__ __forceinline__ void put(uint32_t j, float tl, float h, uint32_t r) {
+    lo[j * S] = tl;
+    hi[j * S] = h;
+    row[j * S] = r;
+  }
+  __device__ __forceinline__ void sift_up(uint32_t j, float tl, float h, uint32_t r) {
+    while (j > 0) {
+      const uint32_t p = (j - 1) >> 1;
+      const float ph = hi[p * S];
+      if (!(ph < h)) break;
+      put(j, lo[p * S], ph, row[p * S]);
+      j = p;
+    }
+    put(j, tl, h, r);
+  }
+  __device__ __forceinline__ void sift_down(uint32_t j, float tl, float h, uint32_t r) {
+    for (;;) {
+      uint32_t c = 2 * j + 1;
+      if (c >= n) break;
+      float ch = hi[c * S];
+      if (c + 1 < n) {
+        const float c2 = hi[(c + 1) * S];
+        if (c2 > ch) {
+          ++c;
+          ch = c2;
+        }
+      }
+      if (!(ch > h)) break;
+      put(j, lo[c * S], ch, row[c * S]);
+      j = c;
+    }
+    put(j, tl, h, r);
+  }
+  __device__ __forceinline__ void refresh() { b_hi = n < k ? cut_hi : fminf(hi[0], cut_hi); }
+
+  // Offer the point at tree row r whose exact distance lies in [clo, chi].
+  __device__ __forceinline__ void offer(float clo, float chi, uint32_t r, bool in_chunk) {
+    double cx = 0.0;
+    bool have_x = false;
+    if (!(chi <= cut_lo)) {  // the cutoff test, unless clearly inside
+      if (clo > cut_hi) return;
+      cx = exact_of(r, in_chunk);
+      have_x = true;
+      if (dbits(cx) > cut_bits) return;
+    }
+    if (n < k) {  // not full: the reference keeps every candidate
+      ++n;
+      sift_up(n - 1, tag(clo, in_chunk), chi, r);
+      refresh();
+      return;
+    }
+    const float rh = hi[0];
+    if (clo > rh) return;
+    const float rl = fabsf(lo[0]);
+    float sec = __int_as_float(0xff800000);
+    if (n > 1) sec = hi[S];
+    if (n > 2) sec = fmaxf(sec, hi[2 * S]);
+    if (chi < rl && sec < rl) {
+      sift_down(0, tag(clo, in_chunk), chi, r);
+      refresh();
+      return;
+    }
+    offer_exact(r, in_chunk, have_x, cx);
+  }
+
+  // Enclosures too close to call: exact values of the candidate and of every
+  // slot that can be the worst (hi >= lo[0]); those slots keep their tightened
+  // enclosures; the candidate replaces the exact worst if it is before it.
+  __device__ __noinline__ void offer_exact(uint32_t r, bool in_chunk, bool have_x, double cx) {
+    if (!have_x) cx = exact_of(r, in_chunk);
+    const uint32_t cid = indices[r];
+    const float rl = fabsf(lo[0]);
+    uint64_t wb = 0;
+    uint32_t wid = 0, wj = 0;
+    bool any = false;
+    for (uint32_t j = 0; j < n; ++j) {
+      if (hi[j * S] >= rl) {
+        const bool ic = chunk_of(lo[j * S]);
+        const uint32_t rj = row[j * S];
+        const uint64_t xb = dbits(exact_of(rj, ic));
+        lo[j * S] = tag(mag_dn32(xb), ic);
+        hi[j * S] = mag_up32(xb);
+        const uint32_t id = indices[rj];
+        if (!any || xb > wb || (xb == wb && id > wid)) {
+          wb = xb;
+          wid = id;
+          wj = j;
+          any = true;
+        }
+      }
+    }
+    const uint64_t cb = dbits(cx);
+    if (cb < wb || (cb == wb && cid < wid)) put(wj, tag(mag_dn32(cb), in_chunk), mag_up32(cb), r);
+    for (uint32_t j = n / 2; j-- > 0;) sift_down(j, lo[j * S], hi[j * S], row[j * S]);
+    refresh();
+  }
+
+  // write_results (query.rs:421-429, 483-493): the exact values sorted by
+  // (distance, index); empty slots after every real one.
+  __device__ __forceinline__ void write(double* od, int64_t* oi, uint64_t k_, uint64_t n_points) const {
+    uint64_t xb[K];
+    uint32_t id[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      if (static_cast<uint32_t>(j) < n) {
+        const uint32_t rj = row[j * S];
+        xb[j] = dbits(exact_of(rj, chunk_of(lo[j * S])));
+        id[j] = indices[rj];
+      } else {
+        xb[j] = ~0ull;
+        id[j] = NO_ID;
+      }
+    }
+#pragma unroll
+    for (int i = 1; i < K; ++i) {
+#pragma unroll
+      for (int j = i; j > 0; --j) {
+        const bool sw = xb[j] < xb[j - 1] || (xb[j] == xb[j - 1] && id[j] < id[j - 1]);
+        const uint64_t tx = xb[j];
+        const uint32_t ti = id[j];
+        xb[j] = sw ? xb[j - 1] : xb[j];
+        id[j] = sw ? id[j - 1] : id[j];
+        xb[j - 1] = sw ? tx : xb[j - 1];
+        id[j - 1] = sw ? ti : id[j - 1];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      if (static_cast<uint64_t>(j) < k_) {
+        if (xb[j] != ~0ull) {
+          od[j] = restore<M>(bitsd(xb[j]), 0.0);
+          oi[j] = static_cast<int64_t>(id[j]);
+        } else {
+          od[j] = bitsd(INF_BITS);
+          oi[j] = static_cast<int64_t>(n_points);
+        }
+      }
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
 // Runtime-width variants (the tensor-core filter path, 16 <= d <= 128):
 // the exact FP64 value follows the reference's Folded (d <= 16) or Streamed
 // (d > 16) L2 order (kernel.rs:343-354, 177-188) from the query in memory.

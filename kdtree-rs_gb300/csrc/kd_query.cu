@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 
 #include "kd_internal.hpp"
 
@@ -444,76 +445,7 @@ __global__ void k_landing_leaf(const DNode* nodes, const double* queries, uint64
   atomicAdd(&counts[node], 1u);
 }
 
-constexpr int SCAN_THREADS = 1024;
-constexpr int SCAN_ITEMS = 4;
-constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
-
-__device__ uint32_t block_scan_excl(uint32_t v, uint32_t* total) {
-  __shared__ uint32_t warp_sums[SCAN_THREADS / 32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) warp_sums[warp] = x;
-  __syncthreads();
-  if (warp == 0) {
-    uint32_t w = warp_sums[lane];
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
-      if (lane >= o) w += y;
-    }
-    warp_sums[lane] = w;
-  }
-  __syncthreads();
-  const uint32_t off = warp ? warp_sums[warp - 1] : 0;
-  *total = warp_sums[SCAN_THREADS / 32 - 1];
-  __syncthreads();
-  return off + x - v;
-}
-
-// Exclusive scan of a[0, n) in place: per-tile scan, tile sums, offsets.
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(uint32_t* a, uint64_t n, uint32_t* tile_sums) {
-  const uint64_t base = blockIdx.x * static_cast<uint64_t>(SCAN_TILE) + threadIdx.x * SCAN_ITEMS;
-  uint32_t v[SCAN_ITEMS], s = 0;
-#pragma unroll
-  for (int j = 0; j < SCAN_ITEMS; ++j) {
-    v[j] = (base + j < n) ? a[base + j] : 0;
-    s += v[j];
-  }
-  uint32_t total;
-  uint32_t run = block_scan_excl(s, &total);
-#pragma unroll
-  for (int j = 0; j < SCAN_ITEMS; ++j) {
-    if (base + j < n) a[base + j] = run;
-    run += v[j];
-  }
-  if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
-}
-
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_sums(uint32_t* sums, uint64_t n_tiles) {
-  __shared__ uint32_t carry;
-  if (threadIdx.x == 0) carry = 0;
-  __syncthreads();
-  for (uint64_t b = 0; b < n_tiles; b += SCAN_THREADS) {
-    uint64_t i = b + threadIdx.x;
-    uint32_t v = i < n_tiles ? sums[i] : 0, total;
-    uint32_t ex = block_scan_excl(v, &total);
-    const uint32_t c = carry;
-    if (i < n_tiles) sums[i] = c + ex;
-    __syncthreads();
-    if (threadIdx.x == 0) carry = c + total;
-    __syncthreads();
-  }
-}
-
-__global__ void k_scan_add(uint32_t* a, uint64_t n, const uint32_t* tile_sums) {
-  const uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
-  if (i < n) a[i] += tile_sums[i / SCAN_TILE];
-}
+#include "kd_scan.cuh"
 
 __global__ void k_scatter_order(const uint32_t* leaf_of, uint32_t* offsets, uint64_t nq, uint32_t* order) {
   uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
@@ -631,7 +563,7 @@ int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, cons
   void* axes = nullptr;
   const bool dyn = !(qp.metric != M_LP && (t->ndim == 2 || t->ndim == 3 || t->ndim == 8));
   if (dyn) {
-    cudaError_t e = cudaMallocAsync(&axes, std::max<uint64_t>(1, nq * t->ndim) * sizeof(double), st);
+    cudaError_t e = dev_alloc(&axes, std::max<uint64_t>(1, nq * t->ndim) * sizeof(double), st);
     if (e != cudaSuccess) {
       cudaGetLastError();
       return fail(KD_ERR_OUT_OF_MEMORY, "device allocation failed");
@@ -641,7 +573,7 @@ int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, cons
   void* sort_mem = nullptr;
   if (nq >= ORDER_MIN_QUERIES && nq < 0xffffffffull) {
     const uint64_t words = 2 * nq + order_scratch_words(t);
-    cudaError_t e = cudaMallocAsync(&sort_mem, words * sizeof(uint32_t), st);
+    cudaError_t e = dev_alloc(&sort_mem, words * sizeof(uint32_t), st);
     if (e == cudaSuccess) {
       uint32_t* leaf_of = static_cast<uint32_t*>(sort_mem);
       uint32_t* order = leaf_of + nq;

@@ -92,10 +92,22 @@ struct PointFilter {
   }
 };
 
+// Shared memory of the k-best heaps of one block (K >= 8; a dummy word below).
+template <int K>
+struct PacketSmem {
+  static constexpr int HK = K >= 8 ? K : 1;
+  float lo[HK * QUERY_THREADS], hi[HK * QUERY_THREADS];
+  uint32_t row[HK * QUERY_THREADS];
+};
+
+// The 32 lanes of a warp run the sorted batch positions tid (one per lane) of
+// the queries described by `a`; every lane of the warp must call it together.
+// s_lo / s_hi / s_row: the block's heap arrays, K * QUERY_THREADS words each
+// (unused for K < 8).
 template <int M, int D, int K>
-__global__ void __launch_bounds__(QUERY_THREADS) k_query_packet(QArgs a) {
+__device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, float* s_lo, float* s_hi,
+                                               uint32_t* s_row) {
   static_assert(D > 0 && M != M_LP, "packet path: compile-time width, metric without pow()");
-  const uint64_t tid = blockIdx.x * static_cast<uint64_t>(QUERY_THREADS) + threadIdx.x;
   const bool in_range = tid < a.nq;
   const uint64_t qi = in_range ? (a.order ? a.order[tid] : tid) : 0;
   // Lanes past the batch end (or with a non-finite query) stay in the warp for
@@ -119,8 +131,12 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query_packet(QArgs a) {
   PointFilter<M, D> filt;
   filt.init(q, a.coord_max);
 
-  LazySet<M, D, K> best;
-  best.init(a.k, a.cutoff, &q, a.data, a.indices);
+  // k-best set: a shared-memory heap from K = 8 up, register slots below
+  std::conditional_t<(K >= 8), LazyHeap<M, D, K>, LazySet<M, D, K>> best;
+  if constexpr (K >= 8)
+    best.init(a.k, a.cutoff, &q, a.data, a.indices, s_lo, s_hi, s_row);
+  else
+    best.init(a.k, a.cutoff, &q, a.data, a.indices);
   float thr = filt.threshold(best.b_hi);
 
   uint32_t stack[PACKET_STACK];  // identical in every lane
@@ -176,4 +192,11 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query_packet(QArgs a) {
     stack[sp++] = left_first ? node + 1 : nd.right;
   }
   if (live) best.write(a.out_d + qi * a.k, a.out_i + qi * a.k, a.k, a.n_points);
+}
+
+template <int M, int D, int K>
+__global__ void __launch_bounds__(QUERY_THREADS) k_query_packet(QArgs a) {
+  __shared__ PacketSmem<K> sm;
+  packet_queries<M, D, K>(a, blockIdx.x * static_cast<uint64_t>(QUERY_THREADS) + threadIdx.x, sm.lo, sm.hi,
+                          sm.row);
 }

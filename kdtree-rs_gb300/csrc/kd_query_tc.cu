@@ -526,7 +526,7 @@ int query_tc_on_device(kd_tree* t, const double* d_queries, uint64_t nq, const Q
   const uint64_t q32_bytes = nq * d * sizeof(float);
   const uint64_t sort_words = 2 * nq + order_scratch_words(t) + n_qt;
   const uint64_t total = qbytes + 2 * fbytes + q32_bytes + sort_words * sizeof(uint32_t) + 256;
-  if (cudaMallocAsync(&mem, total, st) != cudaSuccess) {
+  if (dev_alloc(&mem, total, st) != cudaSuccess) {
     cudaGetLastError();
     return fail(KD_ERR_OUT_OF_MEMORY, "device allocation failed");
   }

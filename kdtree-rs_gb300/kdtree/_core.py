@@ -62,6 +62,12 @@ def _load():
     L.kd_original_data.restype = ctypes.c_int
     L.kd_export.argtypes = [P, P, P, P, P, P]
     L.kd_export.restype = ctypes.c_int
+    L.kd_batch_create.argtypes = [P, u64, d, ctypes.c_int, d, d, ctypes.POINTER(P)]
+    L.kd_batch_create.restype = ctypes.c_int
+    L.kd_batch_run_mode.argtypes = [P, P, ctypes.c_int]
+    L.kd_batch_run_mode.restype = ctypes.c_int
+    L.kd_batch_free.argtypes = [P]
+    L.kd_batch_free.restype = None
     L.kd_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.kd_last_error.restype = ctypes.c_size_t
     return L
@@ -233,3 +239,80 @@ class KDTree:
         if st != KD_OK:
             _raise(st)
         return data, idx, words, split, boxes
+
+
+# -- batched queries over many trees (no reference counterpart) -------------
+class _BatchJob(ctypes.Structure):
+    _fields_ = [("tree", ctypes.c_void_p), ("d_queries", ctypes.c_void_p), ("n_queries", ctypes.c_uint64),
+                ("k", ctypes.c_uint64), ("d_out_distances", ctypes.c_void_p), ("d_out_indices", ctypes.c_void_p)]
+
+
+BATCH_GRAPH, BATCH_FUSED, BATCH_PER_JOB = 0, 1, 2
+
+
+def _cuda_array(a, typestr: str, shape, what: str) -> int:
+    """Device address of a C-contiguous CUDA array (anything exposing
+    __cuda_array_interface__, e.g. a torch tensor) of the given dtype and shape."""
+    iface = getattr(a, "__cuda_array_interface__", None)
+    if iface is None:
+        raise TypeError(f"{what}: expected a CUDA device array, got {type(a).__name__}")
+    if iface["typestr"] != typestr or tuple(iface["shape"]) != tuple(shape):
+        raise ValueError(f"{what}: expected {typestr} of shape {tuple(shape)}, got {iface['typestr']} "
+                         f"{tuple(iface['shape'])}")
+    strides = iface.get("strides")
+    if strides is not None:
+        item = int(typestr[2:])
+        want, acc = [], item
+        for n in reversed(shape):
+            want.append(acc)
+            acc *= n
+        if tuple(strides) != tuple(reversed(want)):
+            raise ValueError(f"{what}: must be C-contiguous")
+    return int(iface["data"][0])
+
+
+class BatchQuery:
+    """Exact k-NN for many (tree, query batch) jobs in one pass on the device
+    (kd_batch_* in include/kdtree_gb300.h).  No reference counterpart: it fuses
+    a caller's loop of `KDTree.query` calls; each job's results equal that
+    call's.  Jobs are (tree, queries[n, ndim] f64, k, out_distances[n, k] f64,
+    out_indices[n, k] i64), arrays in device memory that stay valid while the
+    plan lives; `run()` recomputes every job from the arrays' current contents.
+    """
+
+    __slots__ = ("_h", "_trees")
+
+    def __init__(self, jobs, *, p: float = 2.0, max_distance=None, eps: float = 0.0):
+        jobs = list(jobs)
+        arr = (_BatchJob * max(len(jobs), 1))()
+        for j, (tree, q, k, od, oi) in enumerate(jobs):
+            if not isinstance(tree, KDTree):
+                raise TypeError(f"job {j}: expected a KDTree")
+            k = _usize(k, "k")
+            n = int(q.__cuda_array_interface__["shape"][0]) if hasattr(q, "__cuda_array_interface__") else 0
+            arr[j] = _BatchJob(tree._h, _cuda_array(q, "<f8", (n, tree.ndim), f"job {j} queries"), n, k,
+                               _cuda_array(od, "<f8", (n, k), f"job {j} distances"),
+                               _cuda_array(oi, "<i8", (n, k), f"job {j} indices"))
+        h = ctypes.c_void_p()
+        has_max = max_distance is not None
+        st = _lib.kd_batch_create(ctypes.cast(arr, ctypes.c_void_p), len(jobs), _f64(p), int(has_max),
+                                  _f64(max_distance) if has_max else 0.0, _f64(eps), ctypes.byref(h))
+        if st != KD_OK:
+            _raise(st)
+        self._h = h
+        self._trees = [j[0] for j in jobs]  # keep the trees alive with the plan
+
+    def run(self, stream=None, mode: int = BATCH_GRAPH):
+        """Run every job on `stream` (a CUDA stream handle as an int, or an
+        object with a `cuda_stream` attribute; None = the legacy default
+        stream) and wait for it."""
+        s = getattr(stream, "cuda_stream", stream)
+        st = _lib.kd_batch_run_mode(self._h, ctypes.c_void_p(s) if s else None, int(mode))
+        if st != KD_OK:
+            _raise(st)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            _lib.kd_batch_free(h)
+            self._h = None

@@ -134,3 +134,35 @@ def test_k_far_beyond_n(oracle):
     g, o = _both(oracle, data, data[:10] + 0.01, 8, k=100)
     assert_bit_exact(g, o)
     assert (g[1][:, 40:] == 40).all()
+
+
+@pytest.mark.parametrize("k", [1, 16, 40])
+def test_host_buffers_pinned_and_pageable(oracle, k):
+    """kd_query with page-locked outputs (kernels write them directly) and with
+    pageable ones (device staging + download): identical results."""
+    import ctypes
+
+    import torch
+
+    from kdtree import KDTree, _core
+
+    rng = np.random.default_rng(40 + k)
+    data = rng.uniform(size=(50_000, 3))
+    q = rng.uniform(size=(30_000, 3))
+    t = KDTree(data, leafsize=16)
+    L = _core._lib
+    P = ctypes.c_void_p
+    outs = []
+    for pinned in (True, False):
+        hq = torch.from_numpy(q)
+        hd = torch.empty((len(q), k), dtype=torch.float64)
+        hi = torch.empty((len(q), k), dtype=torch.int64)
+        if pinned:
+            hq, hd, hi = hq.pin_memory(), hd.pin_memory(), hi.pin_memory()
+        st = L.kd_query(t._h, P(hq.data_ptr()), hq.numel(), k, 2.0, 0, 0.0, 0.0, 0, P(hd.data_ptr()),
+                        P(hi.data_ptr()))
+        assert st == 0, _core._last_error()
+        outs.append((hd.numpy().copy(), hi.numpy().copy()))
+    assert_bit_exact(outs[0], outs[1])
+    o = oracle.OracleKDTree(data, leafsize=16).query(q[:3000], k=k, parallel=True)
+    assert_bit_exact((outs[0][0][:3000], outs[0][1][:3000]), o)

@@ -193,7 +193,7 @@ def run_reference(args):
     return 0
 
 
-PATH_AUTO, PATH_REFERENCE_ORDER, PATH_TENSOR_CORE = 0, 1, 3
+PATH_AUTO, PATH_REFERENCE_ORDER, PATH_PACKET, PATH_TENSOR_CORE = 0, 1, 2, 3
 # kernels one kd_query_device call launches for d=3, k=16 (queries sorted by
 # landing leaf: k_landing_leaf, 3 scan kernels, k_scatter_order; k_query_packet)
 LAUNCHES_PER_STEP = 6
@@ -293,6 +293,11 @@ def precision_cases(lib, torch, stream, dev, cpu_threads):
                 "speedup_tc_vs_fp64_path": (q.shape[0] / ms_tc) / (1000 / ms_ref),
                 "sample_identical": same, "rerank_fraction": int(surv.item()) / pairs,
                 "filter_rel_err_max": float(rel.max()), "filter_rel_err_median": float(np.median(rel))}
+        if d == 16:  # the packet traversal on a 10,000-query sample (the tree barely prunes here)
+            ps = dq[:10_000].contiguous()
+            ms_pk, (pd_, pi_) = time_path(lib, tree, ps, 32, 2.0, PATH_PACKET, 1, torch, stream)
+            case["packet_qps"] = 10_000 / ms_pk * 1e3
+            case["packet_identical"] = bool(torch.equal(pi_, oi[:10_000]) and torch.equal(pd_, od[:10_000]))
         if cpu_threads:
             sys.path.insert(0, str(ROOT / "oracle"))
             import kdtree_oracle
@@ -354,6 +359,180 @@ def batched_case(torch, dev, stream, reps=5):
     return out
 
 
+def serving_case(torch, duration_s=2.0, n_templates=256):
+    """Config 5: 32 trees, N log-uniform in [1e5, 4e6], d in {3, 8, 16}, each a
+    64-component Gaussian mixture (centres uniform in [0,1)^d, sigma 0.01),
+    leafsize 32; requests: tree uniform, Q log-uniform in [1, 1e5] queries from
+    the tree's mixture, k log-uniform in [1, 64] rounded, L2; seed 500.  Served
+    by kdtree.Server (continuous batching).  Peak load: a burst of all request
+    templates; then Poisson arrivals at 50/70/90% of that rate for duration_s
+    each: p50/p99 latency (submission to completion) and sustained queries/s."""
+    import threading
+
+    from kdtree import KDTree, Server
+
+    rng = np.random.default_rng(500)
+    n_trees = 32
+    ns = np.exp(rng.uniform(np.log(1e5), np.log(4e6), n_trees)).astype(np.int64)
+    ds = rng.choice([3, 8, 16], n_trees)
+    trees, centres = [], []
+    t0 = time.perf_counter()
+    for n, d in zip(ns, ds):
+        c = rng.uniform(size=(64, int(d)))
+        data = c[rng.integers(0, 64, int(n))] + 0.01 * rng.standard_normal((int(n), int(d)))
+        trees.append(KDTree(data))
+        centres.append(c)
+        del data
+    build_s = time.perf_counter() - t0
+    templates = []
+    for _ in range(n_templates):
+        ti = int(rng.integers(n_trees))
+        nq = max(1, int(np.exp(rng.uniform(0.0, np.log(1e5)))))
+        k = max(1, int(round(np.exp(rng.uniform(0.0, np.log(64))))))
+        d = int(ds[ti])
+        q = centres[ti][rng.integers(0, 64, nq)] + 0.01 * rng.standard_normal((nq, d))
+        qp = torch.from_numpy(q).pin_memory().numpy()
+        od = torch.empty((nq, k), dtype=torch.float64).pin_memory().numpy()
+        oi = torch.empty((nq, k), dtype=torch.int64).pin_memory().numpy()
+        templates.append((ti, qp, k, od, oi))
+    srv = Server(trees)
+    # warm-up, and three requests checked against lone KDTree.query calls
+    tickets = [srv.submit(ti, q, k, out=(od, oi)) for ti, q, k, od, oi in templates]
+    for tk in tickets:
+        srv.wait(tk)
+    identical = True
+    for ti, q, k, od, oi in templates[:3]:
+        d_, i_ = trees[ti].query(q, k=k)
+        identical &= bool(np.array_equal(d_.view(np.int64), od.view(np.int64)) and np.array_equal(i_, oi))
+    # peak: everything at once
+    best = None
+    for _ in range(2):
+        t0 = time.perf_counter()
+        tickets = [srv.submit(ti, q, k, out=(od, oi)) for ti, q, k, od, oi in templates]
+        for tk in tickets:
+            srv.wait(tk)
+        el = time.perf_counter() - t0
+        best = el if best is None else min(best, el)
+    total_q = sum(t[1].shape[0] for t in templates)
+    peak_rps = n_templates / best
+    out = {"trees": n_trees, "points": int(ns.sum()), "build_all_s": build_s, "templates": n_templates,
+           "identical_to_lone_queries": identical,
+           "peak": {"requests_per_s": peak_rps, "queries_per_s": total_q / best}}
+    for frac in (0.5, 0.7, 0.9):
+        rate = frac * peak_rps
+        gaps = rng.exponential(1.0 / rate, int(rate * duration_s) + 1)
+        order = rng.integers(0, n_templates, len(gaps))
+        busy = [False] * n_templates
+        lock = threading.Lock()
+        pending = []
+        lat = []
+        done_q = [0]
+        cv = threading.Condition(lock)
+        finished = [False]
+
+        def waiter():
+            while True:
+                with cv:
+                    while not pending and not finished[0]:
+                        cv.wait()
+                    if not pending:
+                        return
+                    tk, j = pending.pop(0)
+                _, _, l = srv.wait(tk)
+                with cv:
+                    busy[j] = False
+                    lat.append(l)
+                    done_q[0] += templates[j][1].shape[0]
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        t_start = time.perf_counter()
+        t_next = t_start
+        for g, j in zip(gaps, order):
+            t_next += g
+            while time.perf_counter() < t_next:
+                pass
+            j = int(j)
+            with cv:
+                while busy[j]:
+                    j = (j + 1) % n_templates
+                busy[j] = True
+            ti, q, k, od, oi = templates[j]
+            tk = srv.submit(ti, q, k, out=(od, oi))
+            with cv:
+                pending.append((tk, j))
+                cv.notify()
+        with cv:
+            finished[0] = True
+            cv.notify()
+        th.join()
+        el = time.perf_counter() - t_start
+        lat_ms = np.array(lat) * 1e3
+        out[f"load_{int(frac * 100)}"] = {"offered_requests_per_s": rate, "requests": len(lat),
+                                          "p50_ms": float(np.percentile(lat_ms, 50)),
+                                          "p99_ms": float(np.percentile(lat_ms, 99)),
+                                          "sustained_queries_per_s": done_q[0] / el}
+    srv.close()
+    del trees
+    return out
+
+
+def grid_case(lib, torch, stream, dev, cpu_threads):
+    """The reference's small-size grid (tests/benchmark.py, benches/grid.rs):
+    d in {3, 8, 16}, N = 10,000, Q = 1,000, k = 1 -- the GPU build and query
+    times (host wall time of the synchronous C-ABI call, inputs in HBM for the
+    query) beside the oracle on all host cores."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from grid_workloads import build_cases, make_data, make_queries, query_cases
+
+    from kdtree import KDTree
+
+    out = {}
+    okd = None
+    if cpu_threads:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import kdtree_oracle as okd
+    for name, d, n, dist in build_cases():
+        data = make_data(dist, n, d)
+        KDTree(data, leafsize=16)
+        t0 = time.perf_counter()
+        for _ in range(5):
+            KDTree(data, leafsize=16)
+        case = {"gpu_ms": (time.perf_counter() - t0) / 5 * 1e3}
+        if okd:
+            t0 = time.perf_counter()
+            okd.OracleKDTree(data, leafsize=16)
+            case["cpu_ms"] = (time.perf_counter() - t0) * 1e3
+        out[name] = case
+    P = ctypes.c_void_p
+    for name, d, n, q, dist, leaf, p in query_cases():
+        data = make_data(dist, n, d)
+        qs = make_queries(q, d)
+        tree = KDTree(data, leafsize=leaf)
+        dq = torch.from_numpy(qs).to(dev)
+        od = torch.empty((q, 1), dtype=torch.float64, device=dev)
+        oi = torch.empty((q, 1), dtype=torch.int64, device=dev)
+
+        def call():
+            st = lib.kd_query_device(tree._h, P(dq.data_ptr()), dq.numel(), 1, p, 0, 0.0, 0.0, P(od.data_ptr()),
+                                     P(oi.data_ptr()), P(stream.cuda_stream))
+            if st:
+                raise RuntimeError("kd_query_device failed")
+
+        call()
+        t0 = time.perf_counter()
+        for _ in range(10):
+            call()
+        case = {"gpu_ms": (time.perf_counter() - t0) / 10 * 1e3}
+        if okd:
+            ot = okd.OracleKDTree(data, leafsize=leaf)
+            t0 = time.perf_counter()
+            ot.query(qs, k=1, p=p, threads=cpu_threads)
+            case["cpu_ms"] = (time.perf_counter() - t0) * 1e3
+        out[name] = case
+    return out
+
+
 def run_profile_tc():
     """A tensor-core-path case small enough for an ncu capture: one CTA-filling
     batch (152 x 128 queries) against 100,000 points, d=64, k=32."""
@@ -387,6 +566,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-cases", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--batched-only", action="store_true", help="only run the batched multi-tree case")
+    ap.add_argument("--serving-only", action="store_true", help="only run the serving case")
     ap.add_argument("--profile-tc", action="store_true",
                     help="only run the tensor-core path on a profiling-sized case (N=100k, d=64, "
                          "19,456 queries, k=32), 3 calls")
@@ -395,6 +575,11 @@ def main():
         return run_reference(args)
     if args.profile_tc:
         return run_profile_tc()
+    if args.serving_only:
+        import torch
+
+        print(json.dumps({"serving": serving_case(torch)}), flush=True)
+        return 0
     if args.batched_only:
         import torch
 
@@ -557,7 +742,9 @@ def main():
             ct = kdtree_oracle.max_threads()
         line["cases"] = {"plain_scale": plain_scale_cases(lib, torch, stream, dev),
                          "precision": precision_cases(lib, torch, stream, dev, ct),
-                         "batched": batched_case(torch, dev, stream)}
+                         "grid": grid_case(lib, torch, stream, dev, ct),
+                         "batched": batched_case(torch, dev, stream),
+                         "serving": serving_case(torch)}
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()

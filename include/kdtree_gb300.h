@@ -92,7 +92,7 @@ int kd_query_device(const kd_tree* tree, const double* d_queries, uint64_t n_val
  *   KD_PATH_AUTO            what kd_query / kd_query_device run
  *   KD_PATH_REFERENCE_ORDER one thread per query, the reference's depth-first
  *                           order (FP64 decisions; the only order for eps > 0)
- *   KD_PATH_PACKET          warp-shared traversal (d in {2, 3, 8}, eps = 0)
+ *   KD_PATH_PACKET          warp-shared traversal (d in {2, 3, 8, 16}, eps = 0, k <= 32)
  *   KD_PATH_TENSOR_CORE     tcgen05 BF16 distance filter + FP64 re-rank
  *                           (L2, eps = 0, 16 <= d <= 128, k <= 32)
  * A path that does not apply to a call falls back to the reference order. */
@@ -181,6 +181,40 @@ int kd_batch_run_mode(kd_batch* batch, void* stream, int mode);
 
 /* Release a plan (NULL is ignored). */
 void kd_batch_free(kd_batch* batch);
+
+/* ---- Serving: continuous batching over a fixed set of trees --------------
+ * No reference counterpart: a request loop in front of `Tree::query`
+ * (src/query.rs:29-78).  A scheduler thread forms a batch whenever one of two
+ * batch slots is free: every waiting request that fits the slot, in arrival
+ * order, runs as one batch (the kernels of kd_batch_run, plus per-request
+ * launches for requests outside the packet traversal).  A request's results
+ * are exactly kd_query's for the same tree and queries, whatever it is batched
+ * with. */
+typedef struct kd_server kd_server;
+
+/* Start a server over n_trees trees (all on the current device); p,
+ * max_distance and eps apply to every request and are validated as kd_query
+ * validates them.  max_batch_queries caps the queries of one batch (0: sized
+ * from free device memory, at most 2^20); the two slots' staging (queries, 64
+ * results per query on average) is allocated here. */
+int kd_server_create(const kd_tree* const* trees, uint64_t n_trees, double p, int has_max_distance,
+                     double max_distance, double eps, uint64_t max_batch_queries, kd_server** out);
+
+/* Queue a request for tree index `tree`: n_queries rows in HOST memory, k
+ * results each into host out_distances / out_indices (n_queries * k).  The
+ * three buffers must stay valid until kd_server_wait returns for the ticket.
+ * Validated as kd_query validates a call (k > 0, n_queries > 0); a request
+ * larger than one batch fails with KD_ERR_INVALID_ARGUMENT.  Returns at once. */
+int kd_server_submit(kd_server* server, uint64_t tree, const double* queries, uint64_t n_queries, uint64_t k,
+                     double* out_distances, int64_t* out_indices, uint64_t* ticket);
+
+/* Wait for a request; returns its status (KD_ERR_NONFINITE_DATA for a
+ * non-finite query) and, when latency_s is not NULL, the seconds from its
+ * submission to the completion of its batch.  Each ticket is waited for once. */
+int kd_server_wait(kd_server* server, uint64_t ticket, double* latency_s);
+
+/* Finish every queued request, stop the threads, release everything. */
+void kd_server_free(kd_server* server);
 
 /* Getters: `Tree::ndim`, `Tree::n_points`, `Tree::leafsize`
  * (src/tree.rs:48-58).  kd_n_nodes has no Python getter in the reference. */

@@ -1,32 +1,45 @@
-// kd_batch.cu -- many (tree, query batch) jobs in one pass on the device.
+// kd_batch.cu -- many (tree, query batch) jobs in one pass on the device: the
+// batch plan (kd_batch_*) and the serving loop built on it (kd_server_*).
 //
 // No reference counterpart: the reference answers one Tree::query call at a
 // time (src/query.rs:29-78); a batch is its caller's loop over many trees,
-// fused.  Running a plan:
+// fused.  Running a batch:
 //  1. one kernel walks every query of every packet job down its own tree to
 //     its landing leaf and counts it into bin (job, leaf); one scan over all
 //     bins and one scatter leave each job's queries grouped by landing leaf,
-//     jobs one after another in the batch order;
+//     jobs one after another in the batch order (jobs below SORT_MIN_QUERIES
+//     queries keep their own order: one bin);
 //  2. ONE persistent kernel: each warp takes the next task -- 32 consecutive
-//     positions of one job's sorted queries -- from a global counter and runs
-//     the packet traversal (kd_query_packet.cuh) for that job's width and k.
-//     Jobs are laid out most expensive class first, so the long tasks start
-//     early and the short ones fill the tail;
-//  3. jobs outside the packet traversal's envelope (general L^p, eps > 0,
-//     k > 32, widths other than 2, 3 and 8, the reference-order switch) run as
-//     ordinary per-job launches of the same kernels kd_query_device uses,
-//     without the tensor-core filter (its set-up allocates and synchronises).
+//     positions of one job's queries -- from a global counter and runs the
+//     packet traversal (kd_query_packet.cuh) for that job's width and k.  Jobs
+//     are laid out most expensive class first, so the long tasks start early
+//     and the short ones fill the tail;
+//  3. jobs outside the fused kernel's envelope (general L^p, eps > 0, k > 32,
+//     widths other than 2, 3 and 8, the reference-order switch) run as
+//     ordinary per-job launches of the kernels kd_query_device uses -- the
+//     packet traversal for width 16, the reference-order descent otherwise;
+//     never the tensor-core filter, whose brute-force scan only pays on
+//     trees that do not prune.
 // A query's result depends on that query and its tree alone, so every job
 // gets exactly what kd_query_device returns for it.
 //
-// The first graph run of a plan times a few launch shapes -- persistent grid
-// size and whether to sort -- and keeps the fastest (the autotuner), then
-// captures the whole sequence in a CUDA graph; later runs replay the graph.
+// A plan (kd_batch_create) fixes its jobs.  Its first graph run times a few
+// launch shapes -- persistent grid size, sorting on or off -- and keeps the
+// fastest (the autotuner), then captures the whole sequence in a CUDA graph;
+// later runs replay the graph.  The server (kd_server_create) forms a new batch
+// from the waiting requests whenever one of its two batch slots is free
+// (continuous batching), with the same kernels.
 #include <algorithm>
+#include <chrono>
+#include <condition_variable>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
+#include <mutex>
 #include <new>
+#include <thread>
 #include <type_traits>
+#include <unordered_map>
 #include <vector>
 
 #include "kd_internal.hpp"
@@ -41,10 +54,11 @@ namespace {
 
 constexpr uint32_t CLS_OTHER = 0xffffffffu;
 constexpr int BATCH_K[5] = {1, 4, 8, 16, 32};
+constexpr uint64_t SORT_MIN_QUERIES = 1024;
 
 // Packet class of a job: width index * 5 + k index, or CLS_OTHER.
-uint32_t packet_class(const kd_tree* t, const QueryParams& qp, bool reference_order) {
-  if (qp.metric == M_LP || qp.eps_factor != 1.0 || qp.k > 32 || t->n_points >= ROW_NONE || reference_order)
+uint32_t packet_class(const kd_tree* t, const QueryParams& qp, uint64_t k, bool reference_order) {
+  if (qp.metric == M_LP || qp.eps_factor != 1.0 || k > 32 || t->n_points >= ROW_NONE || reference_order)
     return CLS_OTHER;
   int di;
   switch (t->ndim) {
@@ -54,15 +68,23 @@ uint32_t packet_class(const kd_tree* t, const QueryParams& qp, bool reference_or
     default: return CLS_OTHER;
   }
   int ki = 0;
-  while (BATCH_K[ki] < static_cast<int>(qp.k)) ++ki;
+  while (BATCH_K[ki] < static_cast<int>(k)) ++ki;
   return static_cast<uint32_t>(di * 5 + ki);
 }
 
+bool reference_order_forced() {
+  static const bool force = [] {
+    const char* m = std::getenv("KD_QUERY_MODE");
+    return m && std::strcmp(m, "dfs") == 0;
+  }();
+  return force;
+}
+
 struct BatchJob {
-  QArgs a;             // the job's query arguments; a.order points into the batch order
+  QArgs a;             // the job's query arguments; a.order points into the batch order or is NULL
   uint64_t bin_start;  // the job's first landing-leaf bin
-  uint32_t cls;        // packet class or CLS_OTHER
-  uint32_t pad;
+  uint32_t cls;        // packet class
+  uint32_t sorted;     // 1: bins per node (sorted by landing leaf); 0: one bin
 };
 
 struct BatchArgs {
@@ -92,10 +114,9 @@ __global__ void k_batch_landing(const BatchJob* jobs, const uint32_t* q_start, u
   if (g >= total) return;
   const uint32_t j = find_range(q_start, n_jobs, g);
   const BatchJob& J = jobs[j];
-  const uint32_t i = g - q_start[j];
   uint32_t node = 0;
-  if (J.cls != CLS_OTHER) {
-    const double* q = J.a.queries + static_cast<uint64_t>(i) * J.a.d;
+  if (J.sorted) {
+    const double* q = J.a.queries + static_cast<uint64_t>(g - q_start[j]) * J.a.d;
     for (;;) {
       const DNode nd = J.a.nodes[node];
       if (nd.meta & KD_NODE_LEAF) break;
@@ -117,19 +138,20 @@ __global__ void k_batch_scatter(const uint32_t* q_start, uint32_t n_jobs, uint32
 }
 
 template <int M, int D, int K>
-__device__ __noinline__ void batch_task(const QArgs* a, uint64_t tid, float* lo, float* hi, uint32_t* row) {
-  packet_queries<M, D, K>(*a, tid, lo, hi, row);
+__device__ __noinline__ void batch_task(const QArgs* a, uint64_t tid, float* lo, float* hi, uint32_t* row,
+                                        uint32_t* stack) {
+  packet_queries<M, D, K>(*a, tid, lo, hi, row, stack);
 }
 
 template <int M, int D, int KMAX>
 __device__ __forceinline__ void run_k(uint32_t ki, const QArgs* a, uint64_t tid, float* lo, float* hi,
-                                      uint32_t* row) {
+                                      uint32_t* row, uint32_t* stack) {
   switch (ki) {
-    case 0: batch_task<M, D, 1>(a, tid, lo, hi, row); break;
-    case 1: if constexpr (KMAX >= 4) batch_task<M, D, 4>(a, tid, lo, hi, row); break;
-    case 2: if constexpr (KMAX >= 8) batch_task<M, D, 8>(a, tid, lo, hi, row); break;
-    case 3: if constexpr (KMAX >= 16) batch_task<M, D, 16>(a, tid, lo, hi, row); break;
-    default: if constexpr (KMAX >= 32) batch_task<M, D, 32>(a, tid, lo, hi, row); break;
+    case 0: batch_task<M, D, 1>(a, tid, lo, hi, row, stack); break;
+    case 1: if constexpr (KMAX >= 4) batch_task<M, D, 4>(a, tid, lo, hi, row, stack); break;
+    case 2: if constexpr (KMAX >= 8) batch_task<M, D, 8>(a, tid, lo, hi, row, stack); break;
+    case 3: if constexpr (KMAX >= 16) batch_task<M, D, 16>(a, tid, lo, hi, row, stack); break;
+    default: if constexpr (KMAX >= 32) batch_task<M, D, 32>(a, tid, lo, hi, row, stack); break;
   }
 }
 
@@ -148,24 +170,19 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query_batch(BatchArgs b) {
     const uint32_t cls = J->cls;
     const uint64_t tid = static_cast<uint64_t>(t - b.task_start[j]) * 32 + lane;
     switch (cls / 5) {
-      case 0: run_k<M, 2, KMAX>(cls % 5, &J->a, tid, sm.lo, sm.hi, sm.row); break;
-      case 1: run_k<M, 3, KMAX>(cls % 5, &J->a, tid, sm.lo, sm.hi, sm.row); break;
-      default: run_k<M, 8, KMAX>(cls % 5, &J->a, tid, sm.lo, sm.hi, sm.row); break;
+      case 0: run_k<M, 2, KMAX>(cls % 5, &J->a, tid, sm.lo, sm.hi, sm.row, sm.stack); break;
+      case 1: run_k<M, 3, KMAX>(cls % 5, &J->a, tid, sm.lo, sm.hi, sm.row, sm.stack); break;
+      default: run_k<M, 8, KMAX>(cls % 5, &J->a, tid, sm.lo, sm.hi, sm.row, sm.stack); break;
     }
   }
 }
 
-template <int M, int KMAX>
-cudaError_t launch_batch(const BatchArgs& b, unsigned blocks, cudaStream_t st) {
-  k_query_batch<M, KMAX><<<blocks, QUERY_THREADS, 0, st>>>(b);
-  return cudaGetLastError();
-}
-
 template <int M>
 cudaError_t launch_batch_k(const BatchArgs& b, int kmax, unsigned blocks, cudaStream_t st) {
-  if (kmax <= 4) return launch_batch<M, 4>(b, blocks, st);
-  if (kmax <= 16) return launch_batch<M, 16>(b, blocks, st);
-  return launch_batch<M, 32>(b, blocks, st);
+  if (kmax <= 4) k_query_batch<M, 4><<<blocks, QUERY_THREADS, 0, st>>>(b);
+  else if (kmax <= 16) k_query_batch<M, 16><<<blocks, QUERY_THREADS, 0, st>>>(b);
+  else k_query_batch<M, 32><<<blocks, QUERY_THREADS, 0, st>>>(b);
+  return cudaGetLastError();
 }
 
 template <int M, int KMAX>
@@ -189,12 +206,173 @@ int resident_blocks_per_sm(int metric, int kmax) {
   }
 }
 
-bool reference_order_forced() {
-  static const bool force = [] {
-    const char* m = std::getenv("KD_QUERY_MODE");
-    return m && std::strcmp(m, "dfs") == 0;
-  }();
-  return force;
+// ---------------------------------------------------------------------------
+// Host side: a batch's layout and its device buffers.
+// ---------------------------------------------------------------------------
+
+// One job as the batch code sees it: device buffers and a device status word.
+struct JobSpec {
+  const kd_tree* tree;
+  const double* queries;
+  uint64_t nq, k;
+  double* out_d;
+  int64_t* out_i;
+  uint32_t* status;
+};
+
+struct Layout {
+  std::vector<uint32_t> packet;  // spec ids of the packet jobs, in batch order
+  std::vector<uint32_t> other;   // spec ids run per job
+  std::vector<uint32_t> q_start, task_start;
+  std::vector<BatchJob> table;
+  uint64_t n_bins = 1;
+  uint32_t total_q = 0, n_tasks = 0;
+  int kmax = 1;
+};
+
+void fill_args(QArgs* a, const JobSpec& J, const QueryParams& qp) {
+  const kd_tree* t = J.tree;
+  *a = QArgs{};
+  a->data = t->data;
+  a->data32 = t->data32;
+  a->indices = t->indices;
+  a->nodes = t->nodes;
+  a->boxes = t->boxes;
+  a->boxes32 = t->boxes32;
+  a->coord_max = t->coord_max32;
+  a->queries = J.queries;
+  a->out_d = J.out_d;
+  a->out_i = J.out_i;
+  a->status = J.status;
+  a->nq = J.nq;
+  a->d = t->ndim;
+  a->k = J.k;
+  a->n_points = t->n_points;
+  a->p = qp.p;
+  a->cutoff = qp.cutoff;
+  a->eps_factor = qp.eps_factor;
+  a->use_eps = qp.eps_factor != 1.0;
+}
+
+// Lay the jobs out.  `order` is the device batch order (total packet queries
+// u32); sort = false gives every job one bin and no order.
+void make_layout(const std::vector<JobSpec>& specs, const QueryParams& qp, bool sort, uint32_t* order,
+                 Layout* L) {
+  *L = Layout{};
+  const bool ref = reference_order_forced();
+  std::vector<uint32_t> cls(specs.size());
+  for (size_t j = 0; j < specs.size(); ++j) {
+    cls[j] = packet_class(specs[j].tree, qp, specs[j].k, ref);
+    (cls[j] == CLS_OTHER ? L->other : L->packet).push_back(static_cast<uint32_t>(j));
+  }
+  // most expensive class first: larger k, then wider points
+  std::stable_sort(L->packet.begin(), L->packet.end(), [&](uint32_t x, uint32_t y) {
+    if (cls[x] % 5 != cls[y] % 5) return cls[x] % 5 > cls[y] % 5;
+    return cls[x] / 5 > cls[y] / 5;
+  });
+  const size_t n = L->packet.size();
+  L->q_start.assign(n + 1, 0);
+  L->task_start.assign(n + 1, 0);
+  L->table.resize(n);
+  uint64_t bins = 0;
+  for (size_t i = 0; i < n; ++i) {
+    const JobSpec& J = specs[L->packet[i]];
+    BatchJob& B = L->table[i];
+    fill_args(&B.a, J, qp);
+    B.cls = cls[L->packet[i]];
+    B.sorted = sort && J.nq >= SORT_MIN_QUERIES;
+    B.a.order = B.sorted ? order + L->q_start[i] : nullptr;
+    B.bin_start = bins;
+    bins += B.sorted ? J.tree->n_nodes : 1;
+    L->q_start[i + 1] = L->q_start[i] + static_cast<uint32_t>(J.nq);
+    L->task_start[i + 1] = L->task_start[i] + static_cast<uint32_t>((J.nq + 31) / 32);
+    L->kmax = std::max(L->kmax, BATCH_K[B.cls % 5]);
+  }
+  L->n_bins = std::max<uint64_t>(bins, 1);
+  L->total_q = L->q_start[n];
+  L->n_tasks = L->task_start[n];
+}
+
+// Device buffers of one batch, carved from one allocation.
+struct Buffers {
+  void* mem = nullptr;
+  BatchJob* jobs[2] = {nullptr, nullptr};
+  uint32_t* q_start = nullptr;
+  uint32_t* task_start = nullptr;
+  uint64_t* bin_of = nullptr;
+  uint32_t* order = nullptr;
+  uint32_t* bins = nullptr;
+  uint32_t* tile_sums = nullptr;
+  uint32_t* counter = nullptr;
+  uint64_t cap_jobs = 0, cap_q = 0, cap_bins = 0;
+  ~Buffers() {
+    if (mem) cudaFree(mem);
+  }
+};
+
+// Sizes of the carve-up; `extra` bytes at the end are the caller's.
+uint64_t round256(uint64_t x) { return (x + 255) & ~255ull; }
+
+int alloc_buffers(Buffers* B, uint64_t cap_jobs, uint64_t cap_q, uint64_t cap_bins, uint64_t extra, char** extra_p) {
+  cap_jobs = std::max<uint64_t>(cap_jobs, 1);
+  cap_q = std::max<uint64_t>(cap_q, 1);
+  cap_bins = std::max<uint64_t>(cap_bins, 1);
+  const uint64_t n_tiles = (cap_bins + SCAN_TILE - 1) / SCAN_TILE;
+  const uint64_t sz_jobs = round256(cap_jobs * sizeof(BatchJob));
+  const uint64_t sz_st = round256((cap_jobs + 1) * sizeof(uint32_t));
+  const uint64_t total = 2 * sz_jobs + 2 * sz_st + round256(cap_q * 8) + round256(cap_q * 4) +
+                         round256(cap_bins * 4) + round256(n_tiles * 4) + 256 + round256(extra);
+  cudaError_t e = cudaMalloc(&B->mem, total);
+  if (e != cudaSuccess) {
+    B->mem = nullptr;
+    return cuda_fail(e, "cudaMalloc");
+  }
+  char* m = static_cast<char*>(B->mem);
+  auto take = [&](uint64_t bytes) {
+    char* p = m;
+    m += bytes;
+    return p;
+  };
+  B->jobs[0] = reinterpret_cast<BatchJob*>(take(sz_jobs));
+  B->jobs[1] = reinterpret_cast<BatchJob*>(take(sz_jobs));
+  B->q_start = reinterpret_cast<uint32_t*>(take(sz_st));
+  B->task_start = reinterpret_cast<uint32_t*>(take(sz_st));
+  B->bin_of = reinterpret_cast<uint64_t*>(take(round256(cap_q * 8)));
+  B->order = reinterpret_cast<uint32_t*>(take(round256(cap_q * 4)));
+  B->bins = reinterpret_cast<uint32_t*>(take(round256(cap_bins * 4)));
+  B->tile_sums = reinterpret_cast<uint32_t*>(take(round256(n_tiles * 4)));
+  B->counter = reinterpret_cast<uint32_t*>(take(256));
+  if (extra_p) *extra_p = take(round256(extra));
+  B->cap_jobs = cap_jobs;
+  B->cap_q = cap_q;
+  B->cap_bins = cap_bins;
+  return KD_OK;
+}
+
+// Enqueue the sort and the persistent kernel of a layout whose table, q_start
+// and task_start are already in B (table in B->jobs[table]).
+int enqueue_packet(const Layout& L, const Buffers& B, int table, int metric, unsigned blocks, cudaStream_t st) {
+  if (!L.n_tasks) return KD_OK;
+  const uint32_t n = static_cast<uint32_t>(L.packet.size());
+  KD_TRY_CUDA(cudaMemsetAsync(B.bins, 0, L.n_bins * sizeof(uint32_t), st));
+  const unsigned qb = (L.total_q + 255) / 256;
+  k_batch_landing<<<qb, 256, 0, st>>>(B.jobs[table], B.q_start, n, L.total_q, B.bin_of, B.bins);
+  const uint64_t n_tiles = (L.n_bins + SCAN_TILE - 1) / SCAN_TILE;
+  k_scan_tiles<<<static_cast<unsigned>(n_tiles), SCAN_THREADS, 0, st>>>(B.bins, L.n_bins, B.tile_sums);
+  k_scan_sums<<<1, SCAN_THREADS, 0, st>>>(B.tile_sums, n_tiles);
+  k_scan_add<<<static_cast<unsigned>((L.n_bins + 255) / 256), 256, 0, st>>>(B.bins, L.n_bins, B.tile_sums);
+  k_batch_scatter<<<qb, 256, 0, st>>>(B.q_start, n, L.total_q, B.bin_of, B.bins, B.order);
+  KD_TRY_CUDA(cudaGetLastError());
+  KD_TRY_CUDA(cudaMemsetAsync(B.counter, 0, sizeof(uint32_t), st));
+  BatchArgs a{B.jobs[table], B.task_start, n, L.n_tasks, B.counter};
+  cudaError_t e;
+  switch (metric) {
+    case M_L1: e = launch_batch_k<M_L1>(a, L.kmax, blocks, st); break;
+    case M_L2: e = launch_batch_k<M_L2>(a, L.kmax, blocks, st); break;
+    default: e = launch_batch_k<M_LINF>(a, L.kmax, blocks, st); break;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "k_query_batch");
+  return KD_OK;
 }
 
 struct DeviceScope {
@@ -210,103 +388,74 @@ struct DeviceScope {
   }
 };
 
+int job_error(const kd_tree* tree, uint64_t nq, uint64_t k, const void* q, const void* od, const void* oi,
+              int dev, const std::string& who) {
+  if (!tree) return fail(KD_ERR_INVALID_ARGUMENT, who + ": tree is NULL");
+  if (k == 0) return fail(KD_ERR_INVALID_K, "k must be greater than zero");
+  if (nq == 0) return fail(KD_ERR_INVALID_SHAPE, "queries must be a contiguous row-major matrix");
+  if (!q || !od || !oi) return fail(KD_ERR_INVALID_ARGUMENT, who + ": NULL buffer");
+  if (tree->device != dev) return fail(KD_ERR_INVALID_ARGUMENT, who + ": tree lives on another device");
+  if (nq > (~0ull / sizeof(double)) / k / tree->ndim) return fail(KD_ERR_OUT_OF_MEMORY, "output would not fit in memory");
+  return KD_OK;
+}
+
 }  // namespace
 }  // namespace kd
 
 using namespace kd;
 
-// The plan behind the opaque kd_batch* of the C ABI.
+// ===========================================================================
+// The batch plan behind the opaque kd_batch* of the C ABI.
+// ===========================================================================
 struct kd_batch {
   int device = 0;
-  QueryParams qp{};
-  std::vector<kd_batch_job> jobs;       // caller's jobs, in caller order
-  std::vector<uint32_t> cls;            // packet class per caller job
-  std::vector<uint32_t> packet_order;   // caller job ids of packet jobs, batch order
-  std::vector<uint32_t> other;          // caller job ids run per job
-  std::vector<uint64_t> other_axes;     // offset of each other job in axes scratch
-  uint32_t total_q = 0;                 // queries of packet jobs
-  uint32_t n_tasks = 0;
-  uint64_t n_bins = 0;
-  int kmax = 1;
   int sms = 1;
-  // device memory (one allocation)
-  void* mem = nullptr;
-  BatchJob* jobs_sorted = nullptr;  // packet jobs, order = batch order
-  BatchJob* jobs_plain = nullptr;   // packet jobs, no order
-  uint32_t* q_start = nullptr;      // n_packet + 1
-  uint32_t* task_start = nullptr;   // n_packet + 1
-  uint64_t* bin_of = nullptr;       // total_q
-  uint32_t* order = nullptr;        // total_q
-  uint32_t* bins = nullptr;         // n_bins
-  uint32_t* tile_sums = nullptr;
-  uint32_t* counter = nullptr;
+  QueryParams qp{};
+  std::vector<JobSpec> specs;  // caller order
+  Layout layout[2];            // [0] sorted, [1] unsorted (same jobs and positions)
+  Buffers buf;
   uint32_t* status = nullptr;
-  double* axes = nullptr;           // other jobs' CellBound scratch
-  // tuned launch and the captured graph
+  double* axes = nullptr;              // other jobs' CellBound scratch
+  std::vector<uint64_t> axes_off;      // per other job (layout order)
   bool tuned = false;
   unsigned blocks = 0;
-  bool sort = true;
+  int table = 0;
   cudaStream_t capture_stream = nullptr;
   cudaGraphExec_t exec = nullptr;
 };
 
 namespace {
 
-// Enqueue one run of the plan on st: fused (sort + persistent kernel + other
-// jobs) or per job.
-int enqueue(kd_batch* b, cudaStream_t st, bool per_job, unsigned blocks, bool sort) {
+int enqueue_plan(kd_batch* b, cudaStream_t st, bool per_job, unsigned blocks, int table) {
   KD_TRY_CUDA(cudaMemsetAsync(b->status, 0, sizeof(uint32_t), st));
+  const Layout& L = b->layout[table];
   if (per_job) {
-    for (size_t j = 0; j < b->jobs.size(); ++j) {
-      const kd_batch_job& J = b->jobs[j];
+    for (uint32_t j : L.packet) {
+      const JobSpec& J = b->specs[j];
       QueryParams qp = b->qp;
       qp.k = J.k;
-      if (b->cls[j] == CLS_OTHER) continue;
-      int rc = query_on_device(J.tree, J.d_queries, J.n_queries, qp, J.d_out_distances, J.d_out_indices, st,
-                               b->status);
+      qp.path = PATH_PACKET;
+      int rc = query_on_device(J.tree, J.queries, J.nq, qp, J.out_d, J.out_i, st, b->status);
       if (rc) return rc;
     }
-  } else if (b->n_tasks) {
-    const uint32_t n_packet = static_cast<uint32_t>(b->packet_order.size());
-    if (sort) {
-      KD_TRY_CUDA(cudaMemsetAsync(b->bins, 0, b->n_bins * sizeof(uint32_t), st));
-      const unsigned qb = (b->total_q + 255) / 256;
-      k_batch_landing<<<qb, 256, 0, st>>>(b->jobs_sorted, b->q_start, n_packet, b->total_q, b->bin_of, b->bins);
-      const uint64_t n_tiles = (b->n_bins + SCAN_TILE - 1) / SCAN_TILE;
-      k_scan_tiles<<<static_cast<unsigned>(n_tiles), SCAN_THREADS, 0, st>>>(b->bins, b->n_bins, b->tile_sums);
-      k_scan_sums<<<1, SCAN_THREADS, 0, st>>>(b->tile_sums, n_tiles);
-      k_scan_add<<<static_cast<unsigned>((b->n_bins + 255) / 256), 256, 0, st>>>(b->bins, b->n_bins,
-                                                                                 b->tile_sums);
-      k_batch_scatter<<<qb, 256, 0, st>>>(b->q_start, n_packet, b->total_q, b->bin_of, b->bins, b->order);
-      KD_TRY_CUDA(cudaGetLastError());
-    }
-    KD_TRY_CUDA(cudaMemsetAsync(b->counter, 0, sizeof(uint32_t), st));
-    BatchArgs a{sort ? b->jobs_sorted : b->jobs_plain, b->task_start, n_packet, b->n_tasks, b->counter};
-    cudaError_t e;
-    switch (b->qp.metric) {
-      case M_L1: e = launch_batch_k<M_L1>(a, b->kmax, blocks, st); break;
-      case M_L2: e = launch_batch_k<M_L2>(a, b->kmax, blocks, st); break;
-      default: e = launch_batch_k<M_LINF>(a, b->kmax, blocks, st); break;
-    }
-    if (e != cudaSuccess) return cuda_fail(e, "k_query_batch");
+  } else {
+    int rc = enqueue_packet(L, b->buf, table, b->qp.metric, blocks, st);
+    if (rc) return rc;
   }
-  for (size_t o = 0; o < b->other.size(); ++o) {
-    const kd_batch_job& J = b->jobs[b->other[o]];
+  for (size_t o = 0; o < L.other.size(); ++o) {
+    const JobSpec& J = b->specs[L.other[o]];
     QueryParams qp = b->qp;
     qp.k = J.k;
-    int rc;
-    if (per_job)
-      rc = query_on_device(J.tree, J.d_queries, J.n_queries, qp, J.d_out_distances, J.d_out_indices, st,
-                           b->status);
-    else
-      rc = query_on_device_scratch(J.tree, J.d_queries, J.n_queries, qp, J.d_out_distances, J.d_out_indices, st,
-                                   b->status, b->axes + b->other_axes[o]);
+    qp.path = PATH_PACKET;  // never the tensor-core filter inside a batch
+    int rc = per_job ? query_on_device(J.tree, J.queries, J.nq, qp, J.out_d, J.out_i, st, b->status)
+                     : query_on_device_scratch(J.tree, J.queries, J.nq, qp, J.out_d, J.out_i, st, b->status,
+                                               b->axes + b->axes_off[o]);
     if (rc) return rc;
   }
   return KD_OK;
 }
 
-int finish(kd_batch* b, cudaStream_t st) {
+int finish_plan(kd_batch* b, cudaStream_t st) {
   uint32_t h = 0;
   KD_TRY_CUDA(cudaMemcpyAsync(&h, b->status, sizeof h, cudaMemcpyDeviceToHost, st));
   KD_TRY_CUDA(cudaStreamSynchronize(st));
@@ -317,7 +466,7 @@ int finish(kd_batch* b, cudaStream_t st) {
 // The autotuner: every candidate launch shape runs the plan once to warm up
 // and twice timed; the fastest is kept.  Results are identical for all.
 int tune(kd_batch* b, cudaStream_t st) {
-  const int per_sm = resident_blocks_per_sm(b->qp.metric, b->kmax);
+  const int per_sm = resident_blocks_per_sm(b->qp.metric, b->layout[0].kmax);
   std::vector<unsigned> grids;
   for (int m : {1, 2, 4, 8})
     if (m <= per_sm) grids.push_back(static_cast<unsigned>(b->sms * m));
@@ -326,17 +475,20 @@ int tune(kd_batch* b, cudaStream_t st) {
   grids.erase(std::unique(grids.begin(), grids.end()), grids.end());
   cudaEvent_t e0, e1;
   KD_TRY_CUDA(cudaEventCreate(&e0));
-  KD_TRY_CUDA(cudaEventCreate(&e1));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return cuda_fail(cudaErrorMemoryAllocation, "cudaEventCreate");
+  }
   float best = 1e30f;
   int rc = KD_OK;
-  for (bool sort : {true, false}) {
+  for (int table = 0; table < 2 && rc == KD_OK; ++table) {
     for (unsigned g : grids) {
       float t_min = 1e30f;
       for (int rep = 0; rep < 3 && rc == KD_OK; ++rep) {
         cudaEventRecord(e0, st);
-        rc = enqueue(b, st, false, g, sort);
+        rc = enqueue_plan(b, st, false, g, table);
         cudaEventRecord(e1, st);
-        if (rc == KD_OK) rc = finish(b, st);
+        if (rc == KD_OK) rc = finish_plan(b, st);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
         if (rep > 0) t_min = std::min(t_min, ms);
@@ -345,7 +497,7 @@ int tune(kd_batch* b, cudaStream_t st) {
       if (t_min < best) {
         best = t_min;
         b->blocks = g;
-        b->sort = sort;
+        b->table = table;
       }
     }
   }
@@ -359,7 +511,7 @@ int capture(kd_batch* b) {
   if (!b->capture_stream) KD_TRY_CUDA(cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking));
   cudaGraph_t g = nullptr;
   KD_TRY_CUDA(cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal));
-  const int rc = enqueue(b, b->capture_stream, false, b->blocks, b->sort);
+  const int rc = enqueue_plan(b, b->capture_stream, false, b->blocks, b->table);
   cudaError_t e = cudaStreamEndCapture(b->capture_stream, &g);
   if (rc) {
     if (g) cudaGraphDestroy(g);
@@ -375,19 +527,245 @@ int capture(kd_batch* b) {
   return KD_OK;
 }
 
-void release(kd_batch* b) {
+void release_plan(kd_batch* b) {
   if (!b) return;
   DeviceScope scope(b->device);
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
-  if (b->mem) cudaFree(b->mem);
-  delete b;
+  delete b;  // frees buf
+}
+
+}  // namespace
+
+// ===========================================================================
+// The server behind the opaque kd_server* of the C ABI.
+// ===========================================================================
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+  uint64_t ticket = 0;
+  uint32_t tree = 0;
+  const double* q = nullptr;
+  uint64_t nq = 0, k = 0;
+  double* od = nullptr;
+  int64_t* oi = nullptr;
+  Clock::time_point t_submit;
+  double latency = 0.0;
+  int status = KD_OK;
+  bool done = false;
+};
+
+// One batch in flight: device staging, batch buffers, pinned host tables.
+struct Slot {
+  cudaStream_t st = nullptr;
+  cudaEvent_t done = nullptr;
+  Buffers buf;
+  double* in = nullptr;        // staged queries
+  double* out_d = nullptr;     // staged distances
+  int64_t* out_i = nullptr;    // staged indices
+  uint32_t* status = nullptr;  // one word per job
+  void* host = nullptr;        // pinned: tables, q_start, task_start, status words
+  std::vector<Request*> reqs;
+  int error = KD_OK;
+  std::string error_msg;
+  bool busy = false;
+};
+
+}  // namespace
+
+struct kd_server {
+  int device = 0;
+  int sms = 1;
+  QueryParams qp{};
+  std::vector<const kd_tree*> trees;
+  uint64_t cap_q = 0, cap_in = 0, cap_out = 0, cap_jobs = 0, cap_bins = 0;
+  Slot slots[2];
+  std::mutex mu;
+  std::condition_variable cv;  // queue, slots, completions
+  std::deque<Request*> queue;
+  std::deque<Slot*> inflight;
+  std::unordered_map<uint64_t, Request*> reqs;
+  uint64_t next_ticket = 1;
+  bool stop = false;
+  std::thread scheduler, completer;
+};
+
+namespace {
+
+constexpr uint64_t SERVER_JOBS = 4096;
+
+uint64_t host_bytes(const kd_server* s) {
+  return round256(s->cap_jobs * sizeof(BatchJob)) + 2 * round256((s->cap_jobs + 1) * 4) +
+         round256(s->cap_jobs * 4);
+}
+
+// Stage one batch of requests on slot `sl` (called without the lock).
+int stage_batch(kd_server* s, Slot* sl) {
+  DeviceScope scope(s->device);
+  cudaStream_t st = sl->st;
+  const size_t n = sl->reqs.size();
+  std::vector<JobSpec> specs(n);
+  uint64_t in_off = 0, out_off = 0;
+  for (size_t j = 0; j < n; ++j) {
+    Request* r = sl->reqs[j];
+    const kd_tree* t = s->trees[r->tree];
+    specs[j] = JobSpec{t, sl->in + in_off, r->nq, r->k, sl->out_d + out_off, sl->out_i + out_off, sl->status + j};
+    KD_TRY_CUDA(cudaMemcpyAsync(sl->in + in_off, r->q, r->nq * t->ndim * sizeof(double), cudaMemcpyHostToDevice, st));
+    in_off += r->nq * t->ndim;
+    out_off += r->nq * r->k;
+  }
+  KD_TRY_CUDA(cudaMemsetAsync(sl->status, 0, n * sizeof(uint32_t), st));
+  Layout L;
+  make_layout(specs, s->qp, true, sl->buf.order, &L);
+  char* h = static_cast<char*>(sl->host);
+  BatchJob* h_jobs = reinterpret_cast<BatchJob*>(h);
+  uint32_t* h_qs = reinterpret_cast<uint32_t*>(h + round256(s->cap_jobs * sizeof(BatchJob)));
+  uint32_t* h_ts = h_qs + round256((s->cap_jobs + 1) * 4) / 4;
+  const size_t np = L.packet.size();
+  if (np) {
+    std::memcpy(h_jobs, L.table.data(), np * sizeof(BatchJob));
+    std::memcpy(h_qs, L.q_start.data(), (np + 1) * 4);
+    std::memcpy(h_ts, L.task_start.data(), (np + 1) * 4);
+    KD_TRY_CUDA(cudaMemcpyAsync(sl->buf.jobs[0], h_jobs, np * sizeof(BatchJob), cudaMemcpyHostToDevice, st));
+    KD_TRY_CUDA(cudaMemcpyAsync(sl->buf.q_start, h_qs, (np + 1) * 4, cudaMemcpyHostToDevice, st));
+    KD_TRY_CUDA(cudaMemcpyAsync(sl->buf.task_start, h_ts, (np + 1) * 4, cudaMemcpyHostToDevice, st));
+    const unsigned blocks = static_cast<unsigned>(s->sms * resident_blocks_per_sm(s->qp.metric, L.kmax));
+    int rc = enqueue_packet(L, sl->buf, 0, s->qp.metric, blocks, st);
+    if (rc) return rc;
+  }
+  for (uint32_t j : L.other) {
+    const JobSpec& J = specs[j];
+    QueryParams qp = s->qp;
+    qp.k = J.k;
+    qp.path = PATH_PACKET;
+    int rc = query_on_device(J.tree, J.queries, J.nq, qp, J.out_d, J.out_i, st, J.status);
+    if (rc) return rc;
+  }
+  KD_TRY_CUDA(cudaEventRecord(sl->done, st));
+  return KD_OK;
+}
+
+// Results of a computed batch into the requests' host buffers (issued by the
+// completion thread, so a pageable destination never blocks the scheduler).
+int deliver_batch(Slot* sl, uint32_t* h_status) {
+  cudaStream_t st = sl->st;
+  uint64_t out_off = 0;
+  for (Request* r : sl->reqs) {
+    KD_TRY_CUDA(cudaMemcpyAsync(r->od, sl->out_d + out_off, r->nq * r->k * sizeof(double), cudaMemcpyDeviceToHost, st));
+    KD_TRY_CUDA(cudaMemcpyAsync(r->oi, sl->out_i + out_off, r->nq * r->k * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    out_off += r->nq * r->k;
+  }
+  KD_TRY_CUDA(cudaMemcpyAsync(h_status, sl->status, sl->reqs.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  KD_TRY_CUDA(cudaStreamSynchronize(st));
+  return KD_OK;
+}
+
+void scheduler_loop(kd_server* s) {
+  std::unique_lock<std::mutex> lk(s->mu);
+  for (;;) {
+    Slot* free_slot = nullptr;
+    s->cv.wait(lk, [&] {
+      free_slot = !s->slots[0].busy ? &s->slots[0] : (!s->slots[1].busy ? &s->slots[1] : nullptr);
+      return (s->stop && s->queue.empty()) || (free_slot && !s->queue.empty());
+    });
+    if (s->queue.empty()) return;  // stopping, nothing left
+    // continuous batching: every waiting request that fits, in arrival order
+    Slot* sl = free_slot;
+    sl->busy = true;
+    sl->reqs.clear();
+    uint64_t q = 0, in = 0, out = 0, bins = 0;
+    while (!s->queue.empty() && sl->reqs.size() < s->cap_jobs) {
+      Request* r = s->queue.front();
+      const kd_tree* t = s->trees[r->tree];
+      const uint64_t nb = r->nq >= SORT_MIN_QUERIES ? t->n_nodes : 1;
+      if (!sl->reqs.empty() && (q + r->nq > s->cap_q || in + r->nq * t->ndim > s->cap_in ||
+                                out + r->nq * r->k > s->cap_out || bins + nb > s->cap_bins))
+        break;
+      q += r->nq;
+      in += r->nq * t->ndim;
+      out += r->nq * r->k;
+      bins += nb;
+      sl->reqs.push_back(r);
+      s->queue.pop_front();
+    }
+    lk.unlock();
+    const int rc = stage_batch(s, sl);
+    lk.lock();
+    sl->error = rc;
+    if (rc) sl->error_msg = "batch failed: status " + std::to_string(rc);
+    s->inflight.push_back(sl);
+    s->cv.notify_all();
+  }
+}
+
+void completer_loop(kd_server* s) {
+  std::unique_lock<std::mutex> lk(s->mu);
+  for (;;) {
+    s->cv.wait(lk, [&] { return !s->inflight.empty() || (s->stop && s->queue.empty() && !s->slots[0].busy &&
+                                                            !s->slots[1].busy); });
+    if (s->inflight.empty()) return;
+    Slot* sl = s->inflight.front();
+    lk.unlock();
+    int err = sl->error;
+    uint32_t* h_status = reinterpret_cast<uint32_t*>(static_cast<char*>(sl->host) +
+                                                     round256(s->cap_jobs * sizeof(BatchJob)) +
+                                                     2 * round256((s->cap_jobs + 1) * 4));
+    {
+      DeviceScope scope(s->device);
+      if (!err) {
+        cudaError_t e = cudaEventSynchronize(sl->done);
+        err = e != cudaSuccess ? cuda_fail(e, "cudaEventSynchronize") : deliver_batch(sl, h_status);
+      }
+      if (err) cudaStreamSynchronize(sl->st);  // let whatever was staged drain
+    }
+    const Clock::time_point now = Clock::now();
+    lk.lock();
+    for (size_t j = 0; j < sl->reqs.size(); ++j) {
+      Request* r = sl->reqs[j];
+      r->status = err ? err : (h_status[j] ? KD_ERR_NONFINITE_DATA : KD_OK);
+      r->latency = std::chrono::duration<double>(now - r->t_submit).count();
+      r->done = true;
+    }
+    sl->reqs.clear();
+    sl->busy = false;
+    s->inflight.pop_front();
+    s->cv.notify_all();
+  }
+}
+
+void release_server(kd_server* s) {
+  if (!s) return;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv.notify_all();
+  if (s->scheduler.joinable()) s->scheduler.join();
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+  }
+  s->cv.notify_all();
+  if (s->completer.joinable()) s->completer.join();
+  DeviceScope scope(s->device);
+  for (Slot& sl : s->slots) {
+    if (sl.st) cudaStreamSynchronize(sl.st);
+    if (sl.done) cudaEventDestroy(sl.done);
+    if (sl.st) cudaStreamDestroy(sl.st);
+    if (sl.host) cudaFreeHost(sl.host);
+  }
+  for (auto& kv : s->reqs) delete kv.second;
+  delete s;
 }
 
 }  // namespace
 
 extern "C" {
 
+// ---------------------------------------------------------------------------
+// Batch plans
+// ---------------------------------------------------------------------------
 int kd_batch_create(const kd_batch_job* jobs, uint64_t n_jobs, double p, int has_max_distance, double max_distance,
                     double eps, kd_batch** out) {
   if (!out) return fail(KD_ERR_INVALID_ARGUMENT, "out is NULL");
@@ -403,146 +781,60 @@ int kd_batch_create(const kd_batch_job* jobs, uint64_t n_jobs, double p, int has
   std::string msg;
   int rc = validate_scalars(1, p, has_max_distance, max_distance, eps, &qp, &msg);
   if (rc) return fail(rc, msg);
+  for (uint64_t j = 0; j < n_jobs; ++j) {
+    const kd_batch_job& J = jobs[j];
+    if ((rc = job_error(J.tree, J.n_queries, J.k, J.d_queries, J.d_out_distances, J.d_out_indices, dev,
+                        "job " + std::to_string(j))))
+      return rc;
+  }
   kd_batch* b = new (std::nothrow) kd_batch();
   if (!b) return fail(KD_ERR_OUT_OF_MEMORY, "host allocation failed");
   b->device = dev;
   b->qp = qp;
-  b->jobs.assign(jobs, jobs + n_jobs);
-  const bool ref = reference_order_forced();
-  uint64_t total_q = 0, axes_words = 0;
+  cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
+  uint64_t total_q = 0, axes_words = 0, bins = 0;
   for (uint64_t j = 0; j < n_jobs; ++j) {
     const kd_batch_job& J = jobs[j];
-    if (!J.tree) rc = fail(KD_ERR_INVALID_ARGUMENT, "job " + std::to_string(j) + ": tree is NULL");
-    else if (J.k == 0) rc = fail(KD_ERR_INVALID_K, "k must be greater than zero");
-    else if (J.n_queries == 0)
-      rc = fail(KD_ERR_INVALID_SHAPE, "queries must be a contiguous row-major matrix");
-    else if (!J.d_queries || !J.d_out_distances || !J.d_out_indices)
-      rc = fail(KD_ERR_INVALID_ARGUMENT, "job " + std::to_string(j) + ": NULL buffer");
-    else if (J.tree->device != dev)
-      rc = fail(KD_ERR_INVALID_ARGUMENT, "job " + std::to_string(j) + ": tree lives on another device");
-    else if (J.n_queries > (~0ull / sizeof(double)) / J.k / J.tree->ndim)
-      rc = fail(KD_ERR_OUT_OF_MEMORY, "output would not fit in memory");
-    if (rc) {
-      delete b;
-      return rc;
-    }
-    QueryParams jq = qp;
-    jq.k = J.k;
-    const uint32_t c = packet_class(J.tree, jq, ref);
-    b->cls.push_back(c);
-    if (c == CLS_OTHER) {
-      b->other.push_back(static_cast<uint32_t>(j));
-      b->other_axes.push_back(axes_words);
-      axes_words += J.n_queries * J.tree->ndim;
-    } else {
-      b->packet_order.push_back(static_cast<uint32_t>(j));
-      total_q += J.n_queries;
-      b->kmax = std::max(b->kmax, BATCH_K[c % 5]);
-    }
+    b->specs.push_back(JobSpec{J.tree, J.d_queries, J.n_queries, J.k, J.d_out_distances, J.d_out_indices, nullptr});
+    total_q += J.n_queries;
+    bins += J.tree->n_nodes;
+    axes_words += J.n_queries * J.tree->ndim;
   }
   if (total_q >= 0xffffffffull) {
     delete b;
     return fail(KD_ERR_INVALID_ARGUMENT, "a batch holds at most 2^32 - 1 queries");
   }
-  // most expensive class first: larger k, then wider points
-  std::stable_sort(b->packet_order.begin(), b->packet_order.end(), [&](uint32_t x, uint32_t y) {
-    const uint32_t cx = b->cls[x], cy = b->cls[y];
-    if (cx % 5 != cy % 5) return cx % 5 > cy % 5;
-    return cx / 5 > cy / 5;
-  });
-  const uint32_t n_packet = static_cast<uint32_t>(b->packet_order.size());
-  std::vector<uint32_t> q_start(n_packet + 1), task_start(n_packet + 1);
-  std::vector<uint64_t> bin_start(n_packet + 1);
-  for (uint32_t i = 0; i < n_packet; ++i) {
-    const kd_batch_job& J = jobs[b->packet_order[i]];
-    q_start[i + 1] = q_start[i] + static_cast<uint32_t>(J.n_queries);
-    task_start[i + 1] = task_start[i] + static_cast<uint32_t>((J.n_queries + 31) / 32);
-    bin_start[i + 1] = bin_start[i] + J.tree->n_nodes;
-  }
-  b->total_q = static_cast<uint32_t>(total_q);
-  b->n_tasks = task_start[n_packet];
-  b->n_bins = std::max<uint64_t>(bin_start[n_packet], 1);
-  const uint64_t n_tiles = (b->n_bins + SCAN_TILE - 1) / SCAN_TILE;
-  cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
-
-  // one device allocation, 256-byte aligned pieces
-  auto up = [](uint64_t x) { return (x + 255) & ~255ull; };
-  const uint64_t sz_jobs = up(std::max<uint32_t>(n_packet, 1) * sizeof(BatchJob));
-  const uint64_t sz_qs = up((n_packet + 1) * sizeof(uint32_t));
-  const uint64_t sz_binof = up(std::max<uint64_t>(total_q, 1) * sizeof(uint64_t));
-  const uint64_t sz_order = up(std::max<uint64_t>(total_q, 1) * sizeof(uint32_t));
-  const uint64_t sz_bins = up(b->n_bins * sizeof(uint32_t));
-  const uint64_t sz_tiles = up(n_tiles * sizeof(uint32_t));
-  const uint64_t sz_axes = up(std::max<uint64_t>(axes_words, 1) * sizeof(double));
-  const uint64_t total = 2 * sz_jobs + 2 * sz_qs + sz_binof + sz_order + sz_bins + sz_tiles + 512 + sz_axes;
-  cudaError_t e = cudaMalloc(&b->mem, total);
-  if (e != cudaSuccess) {
+  char* extra = nullptr;
+  if ((rc = alloc_buffers(&b->buf, n_jobs, total_q, bins, 256 + axes_words * sizeof(double), &extra))) {
     delete b;
-    return cuda_fail(e, "cudaMalloc");
+    return rc;
   }
-  char* m = static_cast<char*>(b->mem);
-  b->jobs_sorted = reinterpret_cast<BatchJob*>(m);
-  m += sz_jobs;
-  b->jobs_plain = reinterpret_cast<BatchJob*>(m);
-  m += sz_jobs;
-  b->q_start = reinterpret_cast<uint32_t*>(m);
-  m += sz_qs;
-  b->task_start = reinterpret_cast<uint32_t*>(m);
-  m += sz_qs;
-  b->bin_of = reinterpret_cast<uint64_t*>(m);
-  m += sz_binof;
-  b->order = reinterpret_cast<uint32_t*>(m);
-  m += sz_order;
-  b->bins = reinterpret_cast<uint32_t*>(m);
-  m += sz_bins;
-  b->tile_sums = reinterpret_cast<uint32_t*>(m);
-  m += sz_tiles;
-  b->counter = reinterpret_cast<uint32_t*>(m);
-  b->status = reinterpret_cast<uint32_t*>(m + 256);
-  m += 512;
-  b->axes = reinterpret_cast<double*>(m);
-
-  std::vector<BatchJob> hs(n_packet), hp(n_packet);
-  for (uint32_t i = 0; i < n_packet; ++i) {
-    const kd_batch_job& J = jobs[b->packet_order[i]];
-    const kd_tree* t = J.tree;
-    QArgs a{};
-    a.data = t->data;
-    a.data32 = t->data32;
-    a.indices = t->indices;
-    a.nodes = t->nodes;
-    a.boxes = t->boxes;
-    a.boxes32 = t->boxes32;
-    a.coord_max = t->coord_max32;
-    a.queries = J.d_queries;
-    a.out_d = J.d_out_distances;
-    a.out_i = J.d_out_indices;
-    a.status = b->status;
-    a.nq = J.n_queries;
-    a.d = t->ndim;
-    a.k = J.k;
-    a.n_points = t->n_points;
-    a.p = qp.p;
-    a.cutoff = qp.cutoff;
-    a.eps_factor = qp.eps_factor;
-    a.use_eps = 0;
-    hs[i].a = a;
-    hs[i].a.order = b->order + q_start[i];
-    hs[i].bin_start = bin_start[i];
-    hs[i].cls = b->cls[b->packet_order[i]];
-    hp[i] = hs[i];
-    hp[i].a.order = nullptr;
+  b->status = reinterpret_cast<uint32_t*>(extra);
+  b->axes = reinterpret_cast<double*>(extra + 256);
+  for (JobSpec& J : b->specs) J.status = b->status;
+  make_layout(b->specs, qp, true, b->buf.order, &b->layout[0]);
+  make_layout(b->specs, qp, false, b->buf.order, &b->layout[1]);
+  uint64_t off = 0;
+  for (uint32_t j : b->layout[0].other) {
+    b->axes_off.push_back(off);
+    off += b->specs[j].nq * b->specs[j].tree->ndim;
   }
-  e = cudaMemcpy(b->jobs_sorted, hs.data(), n_packet * sizeof(BatchJob), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(b->jobs_plain, hp.data(), n_packet * sizeof(BatchJob), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemcpy(b->q_start, q_start.data(), q_start.size() * 4, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess)
-    e = cudaMemcpy(b->task_start, task_start.data(), task_start.size() * 4, cudaMemcpyHostToDevice);
+  const Layout& L = b->layout[0];
+  const size_t np = L.packet.size();
+  cudaError_t e = cudaSuccess;
+  if (np) {
+    e = cudaMemcpy(b->buf.jobs[0], b->layout[0].table.data(), np * sizeof(BatchJob), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->buf.jobs[1], b->layout[1].table.data(), np * sizeof(BatchJob), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->buf.q_start, L.q_start.data(), (np + 1) * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->buf.task_start, L.task_start.data(), (np + 1) * 4, cudaMemcpyHostToDevice);
+  }
   if (e != cudaSuccess) {
-    release(b);
+    release_plan(b);
     return cuda_fail(e, "cudaMemcpy");
   }
-  b->blocks = static_cast<unsigned>(b->sms * resident_blocks_per_sm(qp.metric, b->kmax));
+  b->blocks = static_cast<unsigned>(b->sms * resident_blocks_per_sm(qp.metric, L.kmax));
   *out = b;
   return KD_OK;
 }
@@ -557,14 +849,149 @@ int kd_batch_run_mode(kd_batch* b, void* stream, int mode) {
     if (!b->tuned && (rc = tune(b, st))) return rc;
     if (!b->exec && (rc = capture(b))) return rc;
     KD_TRY_CUDA(cudaGraphLaunch(b->exec, st));
-  } else if ((rc = enqueue(b, st, mode == KD_BATCH_PER_JOB, b->blocks, b->sort))) {
+  } else if ((rc = enqueue_plan(b, st, mode == KD_BATCH_PER_JOB, b->blocks, b->table))) {
     return rc;
   }
-  return finish(b, st);
+  return finish_plan(b, st);
 }
 
 int kd_batch_run(kd_batch* b, void* stream) { return kd_batch_run_mode(b, stream, KD_BATCH_GRAPH); }
 
-void kd_batch_free(kd_batch* b) { release(b); }
+void kd_batch_free(kd_batch* b) { release_plan(b); }
+
+// ---------------------------------------------------------------------------
+// Server
+// ---------------------------------------------------------------------------
+int kd_server_create(const kd_tree* const* trees, uint64_t n_trees, double p, int has_max_distance,
+                     double max_distance, double eps, uint64_t max_batch_queries, kd_server** out) {
+  if (!out) return fail(KD_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  if (!trees || n_trees == 0) return fail(KD_ERR_INVALID_ARGUMENT, "a server needs at least one tree");
+  if (n_trees >= 0xffffffffull) return fail(KD_ERR_INVALID_ARGUMENT, "too many trees");
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(KD_ERR_NO_DEVICE, "no CUDA device is visible; the GB300 engine has no CPU fallback");
+  }
+  QueryParams qp{};
+  std::string msg;
+  int rc = validate_scalars(1, p, has_max_distance, max_distance, eps, &qp, &msg);
+  if (rc) return fail(rc, msg);
+  uint64_t dmax = 1, nodes = 0, nodes_max = 0;
+  for (uint64_t i = 0; i < n_trees; ++i) {
+    if (!trees[i]) return fail(KD_ERR_INVALID_ARGUMENT, "tree " + std::to_string(i) + " is NULL");
+    if (trees[i]->device != dev)
+      return fail(KD_ERR_INVALID_ARGUMENT, "tree " + std::to_string(i) + " lives on another device");
+    dmax = std::max(dmax, trees[i]->ndim);
+    nodes += trees[i]->n_nodes;
+    nodes_max = std::max(nodes_max, trees[i]->n_nodes);
+  }
+  kd_server* s = new (std::nothrow) kd_server();
+  if (!s) return fail(KD_ERR_OUT_OF_MEMORY, "host allocation failed");
+  s->device = dev;
+  s->qp = qp;
+  s->trees.assign(trees, trees + n_trees);
+  cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, dev);
+  // Batch capacity: the requested number of queries, or what a quarter of the
+  // free device memory holds (two slots) at the widest tree and 64 results per
+  // query, at most 2^20 queries.
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  const uint64_t per_q = dmax * 8 + 64 * 16 + 16;
+  uint64_t cap = max_batch_queries ? max_batch_queries : std::min<uint64_t>(1ull << 20, free_b / 8 / per_q);
+  cap = std::max<uint64_t>(cap, 1024);
+  s->cap_q = cap;
+  s->cap_in = cap * dmax;
+  s->cap_out = cap * 64;
+  s->cap_jobs = SERVER_JOBS;
+  s->cap_bins = std::max(2 * nodes, nodes_max + SERVER_JOBS);
+  for (Slot& sl : s->slots) {
+    char* extra = nullptr;
+    const uint64_t extra_b = round256(s->cap_in * 8) + round256(s->cap_out * 8) * 2 + round256(SERVER_JOBS * 4);
+    if ((rc = alloc_buffers(&sl.buf, SERVER_JOBS, cap, s->cap_bins, extra_b, &extra))) {
+      release_server(s);
+      return rc;
+    }
+    sl.in = reinterpret_cast<double*>(extra);
+    extra += round256(s->cap_in * 8);
+    sl.out_d = reinterpret_cast<double*>(extra);
+    extra += round256(s->cap_out * 8);
+    sl.out_i = reinterpret_cast<int64_t*>(extra);
+    extra += round256(s->cap_out * 8);
+    sl.status = reinterpret_cast<uint32_t*>(extra);
+    cudaError_t e = cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaHostAlloc(&sl.host, host_bytes(s) + round256(SERVER_JOBS * 4), cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+      sl.host = nullptr;
+      release_server(s);
+      return cuda_fail(e, "server set-up");
+    }
+  }
+  try {
+    s->scheduler = std::thread(scheduler_loop, s);
+    s->completer = std::thread(completer_loop, s);
+  } catch (...) {
+    release_server(s);
+    return fail(KD_ERR_OUT_OF_MEMORY, "could not start the server threads");
+  }
+  *out = s;
+  return KD_OK;
+}
+
+int kd_server_submit(kd_server* s, uint64_t tree, const double* queries, uint64_t n_queries, uint64_t k,
+                     double* out_distances, int64_t* out_indices, uint64_t* ticket) {
+  if (!s || !ticket) return fail(KD_ERR_INVALID_ARGUMENT, "server or ticket is NULL");
+  if (tree >= s->trees.size()) return fail(KD_ERR_INVALID_ARGUMENT, "no tree " + std::to_string(tree));
+  const kd_tree* t = s->trees[tree];
+  int rc = job_error(t, n_queries, k, queries, out_distances, out_indices, s->device, "request");
+  if (rc) return rc;
+  const uint64_t nb = n_queries >= SORT_MIN_QUERIES ? t->n_nodes : 1;
+  if (n_queries > s->cap_q || n_queries * t->ndim > s->cap_in || n_queries * k > s->cap_out || nb > s->cap_bins)
+    return fail(KD_ERR_INVALID_ARGUMENT, "request exceeds the server's batch capacity (" +
+                                             std::to_string(s->cap_q) + " queries, " +
+                                             std::to_string(s->cap_out) + " results)");
+  Request* r = new (std::nothrow) Request();
+  if (!r) return fail(KD_ERR_OUT_OF_MEMORY, "host allocation failed");
+  r->tree = static_cast<uint32_t>(tree);
+  r->q = queries;
+  r->nq = n_queries;
+  r->k = k;
+  r->od = out_distances;
+  r->oi = out_indices;
+  r->t_submit = Clock::now();
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->stop) {
+      delete r;
+      return fail(KD_ERR_INVALID_ARGUMENT, "server is stopping");
+    }
+    r->ticket = s->next_ticket++;
+    s->reqs[r->ticket] = r;
+    s->queue.push_back(r);
+  }
+  s->cv.notify_all();
+  *ticket = r->ticket;
+  return KD_OK;
+}
+
+int kd_server_wait(kd_server* s, uint64_t ticket, double* latency_s) {
+  if (!s) return fail(KD_ERR_INVALID_ARGUMENT, "server is NULL");
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) return fail(KD_ERR_INVALID_ARGUMENT, "unknown ticket " + std::to_string(ticket));
+  Request* r = it->second;
+  s->cv.wait(lk, [&] { return r->done; });
+  const int st = r->status;
+  if (latency_s) *latency_s = r->latency;
+  s->reqs.erase(it);
+  delete r;
+  lk.unlock();
+  if (st == KD_ERR_NONFINITE_DATA) return fail(st, "all coordinates must be finite");
+  if (st) return fail(st, "the batch holding this request failed on the device");
+  return KD_OK;
+}
+
+void kd_server_free(kd_server* s) { release_server(s); }
 
 }  // extern "C"

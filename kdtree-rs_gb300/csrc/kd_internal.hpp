@@ -37,6 +37,36 @@ struct kd_tree {
 
 namespace kd {
 
+// Launch arguments of the query kernels (every query translation unit).
+constexpr uint32_t NO_ID = 0xffffffffu;
+constexpr uint64_t INF_BITS = 0x7ff0000000000000ull;
+constexpr int QUERY_THREADS = 128;
+
+struct QArgs {
+  const double* data;     // tree order, n * d
+  const float* data32;    // FP32 copy
+  const uint32_t* indices;
+  const DNode* nodes;
+  const double* boxes;    // [lo | hi] per node
+  const float* boxes32;   // outward-rounded FP32 boxes
+  float coord_max;        // >= every |coordinate| of the tree, FP32
+  const double* queries;  // nq * d
+  double* out_d;          // nq * k
+  int64_t* out_i;         // nq * k
+  double* axes_scratch;   // nq * d, dynamic-d CellBound (unused for static d)
+  uint32_t* status;       // bit 0: non-finite query
+  const uint32_t* order;  // optional: thread t runs query order[t] (spatially sorted)
+  bool reference_order;   // run the reference-order descent even where eps = 0
+  uint64_t nq;
+  uint64_t d;
+  uint64_t k;
+  uint64_t n_points;
+  double p;               // LP exponent
+  double cutoff;          // reduced max_distance, >= +0
+  double eps_factor;
+  int use_eps;            // eps_factor != 1
+};
+
 // Thread-local last-error text (read through kd_last_error).
 void set_error(const std::string& msg);
 int fail(int status, const std::string& msg);
@@ -102,6 +132,11 @@ int query_on_device_scratch(const kd_tree* t, const double* d_queries, uint64_t 
 uint64_t order_scratch_words(const kd_tree* t);
 void order_by_landing_leaf(const kd_tree* t, const double* d_queries, uint64_t nq, uint32_t* leaf_of,
                            uint32_t* order, uint32_t* scratch, cudaStream_t stream);
+
+// The packet traversal (warp-shared descent, eps = 0, k <= 32, L1 / L2 /
+// L-inf, widths 2, 3, 8, 16): whether it covers a query, and its launch.
+bool packet_applicable(uint64_t d, int metric, uint64_t k, uint64_t n_points, bool use_eps);
+int launch_packet_query(const QArgs& a, int metric, cudaStream_t stream);
 
 // Exact k-NN through the tensor-core filter (L2, eps = 0, 16 <= d <= 128,
 // k <= 32).  Returns KD_OK, or KD_ERR_INVALID_ARGUMENT without doing anything

@@ -458,7 +458,6 @@ constexpr uint64_t ORDER_MIN_QUERIES = 4096;
 
 #include "kd_lazy_best.cuh"
 #include "kd_query_fast.cuh"
-#include "kd_query_packet.cuh"
 
 // KD_QUERY_MODE=dfs runs every query through the reference-order descent (the
 // eps > 0 kernel) instead of the packet traversal; a diagnostic switch, same results.
@@ -475,10 +474,7 @@ int launch(const QArgs& a, cudaStream_t st) {
   const unsigned blocks = static_cast<unsigned>((a.nq + QUERY_THREADS - 1) / QUERY_THREADS);
   if constexpr (D > 0 && M != M_LP && K > 0) {
     if (a.n_points < ROW_NONE) {
-      if (!a.use_eps && !a.reference_order && !force_reference_order())
-        k_query_packet<M, D, K><<<blocks, QUERY_THREADS, 0, st>>>(a);
-      else
-        k_query_fast<M, D, K><<<blocks, QUERY_THREADS, 0, st>>>(a);
+      k_query_fast<M, D, K><<<blocks, QUERY_THREADS, 0, st>>>(a);
       KD_TRY_CUDA(cudaGetLastError());
       return KD_OK;
     }
@@ -509,6 +505,20 @@ int dispatch_d(const QArgs& a, cudaStream_t st) {
     }
   }
   return dispatch_k<M, 0>(a, st);
+}
+
+// The packet traversal where it applies (eps = 0, not forced to the reference
+// order), else the reference-order kernels.
+int run_kernels(const QArgs& a, int metric, cudaStream_t st) {
+  if (!a.reference_order && !force_reference_order() &&
+      packet_applicable(a.d, metric, a.k, a.n_points, a.use_eps != 0))
+    return launch_packet_query(a, metric, st);
+  switch (metric) {
+    case M_L1: return dispatch_d<M_L1>(a, st);
+    case M_L2: return dispatch_d<M_L2>(a, st);
+    case M_LINF: return dispatch_d<M_LINF>(a, st);
+    default: return dispatch_d<M_LP>(a, st);
+  }
 }
 
 }  // namespace
@@ -584,13 +594,7 @@ int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, cons
       sort_mem = nullptr;
     }
   }
-  int rc;
-  switch (qp.metric) {
-    case M_L1: rc = dispatch_d<M_L1>(a, st); break;
-    case M_L2: rc = dispatch_d<M_L2>(a, st); break;
-    case M_LINF: rc = dispatch_d<M_LINF>(a, st); break;
-    default: rc = dispatch_d<M_LP>(a, st); break;
-  }
+  const int rc = run_kernels(a, qp.metric, st);
   if (axes) cudaFreeAsync(axes, st);
   if (sort_mem) cudaFreeAsync(sort_mem, st);
   return rc;
@@ -620,12 +624,7 @@ int query_on_device_scratch(const kd_tree* t, const double* d_queries, uint64_t 
   a.eps_factor = qp.eps_factor;
   a.use_eps = qp.eps_factor != 1.0;
   a.axes_scratch = d_axes_scratch;
-  switch (qp.metric) {
-    case M_L1: return dispatch_d<M_L1>(a, st);
-    case M_L2: return dispatch_d<M_L2>(a, st);
-    case M_LINF: return dispatch_d<M_LINF>(a, st);
-    default: return dispatch_d<M_LP>(a, st);
-  }
+  return run_kernels(a, qp.metric, st);
 }
 
 }  // namespace kd

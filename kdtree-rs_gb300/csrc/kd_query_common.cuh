@@ -5,35 +5,6 @@
 // unit, so every unit gets its own internal copies.
 #pragma once
 
-constexpr uint32_t NO_ID = 0xffffffffu;
-constexpr uint64_t INF_BITS = 0x7ff0000000000000ull;
-constexpr int QUERY_THREADS = 128;
-
-struct QArgs {
-  const double* data;     // tree order, n * d
-  const float* data32;    // FP32 copy
-  const uint32_t* indices;
-  const DNode* nodes;
-  const double* boxes;    // [lo | hi] per node
-  const float* boxes32;   // outward-rounded FP32 boxes
-  float coord_max;        // >= every |coordinate| of the tree, FP32
-  const double* queries;  // nq * d
-  double* out_d;          // nq * k
-  int64_t* out_i;         // nq * k
-  double* axes_scratch;   // nq * d, dynamic-d CellBound (unused for static d)
-  uint32_t* status;       // bit 0: non-finite query
-  const uint32_t* order;  // optional: thread t runs query order[t] (spatially sorted)
-  bool reference_order;   // run the reference-order descent even where eps = 0
-  uint64_t nq;
-  uint64_t d;
-  uint64_t k;
-  uint64_t n_points;
-  double p;               // LP exponent
-  double cutoff;          // reduced max_distance, >= +0
-  double eps_factor;
-  int use_eps;            // eps_factor != 1
-};
-
 // ---------------------------------------------------------------------------
 // Metric algebra (src/metric.rs:64-98), exact.
 // ---------------------------------------------------------------------------
@@ -98,7 +69,8 @@ __device__ __forceinline__ double exact_dist(const QVec<D>& q, const double* p, 
     }
     return dist;
   }
-  if (D > 0) {
+  if (D > 8) strat = D <= 16 ? S_FOLDED : S_STREAMED;  // L1 / L2 above 8 (kernel.rs:244-270)
+  if (D > 0 && D <= 8) {
     if (D == 4 && in_chunk) {
       double a0 = axis_of<M>(dsub(p[0], q[0])), a1 = axis_of<M>(dsub(p[1], q[1]));
       double a2 = axis_of<M>(dsub(p[2], q[2])), a3 = axis_of<M>(dsub(p[3], q[3]));
@@ -115,6 +87,7 @@ __device__ __forceinline__ double exact_dist(const QVec<D>& q, const double* p, 
     for (int i = 0; i < D; ++i) dist = dadd(dist, axis_of<M>(dsub(q[i], p[i])));
     return dist;
   }
+  if (D > 0) d = D;
   if (strat == S_PACKED) {
     if (d == 4 && in_chunk) {
       double a0 = axis_of<M>(dsub(p[0], q[0])), a1 = axis_of<M>(dsub(p[1], q[1]));

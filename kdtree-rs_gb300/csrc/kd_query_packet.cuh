@@ -3,7 +3,7 @@
 //
 // The 32 queries of a warp -- neighbours, since the batch is sorted by landing
 // leaf -- walk ONE depth-first traversal together: every lane holds the same
-// node stack, so control flow is uniform and the stack accesses coalesce.  A
+// node stack (one copy per warp, in shared memory), so control flow is uniform.  A
 // node is entered when at least one lane's rigorous FP32 lower bound of the
 // exact box distance does not exceed that lane's pruning bound; its children are
 // visited near side first by majority vote.  At a leaf every lane that needs it
@@ -92,10 +92,12 @@ struct PointFilter {
   }
 };
 
-// Shared memory of the k-best heaps of one block (K >= 8; a dummy word below).
+// Shared memory of one block: the warps' node stacks and the k-best heaps
+// (K >= 8; a dummy word below).
 template <int K>
 struct PacketSmem {
   static constexpr int HK = K >= 8 ? K : 1;
+  uint32_t stack[QUERY_THREADS / 32 * PACKET_STACK];
   float lo[HK * QUERY_THREADS], hi[HK * QUERY_THREADS];
   uint32_t row[HK * QUERY_THREADS];
 };
@@ -103,10 +105,11 @@ struct PacketSmem {
 // The 32 lanes of a warp run the sorted batch positions tid (one per lane) of
 // the queries described by `a`; every lane of the warp must call it together.
 // s_lo / s_hi / s_row: the block's heap arrays, K * QUERY_THREADS words each
-// (unused for K < 8).
+// (unused for K < 8); s_stack: the block's node stacks, PACKET_STACK words per
+// warp.
 template <int M, int D, int K>
 __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, float* s_lo, float* s_hi,
-                                               uint32_t* s_row) {
+                                               uint32_t* s_row, uint32_t* s_stack) {
   static_assert(D > 0 && M != M_LP, "packet path: compile-time width, metric without pow()");
   const bool in_range = tid < a.nq;
   const uint64_t qi = in_range ? (a.order ? a.order[tid] : tid) : 0;
@@ -139,7 +142,9 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
     best.init(a.k, a.cutoff, &q, a.data, a.indices);
   float thr = filt.threshold(best.b_hi);
 
-  uint32_t stack[PACKET_STACK];  // identical in every lane
+  // Every lane pushes the same ids to the same words and pops what it pushed
+  // itself, so no lane depends on another's store.
+  uint32_t* stack = s_stack + (threadIdx.x >> 5) * PACKET_STACK;
   int sp = 0;
   stack[sp++] = 0;
   while (sp > 0) {
@@ -198,5 +203,5 @@ template <int M, int D, int K>
 __global__ void __launch_bounds__(QUERY_THREADS) k_query_packet(QArgs a) {
   __shared__ PacketSmem<K> sm;
   packet_queries<M, D, K>(a, blockIdx.x * static_cast<uint64_t>(QUERY_THREADS) + threadIdx.x, sm.lo, sm.hi,
-                          sm.row);
+                          sm.row, sm.stack);
 }

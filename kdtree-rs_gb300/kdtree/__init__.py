@@ -2,6 +2,6 @@
 
 `from kdtree import KDTree` as in the reference (python/kdtree/__init__.py:1-3).
 """
-from ._core import BatchQuery, KDTree
+from ._core import BatchQuery, KDTree, Server
 
-__all__ = ["KDTree", "BatchQuery"]
+__all__ = ["KDTree", "BatchQuery", "Server"]

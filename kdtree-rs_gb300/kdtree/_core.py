@@ -68,6 +68,14 @@ def _load():
     L.kd_batch_run_mode.restype = ctypes.c_int
     L.kd_batch_free.argtypes = [P]
     L.kd_batch_free.restype = None
+    L.kd_server_create.argtypes = [P, u64, d, ctypes.c_int, d, d, u64, ctypes.POINTER(P)]
+    L.kd_server_create.restype = ctypes.c_int
+    L.kd_server_submit.argtypes = [P, u64, P, u64, u64, P, P, ctypes.POINTER(u64)]
+    L.kd_server_submit.restype = ctypes.c_int
+    L.kd_server_wait.argtypes = [P, u64, ctypes.POINTER(d)]
+    L.kd_server_wait.restype = ctypes.c_int
+    L.kd_server_free.argtypes = [P]
+    L.kd_server_free.restype = None
     L.kd_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.kd_last_error.restype = ctypes.c_size_t
     return L
@@ -316,3 +324,72 @@ class BatchQuery:
         if h:
             _lib.kd_batch_free(h)
             self._h = None
+
+
+# -- serving loop (no reference counterpart) ---------------------------------
+class Server:
+    """Continuous-batching query server over a fixed list of trees
+    (kd_server_* in include/kdtree_gb300.h).  `submit` queues a request and
+    returns a ticket at once; `wait` returns (distances, indices, latency_s),
+    the results exactly those of `trees[tree].query(queries, k=k, ...)`.
+    No reference counterpart: it is a request loop in front of KDTree.query."""
+
+    __slots__ = ("_h", "_trees", "_pending", "__weakref__")
+
+    def __init__(self, trees, *, p: float = 2.0, max_distance=None, eps: float = 0.0, max_batch_queries: int = 0):
+        trees = list(trees)
+        for i, t in enumerate(trees):
+            if not isinstance(t, KDTree):
+                raise TypeError(f"tree {i}: expected a KDTree")
+        arr = (ctypes.c_void_p * max(len(trees), 1))(*[t._h for t in trees])
+        h = ctypes.c_void_p()
+        has_max = max_distance is not None
+        st = _lib.kd_server_create(ctypes.cast(arr, ctypes.c_void_p), len(trees), _f64(p), int(has_max),
+                                   _f64(max_distance) if has_max else 0.0, _f64(eps),
+                                   _usize(max_batch_queries, "max_batch_queries"), ctypes.byref(h))
+        if st != KD_OK:
+            _raise(st)
+        self._h = h
+        self._trees = trees
+        self._pending = {}
+
+    def submit(self, tree: int, queries, k: int, out=None) -> int:
+        """Queue `queries` (2-D, tree's width) against trees[tree]; `out` may be
+        a preallocated (float64 [n, k], int64 [n, k]) pair, e.g. page-locked."""
+        t = self._trees[tree]
+        q, _ = _as_points(queries, "query must be one- or two-dimensional", True)
+        if q.shape[1] != t.ndim:
+            raise ValueError(f"dimension mismatch: expected {t.ndim}, got {q.shape[1]}")
+        k = _usize(k, "k")
+        n = q.shape[0]
+        if out is None:
+            out = (np.empty((n, k), np.float64), np.empty((n, k), np.int64))
+        od, oi = out
+        if od.shape != (n, k) or oi.shape != (n, k) or od.dtype != np.float64 or oi.dtype != np.int64 \
+                or not od.flags.c_contiguous or not oi.flags.c_contiguous:
+            raise ValueError("out must be C-contiguous float64 and int64 arrays of shape (n, k)")
+        ticket = ctypes.c_uint64()
+        st = _lib.kd_server_submit(self._h, tree, _ptr(q) if q.size else None, n, k, _ptr(od) if od.size else None,
+                                   _ptr(oi) if oi.size else None, ctypes.byref(ticket))
+        if st != KD_OK:
+            _raise(st)
+        self._pending[ticket.value] = (q, od, oi)
+        return ticket.value
+
+    def wait(self, ticket: int):
+        lat = ctypes.c_double()
+        st = _lib.kd_server_wait(self._h, ticket, ctypes.byref(lat))
+        entry = self._pending.pop(ticket, None)
+        if st != KD_OK:
+            _raise(st)
+        return entry[1], entry[2], lat.value
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h:
+            _lib.kd_server_free(h)
+            self._h = None
+            self._pending.clear()
+
+    def __del__(self):
+        self.close()

@@ -64,3 +64,40 @@ def test_packet_and_reference_order_agree(oracle, tmp_path, d, p, dist):
     q = rng.uniform(size=(spec["nq"], d)) * 1.1 - 0.05
     ref = oracle.OracleKDTree(data, leafsize=16).query(q, k=16, p=p, parallel=True)
     assert_bit_exact(packet, ref)
+
+
+def _path_query(tree, q, k, p, path):
+    import ctypes
+
+    import torch
+
+    from kdtree import _core
+
+    L = _core._lib
+    P, u64, dbl = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double
+    L.kd_query_device_path.argtypes = [P, P, u64, u64, dbl, ctypes.c_int, dbl, dbl, P, P, P, ctypes.c_int, P]
+    L.kd_query_device_path.restype = ctypes.c_int
+    dq = torch.from_numpy(np.ascontiguousarray(q)).cuda()
+    od = torch.empty((q.shape[0], k), dtype=torch.float64, device="cuda")
+    oi = torch.empty((q.shape[0], k), dtype=torch.int64, device="cuda")
+    st = L.kd_query_device_path(tree._h, P(dq.data_ptr()), dq.numel(), k, p, 0, 0.0, 0.0, P(od.data_ptr()),
+                                P(oi.data_ptr()), None, path, None)
+    assert st == 0, _core._last_error()
+    return od.cpu().numpy(), oi.cpu().numpy()
+
+
+@pytest.mark.parametrize("p", [1.0, 2.0, float("inf")])
+@pytest.mark.parametrize("dist", ["uniform", "gmm"])
+@pytest.mark.parametrize("k", [1, 4, 8, 16, 32])
+def test_packet_width16(oracle, p, dist, k):
+    """Width 16 through the packet traversal (Folded L1 / L2 order,
+    kernel.rs:343-354): bit-exact with the oracle."""
+    from kdtree import KDTree
+
+    rng = np.random.default_rng(1600 + k)
+    data = rng.uniform(size=(30_000, 16)) if dist == "uniform" else gmm(30_000, 16, rng)
+    q = data[rng.integers(0, 30_000, 1500)] + 0.02 * rng.standard_normal((1500, 16))
+    t = KDTree(data, leafsize=16)
+    got = _path_query(t, q, k, p, 2)  # KD_PATH_PACKET
+    o = oracle.OracleKDTree(data, leafsize=16).query(q, k=k, p=p, parallel=True)
+    assert_bit_exact(got, o)

@@ -193,7 +193,7 @@ def run_reference(args):
     return 0
 
 
-PATH_AUTO, PATH_REFERENCE_ORDER, PATH_PACKET, PATH_TENSOR_CORE = 0, 1, 2, 3
+PATH_AUTO, PATH_REFERENCE_ORDER, PATH_PACKET, PATH_TENSOR_CORE, PATH_WARP = 0, 1, 2, 3, 4
 # kernels one kd_query_device call launches for d=3, k=16 (queries sorted by
 # landing leaf: k_landing_leaf, 3 scan kernels, k_scatter_order; k_query_packet)
 LAUNCHES_PER_STEP = 6
@@ -557,6 +557,31 @@ def run_profile_tc():
     return 0
 
 
+def run_profile_warp():
+    """A warp-per-query case small enough for an ncu capture: a 64-component
+    Gaussian mixture (sigma 0.01) in d=16, N=1,000,000, leafsize 32, 20,000
+    queries from the same mixture, k=16, L2; 3 calls."""
+    import torch
+
+    from kdtree import KDTree
+    from kdtree import _core
+
+    lib = _core._lib
+    P_, u64_, d_ = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double
+    lib.kd_query_device_path.argtypes = [P_, P_, u64_, u64_, d_, ctypes.c_int, d_, d_, P_, P_, P_, ctypes.c_int, P_]
+    lib.kd_query_device_path.restype = ctypes.c_int
+    rng = np.random.default_rng(716)
+    c = rng.uniform(size=(64, 16))
+    data = c[rng.integers(0, 64, 1_000_000)] + 0.01 * rng.standard_normal((1_000_000, 16))
+    q = c[rng.integers(0, 64, 20_000)] + 0.01 * rng.standard_normal((20_000, 16))
+    tree = KDTree(data)
+    stream = torch.cuda.Stream()
+    dq = torch.from_numpy(q).cuda()
+    ms, _ = time_path(lib, tree, dq, 16, 2.0, PATH_WARP, 3, torch, stream)
+    print(json.dumps({"profile_warp_ms": ms, "queries": q.shape[0], "points": data.shape[0], "d": 16, "k": 16}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -567,6 +592,9 @@ def main():
     ap.add_argument("--no-cases", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--batched-only", action="store_true", help="only run the batched multi-tree case")
     ap.add_argument("--serving-only", action="store_true", help="only run the serving case")
+    ap.add_argument("--profile-warp", action="store_true",
+                    help="only run the warp-per-query path on a profiling-sized case (d=16 mixture, N=1M, "
+                         "20,000 queries, k=16), 3 calls")
     ap.add_argument("--profile-tc", action="store_true",
                     help="only run the tensor-core path on a profiling-sized case (N=100k, d=64, "
                          "19,456 queries, k=32), 3 calls")
@@ -575,6 +603,8 @@ def main():
         return run_reference(args)
     if args.profile_tc:
         return run_profile_tc()
+    if args.profile_warp:
+        return run_profile_warp()
     if args.serving_only:
         import torch
 

@@ -92,15 +92,19 @@ int kd_query_device(const kd_tree* tree, const double* d_queries, uint64_t n_val
  *   KD_PATH_AUTO            what kd_query / kd_query_device run
  *   KD_PATH_REFERENCE_ORDER one thread per query, the reference's depth-first
  *                           order (FP64 decisions; the only order for eps > 0)
- *   KD_PATH_PACKET          warp-shared traversal (d in {2, 3, 8, 16}, eps = 0, k <= 32)
+ *   KD_PATH_PACKET          warp-shared traversal (d in {2, 3, 8, 16}, eps = 0, k <= 64)
  *   KD_PATH_TENSOR_CORE     tcgen05 BF16 distance filter + FP64 re-rank
  *                           (L2, eps = 0, 16 <= d <= 128, k <= 32)
+ *   KD_PATH_WARP            one warp per query, rows and dimensions split
+ *                           across the lanes (d in {2, 3, 8, 16}, eps = 0,
+ *                           k <= 32): for queries that scan many leaf rows
  * A path that does not apply to a call falls back to the reference order. */
 enum kd_query_path {
   KD_PATH_AUTO = 0,
   KD_PATH_REFERENCE_ORDER = 1,
   KD_PATH_PACKET = 2,
-  KD_PATH_TENSOR_CORE = 3
+  KD_PATH_TENSOR_CORE = 3,
+  KD_PATH_WARP = 4
 };
 
 /* kd_query_device with the kernel chosen by `path` (see kd_query_path).

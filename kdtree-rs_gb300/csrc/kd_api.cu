@@ -151,6 +151,7 @@ void free_tree(kd_tree* t) {
   cudaFree(t->tc_w);
   cudaFree(t->tc_v);
   cudaFree(t->tc_centre);
+  cudaFree(t->tc_tbox);
   delete t;
 }
 
@@ -419,7 +420,7 @@ int kd_query_device(const kd_tree* tree, const double* d_queries, uint64_t n_val
 int kd_query_device_path(const kd_tree* tree, const double* d_queries, uint64_t n_values, uint64_t k, double p,
                          int has_max_distance, double max_distance, double eps, double* d_out_distances,
                          int64_t* d_out_indices, void* stream, int path, unsigned long long* d_survivors) {
-  if (path < KD_PATH_AUTO || path > KD_PATH_TENSOR_CORE) return fail(KD_ERR_INVALID_ARGUMENT, "unknown query path");
+  if (path < KD_PATH_AUTO || path > KD_PATH_WARP) return fail(KD_ERR_INVALID_ARGUMENT, "unknown query path");
   return query_common(tree, d_queries, true, n_values, k, p, has_max_distance, max_distance, eps, d_out_distances,
                       d_out_indices, static_cast<cudaStream_t>(stream), path, d_survivors);
 }

@@ -7,19 +7,19 @@
 //  1. one kernel walks every query of every packet job down its own tree to
 //     its landing leaf and counts it into bin (job, leaf); one scan over all
 //     bins and one scatter leave each job's queries grouped by landing leaf,
-//     jobs one after another in the batch order (jobs below SORT_MIN_QUERIES
-//     queries keep their own order: one bin);
-//  2. ONE persistent kernel: each warp takes the next task -- 32 consecutive
-//     positions of one job's queries -- from a global counter and runs the
-//     packet traversal (kd_query_packet.cuh) for that job's width and k.  Jobs
-//     are laid out most expensive class first, so the long tasks start early
-//     and the short ones fill the tail;
+//     jobs one after another in the batch order (jobs below 1,024 queries
+//     keep their own order: one bin);
+//  2. ONE persistent kernel: each warp takes the next task -- 4 consecutive
+//     positions of one job's queries -- from a global counter and runs them
+//     one by one with the warp-per-query traversal (kd_query_warp.cuh) for the
+//     job's width.  Jobs are laid out widest (most expensive) first, so the
+//     long tasks start early and the short ones fill the tail;
 //  3. jobs outside the fused kernel's envelope (general L^p, eps > 0, k > 32,
-//     widths other than 2, 3 and 8, the reference-order switch) run as
-//     ordinary per-job launches of the kernels kd_query_device uses -- the
-//     packet traversal for width 16, the reference-order descent otherwise;
-//     never the tensor-core filter, whose brute-force scan only pays on
-//     trees that do not prune.
+//     widths other than 2, 3, 8 and 16, the reference-order switch) run as
+//     ordinary per-job launches of the kernels kd_query_device uses, on side
+//     streams beside the fused kernel -- the packet traversal for k <= 64,
+//     the reference-order descent otherwise; never the tensor-core filter,
+//     whose brute-force scan only pays on trees that do not prune.
 // A query's result depends on that query and its tree alone, so every job
 // gets exactly what kd_query_device returns for it.
 //
@@ -51,25 +51,23 @@ namespace {
 #include "kd_scan.cuh"
 #include "kd_lazy_best.cuh"
 #include "kd_query_packet.cuh"
+#include "kd_query_warp.cuh"
 
 constexpr uint32_t CLS_OTHER = 0xffffffffu;
-constexpr int BATCH_K[5] = {1, 4, 8, 16, 32};
 constexpr uint64_t SORT_MIN_QUERIES = 1024;
+constexpr uint32_t TASK_QUERIES = 4;  // queries per task: one after another on one warp
 
-// Packet class of a job: width index * 5 + k index, or CLS_OTHER.
-uint32_t packet_class(const kd_tree* t, const QueryParams& qp, uint64_t k, bool reference_order) {
+// Class of a job in the fused kernel (its width index), or CLS_OTHER.
+uint32_t fused_class(const kd_tree* t, const QueryParams& qp, uint64_t k, bool reference_order) {
   if (qp.metric == M_LP || qp.eps_factor != 1.0 || k > 32 || t->n_points >= ROW_NONE || reference_order)
     return CLS_OTHER;
-  int di;
   switch (t->ndim) {
-    case 2: di = 0; break;
-    case 3: di = 1; break;
-    case 8: di = 2; break;
+    case 2: return 0;
+    case 3: return 1;
+    case 8: return 2;
+    case 16: return 3;
     default: return CLS_OTHER;
   }
-  int ki = 0;
-  while (BATCH_K[ki] < static_cast<int>(k)) ++ki;
-  return static_cast<uint32_t>(di * 5 + ki);
 }
 
 bool reference_order_forced() {
@@ -137,29 +135,19 @@ __global__ void k_batch_scatter(const uint32_t* q_start, uint32_t n_jobs, uint32
   order[atomicAdd(&bins[bin_of[g]], 1u)] = g - q_start[j];
 }
 
-template <int M, int D, int K>
-__device__ __noinline__ void batch_task(const QArgs* a, uint64_t tid, float* lo, float* hi, uint32_t* row,
-                                        uint32_t* stack) {
-  packet_queries<M, D, K>(*a, tid, lo, hi, row, stack);
+template <int M, int D>
+__device__ __forceinline__ void batch_query(const QArgs* a, uint64_t w, uint32_t* stack_n, float* stack_lb) {
+  warp_query<M, D>(*a, w, stack_n, stack_lb);
 }
 
-template <int M, int D, int KMAX>
-__device__ __forceinline__ void run_k(uint32_t ki, const QArgs* a, uint64_t tid, float* lo, float* hi,
-                                      uint32_t* row, uint32_t* stack) {
-  switch (ki) {
-    case 0: batch_task<M, D, 1>(a, tid, lo, hi, row, stack); break;
-    case 1: if constexpr (KMAX >= 4) batch_task<M, D, 4>(a, tid, lo, hi, row, stack); break;
-    case 2: if constexpr (KMAX >= 8) batch_task<M, D, 8>(a, tid, lo, hi, row, stack); break;
-    case 3: if constexpr (KMAX >= 16) batch_task<M, D, 16>(a, tid, lo, hi, row, stack); break;
-    default: if constexpr (KMAX >= 32) batch_task<M, D, 32>(a, tid, lo, hi, row, stack); break;
-  }
-}
-
-// The persistent kernel: warps take 32-query tasks until none is left.
-template <int M, int KMAX>
+// The persistent kernel: warps take tasks -- TASK_QUERIES consecutive
+// positions of one job -- until none is left, and run each query with the
+// warp-per-query traversal (kd_query_warp.cuh) for the job's width.
+template <int M>
 __global__ void __launch_bounds__(QUERY_THREADS) k_query_batch(BatchArgs b) {
-  __shared__ PacketSmem<KMAX> sm;
-  const uint32_t lane = threadIdx.x & 31;
+  __shared__ uint32_t s_node[QUERY_THREADS / 32][WARP_STACK];
+  __shared__ float s_lb[QUERY_THREADS / 32][WARP_STACK];
+  const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (;;) {
     uint32_t t = 0;
     if (lane == 0) t = atomicAdd(b.next_task, 1u);
@@ -167,42 +155,31 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query_batch(BatchArgs b) {
     if (t >= b.n_tasks) return;
     const uint32_t j = find_range(b.task_start, b.n_jobs, t);
     const BatchJob* J = b.jobs + j;
-    const uint32_t cls = J->cls;
-    const uint64_t tid = static_cast<uint64_t>(t - b.task_start[j]) * 32 + lane;
-    switch (cls / 5) {
-      case 0: run_k<M, 2, KMAX>(cls % 5, &J->a, tid, sm.lo, sm.hi, sm.row, sm.stack); break;
-      case 1: run_k<M, 3, KMAX>(cls % 5, &J->a, tid, sm.lo, sm.hi, sm.row, sm.stack); break;
-      default: run_k<M, 8, KMAX>(cls % 5, &J->a, tid, sm.lo, sm.hi, sm.row, sm.stack); break;
+    const uint64_t first = static_cast<uint64_t>(t - b.task_start[j]) * TASK_QUERIES;
+    const uint64_t last = min(first + TASK_QUERIES, J->a.nq);
+    for (uint64_t w = first; w < last; ++w) {
+      switch (J->cls) {
+        case 0: batch_query<M, 2>(&J->a, w, s_node[wid], s_lb[wid]); break;
+        case 1: batch_query<M, 3>(&J->a, w, s_node[wid], s_lb[wid]); break;
+        case 2: batch_query<M, 8>(&J->a, w, s_node[wid], s_lb[wid]); break;
+        default: batch_query<M, 16>(&J->a, w, s_node[wid], s_lb[wid]); break;
+      }
     }
   }
 }
 
 template <int M>
-cudaError_t launch_batch_k(const BatchArgs& b, int kmax, unsigned blocks, cudaStream_t st) {
-  if (kmax <= 4) k_query_batch<M, 4><<<blocks, QUERY_THREADS, 0, st>>>(b);
-  else if (kmax <= 16) k_query_batch<M, 16><<<blocks, QUERY_THREADS, 0, st>>>(b);
-  else k_query_batch<M, 32><<<blocks, QUERY_THREADS, 0, st>>>(b);
-  return cudaGetLastError();
-}
-
-template <int M, int KMAX>
 int max_blocks_per_sm() {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_query_batch<M, KMAX>, QUERY_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_query_batch<M>, QUERY_THREADS, 0);
   return std::max(n, 1);
 }
 
-int resident_blocks_per_sm(int metric, int kmax) {
-  auto pick = [&](auto m) {
-    constexpr int MM = decltype(m)::value;
-    if (kmax <= 4) return max_blocks_per_sm<MM, 4>();
-    if (kmax <= 16) return max_blocks_per_sm<MM, 16>();
-    return max_blocks_per_sm<MM, 32>();
-  };
+int resident_blocks_per_sm(int metric) {
   switch (metric) {
-    case M_L1: return pick(std::integral_constant<int, M_L1>{});
-    case M_L2: return pick(std::integral_constant<int, M_L2>{});
-    default: return pick(std::integral_constant<int, M_LINF>{});
+    case M_L1: return max_blocks_per_sm<M_L1>();
+    case M_L2: return max_blocks_per_sm<M_L2>();
+    default: return max_blocks_per_sm<M_LINF>();
   }
 }
 
@@ -227,7 +204,6 @@ struct Layout {
   std::vector<BatchJob> table;
   uint64_t n_bins = 1;
   uint32_t total_q = 0, n_tasks = 0;
-  int kmax = 1;
 };
 
 void fill_args(QArgs* a, const JobSpec& J, const QueryParams& qp) {
@@ -262,13 +238,13 @@ void make_layout(const std::vector<JobSpec>& specs, const QueryParams& qp, bool 
   const bool ref = reference_order_forced();
   std::vector<uint32_t> cls(specs.size());
   for (size_t j = 0; j < specs.size(); ++j) {
-    cls[j] = packet_class(specs[j].tree, qp, specs[j].k, ref);
+    cls[j] = fused_class(specs[j].tree, qp, specs[j].k, ref);
     (cls[j] == CLS_OTHER ? L->other : L->packet).push_back(static_cast<uint32_t>(j));
   }
-  // most expensive class first: larger k, then wider points
+  // most expensive first: wider points, then larger k
   std::stable_sort(L->packet.begin(), L->packet.end(), [&](uint32_t x, uint32_t y) {
-    if (cls[x] % 5 != cls[y] % 5) return cls[x] % 5 > cls[y] % 5;
-    return cls[x] / 5 > cls[y] / 5;
+    if (cls[x] != cls[y]) return cls[x] > cls[y];
+    return specs[x].k > specs[y].k;
   });
   const size_t n = L->packet.size();
   L->q_start.assign(n + 1, 0);
@@ -285,8 +261,7 @@ void make_layout(const std::vector<JobSpec>& specs, const QueryParams& qp, bool 
     B.bin_start = bins;
     bins += B.sorted ? J.tree->n_nodes : 1;
     L->q_start[i + 1] = L->q_start[i] + static_cast<uint32_t>(J.nq);
-    L->task_start[i + 1] = L->task_start[i] + static_cast<uint32_t>((J.nq + 31) / 32);
-    L->kmax = std::max(L->kmax, BATCH_K[B.cls % 5]);
+    L->task_start[i + 1] = L->task_start[i] + static_cast<uint32_t>((J.nq + TASK_QUERIES - 1) / TASK_QUERIES);
   }
   L->n_bins = std::max<uint64_t>(bins, 1);
   L->total_q = L->q_start[n];
@@ -365,13 +340,12 @@ int enqueue_packet(const Layout& L, const Buffers& B, int table, int metric, uns
   KD_TRY_CUDA(cudaGetLastError());
   KD_TRY_CUDA(cudaMemsetAsync(B.counter, 0, sizeof(uint32_t), st));
   BatchArgs a{B.jobs[table], B.task_start, n, L.n_tasks, B.counter};
-  cudaError_t e;
   switch (metric) {
-    case M_L1: e = launch_batch_k<M_L1>(a, L.kmax, blocks, st); break;
-    case M_L2: e = launch_batch_k<M_L2>(a, L.kmax, blocks, st); break;
-    default: e = launch_batch_k<M_LINF>(a, L.kmax, blocks, st); break;
+    case M_L1: k_query_batch<M_L1><<<blocks, QUERY_THREADS, 0, st>>>(a); break;
+    case M_L2: k_query_batch<M_L2><<<blocks, QUERY_THREADS, 0, st>>>(a); break;
+    default: k_query_batch<M_LINF><<<blocks, QUERY_THREADS, 0, st>>>(a); break;
   }
-  if (e != cudaSuccess) return cuda_fail(e, "k_query_batch");
+  KD_TRY_CUDA(cudaGetLastError());
   return KD_OK;
 }
 
@@ -387,6 +361,64 @@ struct DeviceScope {
     if (prev >= 0 && cur != prev) cudaSetDevice(prev);
   }
 };
+
+// Streams for a batch's per-job launches: they fork from the batch stream and
+// join back into it, so those jobs' kernels overlap one another (and the fused
+// kernel) instead of queueing one after the other.
+struct SideStreams {
+  static constexpr int N = 4;
+  cudaStream_t s[N] = {};
+  cudaEvent_t fork = nullptr, join[N] = {};
+  int create() {
+    for (int i = 0; i < N; ++i) {
+      KD_TRY_CUDA(cudaStreamCreateWithFlags(&s[i], cudaStreamNonBlocking));
+      KD_TRY_CUDA(cudaEventCreateWithFlags(&join[i], cudaEventDisableTiming));
+    }
+    KD_TRY_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    return KD_OK;
+  }
+  ~SideStreams() {
+    for (int i = 0; i < N; ++i) {
+      if (s[i]) cudaStreamDestroy(s[i]);
+      if (join[i]) cudaEventDestroy(join[i]);
+    }
+    if (fork) cudaEventDestroy(fork);
+  }
+};
+
+// st waits for the side streams that n_other per-job launches used.
+void join_others(SideStreams& ss, size_t n_other, cudaStream_t st) {
+  const int used = static_cast<int>(std::min<size_t>(SideStreams::N, n_other));
+  for (int i = 0; i < used; ++i) {
+    cudaEventRecord(ss.join[i], ss.s[i]);
+    cudaStreamWaitEvent(st, ss.join[i], 0);
+  }
+}
+
+// Per-job launches of `other` on the side streams, forked from st (join them
+// with join_others once st's own work is enqueued).  scratch != NULL: the
+// allocation-free kernels with that CellBound scratch (offsets axes_off), as a
+// graph capture needs.
+int enqueue_others(const std::vector<JobSpec>& specs, const std::vector<uint32_t>& other, const QueryParams& base,
+                   SideStreams& ss, cudaStream_t st, double* scratch, const std::vector<uint64_t>& axes_off) {
+  if (other.empty()) return KD_OK;
+  const int used = static_cast<int>(std::min<size_t>(SideStreams::N, other.size()));
+  KD_TRY_CUDA(cudaEventRecord(ss.fork, st));
+  for (int i = 0; i < used; ++i) KD_TRY_CUDA(cudaStreamWaitEvent(ss.s[i], ss.fork, 0));
+  int rc = KD_OK;
+  for (size_t o = 0; o < other.size() && rc == KD_OK; ++o) {
+    const JobSpec& J = specs[other[o]];
+    QueryParams qp = base;
+    qp.k = J.k;
+    qp.path = PATH_PACKET;  // never the tensor-core filter inside a batch
+    cudaStream_t side = ss.s[o % SideStreams::N];
+    rc = scratch ? query_on_device_scratch(J.tree, J.queries, J.nq, qp, J.out_d, J.out_i, side, J.status,
+                                           scratch + axes_off[o])
+                 : query_on_device(J.tree, J.queries, J.nq, qp, J.out_d, J.out_i, side, J.status);
+  }
+  if (rc) join_others(ss, other.size(), st);  // nothing is left behind on a failure
+  return rc;
+}
 
 int job_error(const kd_tree* tree, uint64_t nq, uint64_t k, const void* q, const void* od, const void* oi,
               int dev, const std::string& who) {
@@ -420,6 +452,7 @@ struct kd_batch {
   bool tuned = false;
   unsigned blocks = 0;
   int table = 0;
+  SideStreams side;
   cudaStream_t capture_stream = nullptr;
   cudaGraphExec_t exec = nullptr;
 };
@@ -429,30 +462,21 @@ namespace {
 int enqueue_plan(kd_batch* b, cudaStream_t st, bool per_job, unsigned blocks, int table) {
   KD_TRY_CUDA(cudaMemsetAsync(b->status, 0, sizeof(uint32_t), st));
   const Layout& L = b->layout[table];
-  if (per_job) {
-    for (uint32_t j : L.packet) {
-      const JobSpec& J = b->specs[j];
+  if (per_job) {  // one launch sequence per job, one after another (the baseline)
+    for (const JobSpec& J : b->specs) {
       QueryParams qp = b->qp;
       qp.k = J.k;
       qp.path = PATH_PACKET;
       int rc = query_on_device(J.tree, J.queries, J.nq, qp, J.out_d, J.out_i, st, b->status);
       if (rc) return rc;
     }
-  } else {
-    int rc = enqueue_packet(L, b->buf, table, b->qp.metric, blocks, st);
-    if (rc) return rc;
+    return KD_OK;
   }
-  for (size_t o = 0; o < L.other.size(); ++o) {
-    const JobSpec& J = b->specs[L.other[o]];
-    QueryParams qp = b->qp;
-    qp.k = J.k;
-    qp.path = PATH_PACKET;  // never the tensor-core filter inside a batch
-    int rc = per_job ? query_on_device(J.tree, J.queries, J.nq, qp, J.out_d, J.out_i, st, b->status)
-                     : query_on_device_scratch(J.tree, J.queries, J.nq, qp, J.out_d, J.out_i, st, b->status,
-                                               b->axes + b->axes_off[o]);
-    if (rc) return rc;
-  }
-  return KD_OK;
+  int rc = enqueue_others(b->specs, L.other, b->qp, b->side, st, b->axes, b->axes_off);
+  if (rc) return rc;
+  rc = enqueue_packet(L, b->buf, table, b->qp.metric, blocks, st);
+  join_others(b->side, L.other.size(), st);
+  return rc;
 }
 
 int finish_plan(kd_batch* b, cudaStream_t st) {
@@ -466,7 +490,7 @@ int finish_plan(kd_batch* b, cudaStream_t st) {
 // The autotuner: every candidate launch shape runs the plan once to warm up
 // and twice timed; the fastest is kept.  Results are identical for all.
 int tune(kd_batch* b, cudaStream_t st) {
-  const int per_sm = resident_blocks_per_sm(b->qp.metric, b->layout[0].kmax);
+  const int per_sm = resident_blocks_per_sm(b->qp.metric);
   std::vector<unsigned> grids;
   for (int m : {1, 2, 4, 8})
     if (m <= per_sm) grids.push_back(static_cast<unsigned>(b->sms * m));
@@ -567,6 +591,7 @@ struct Slot {
   int64_t* out_i = nullptr;    // staged indices
   uint32_t* status = nullptr;  // one word per job
   void* host = nullptr;        // pinned: tables, q_start, task_start, status words
+  SideStreams side;
   std::vector<Request*> reqs;
   int error = KD_OK;
   std::string error_msg;
@@ -631,18 +656,16 @@ int stage_batch(kd_server* s, Slot* sl) {
     KD_TRY_CUDA(cudaMemcpyAsync(sl->buf.jobs[0], h_jobs, np * sizeof(BatchJob), cudaMemcpyHostToDevice, st));
     KD_TRY_CUDA(cudaMemcpyAsync(sl->buf.q_start, h_qs, (np + 1) * 4, cudaMemcpyHostToDevice, st));
     KD_TRY_CUDA(cudaMemcpyAsync(sl->buf.task_start, h_ts, (np + 1) * 4, cudaMemcpyHostToDevice, st));
-    const unsigned blocks = static_cast<unsigned>(s->sms * resident_blocks_per_sm(s->qp.metric, L.kmax));
-    int rc = enqueue_packet(L, sl->buf, 0, s->qp.metric, blocks, st);
-    if (rc) return rc;
   }
-  for (uint32_t j : L.other) {
-    const JobSpec& J = specs[j];
-    QueryParams qp = s->qp;
-    qp.k = J.k;
-    qp.path = PATH_PACKET;
-    int rc = query_on_device(J.tree, J.queries, J.nq, qp, J.out_d, J.out_i, st, J.status);
-    if (rc) return rc;
+  // the per-job launches fork first, so they run beside the fused kernel
+  int rc = enqueue_others(specs, L.other, s->qp, sl->side, st, nullptr, {});
+  if (rc) return rc;
+  if (np) {
+    const unsigned blocks = static_cast<unsigned>(s->sms * resident_blocks_per_sm(s->qp.metric));
+    rc = enqueue_packet(L, sl->buf, 0, s->qp.metric, blocks, st);
   }
+  join_others(sl->side, L.other.size(), st);
+  if (rc) return rc;
   KD_TRY_CUDA(cudaEventRecord(sl->done, st));
   return KD_OK;
 }
@@ -834,7 +857,11 @@ int kd_batch_create(const kd_batch_job* jobs, uint64_t n_jobs, double p, int has
     release_plan(b);
     return cuda_fail(e, "cudaMemcpy");
   }
-  b->blocks = static_cast<unsigned>(b->sms * resident_blocks_per_sm(qp.metric, L.kmax));
+  if ((rc = b->side.create())) {
+    release_plan(b);
+    return rc;
+  }
+  b->blocks = static_cast<unsigned>(b->sms * resident_blocks_per_sm(qp.metric));
   *out = b;
   return KD_OK;
 }
@@ -919,6 +946,10 @@ int kd_server_create(const kd_tree* const* trees, uint64_t n_trees, double p, in
     sl.out_i = reinterpret_cast<int64_t*>(extra);
     extra += round256(s->cap_out * 8);
     sl.status = reinterpret_cast<uint32_t*>(extra);
+    if ((rc = sl.side.create())) {
+      release_server(s);
+      return rc;
+    }
     cudaError_t e = cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaHostAlloc(&sl.host, host_bytes(s) + round256(SERVER_JOBS * 4), cudaHostAllocDefault);

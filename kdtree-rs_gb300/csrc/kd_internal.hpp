@@ -32,7 +32,12 @@ struct kd_tree {
   float* tc_w = nullptr;          // per point: |p_b|^2 (1 - 2^-12) - v^2, rounded down
   float* tc_v = nullptr;          // per point: 2^-8 |p_b|, rounded up
   double* tc_centre = nullptr;    // ndim, the root box centre
+  float* tc_tbox = nullptr;       // per 256-point tile: [lo | hi] FP32 enclosure (ndim each)
   uint32_t tc_dpad = 0;
+  // Width 16: which exact path the automatic choice measured faster on this
+  // tree (-1 not yet measured, 0 warp-per-query traversal, 1 tensor-core filter).
+  std::mutex choice_mutex;
+  int auto_choice = -1;
 };
 
 namespace kd {
@@ -95,7 +100,7 @@ int build_on_device(const double* d_src, uint64_t n_points, uint64_t ndim, uint6
 // Parameters of one query call after validation (src/query.rs:38-62).
 // Which query kernel runs (kd_query_device_path): the automatic choice, the
 // reference-order descent, the packet traversal, or the tensor-core filter.
-enum QueryPath : int { PATH_AUTO = 0, PATH_REFERENCE_ORDER = 1, PATH_PACKET = 2, PATH_TENSOR_CORE = 3 };
+enum QueryPath : int { PATH_AUTO = 0, PATH_REFERENCE_ORDER = 1, PATH_PACKET = 2, PATH_TENSOR_CORE = 3, PATH_WARP = 4 };
 
 struct QueryParams {
   int path = PATH_AUTO;
@@ -133,10 +138,14 @@ uint64_t order_scratch_words(const kd_tree* t);
 void order_by_landing_leaf(const kd_tree* t, const double* d_queries, uint64_t nq, uint32_t* leaf_of,
                            uint32_t* order, uint32_t* scratch, cudaStream_t stream);
 
-// The packet traversal (warp-shared descent, eps = 0, k <= 32, L1 / L2 /
+// The packet traversal (warp-shared descent, eps = 0, k <= 64, L1 / L2 /
 // L-inf, widths 2, 3, 8, 16): whether it covers a query, and its launch.
 bool packet_applicable(uint64_t d, int metric, uint64_t k, uint64_t n_points, bool use_eps);
 int launch_packet_query(const QArgs& a, int metric, cudaStream_t stream);
+// One warp per query (the same envelope with k <= 32): for trees whose queries
+// scan many leaf rows.
+bool warp_applicable(uint64_t d, int metric, uint64_t k, uint64_t n_points, bool use_eps);
+int launch_warp_query(const QArgs& a, int metric, cudaStream_t stream);
 
 // Exact k-NN through the tensor-core filter (L2, eps = 0, 16 <= d <= 128,
 // k <= 32).  Returns KD_OK, or KD_ERR_INVALID_ARGUMENT without doing anything

@@ -570,44 +570,56 @@ struct LazyHeap {
   }
 
   // write_results (query.rs:421-429, 483-493): the exact values sorted by
-  // (distance, index); empty slots after every real one.
-  __device__ __forceinline__ void write(double* od, int64_t* oi, uint64_t k_, uint64_t n_points) const {
-    uint64_t xb[K];
-    uint32_t id[K];
-#pragma unroll
-    for (int j = 0; j < K; ++j) {
-      if (static_cast<uint32_t>(j) < n) {
-        const uint32_t rj = row[j * S];
-        xb[j] = dbits(exact_of(rj, chunk_of(lo[j * S])));
-        id[j] = indices[rj];
+  // (distance, index), empty slots after every real one.  The slots are
+  // rewritten in place -- exact distance bits in lo / hi, original index in
+  // row -- and heap-sorted there, so no K-sized register array is needed.
+  __device__ __forceinline__ uint64_t key_at(uint32_t j) const {
+    return (static_cast<uint64_t>(__float_as_uint(hi[j * S])) << 32) | __float_as_uint(lo[j * S]);
+  }
+  __device__ __forceinline__ bool after(uint32_t a, uint32_t b) const {  // slot a sorts after slot b
+    const uint64_t ka = key_at(a), kb = key_at(b);
+    return ka > kb || (ka == kb && row[a * S] > row[b * S]);
+  }
+  __device__ __forceinline__ void swap_slots(uint32_t a, uint32_t b) {
+    const float l = lo[a * S], h = hi[a * S];
+    const uint32_t r = row[a * S];
+    lo[a * S] = lo[b * S];
+    hi[a * S] = hi[b * S];
+    row[a * S] = row[b * S];
+    lo[b * S] = l;
+    hi[b * S] = h;
+    row[b * S] = r;
+  }
+  __device__ __forceinline__ void sift_exact(uint32_t j, uint32_t m) {
+    for (;;) {
+      uint32_t c = 2 * j + 1;
+      if (c >= m) return;
+      if (c + 1 < m && after(c + 1, c)) ++c;
+      if (!after(c, j)) return;
+      swap_slots(j, c);
+      j = c;
+    }
+  }
+  __device__ __forceinline__ void write(double* od, int64_t* oi, uint64_t k_, uint64_t n_points) {
+    for (uint32_t j = 0; j < n; ++j) {
+      const uint32_t rj = row[j * S];
+      const uint64_t xb = dbits(exact_of(rj, chunk_of(lo[j * S])));
+      lo[j * S] = __uint_as_float(static_cast<uint32_t>(xb));
+      hi[j * S] = __uint_as_float(static_cast<uint32_t>(xb >> 32));
+      row[j * S] = indices[rj];
+    }
+    for (uint32_t j = n / 2; j-- > 0;) sift_exact(j, n);
+    for (uint32_t m = n; m > 1; --m) {
+      swap_slots(0, m - 1);
+      sift_exact(0, m - 1);
+    }
+    for (uint32_t j = 0; j < k_; ++j) {
+      if (j < n) {
+        od[j] = restore<M>(bitsd(key_at(j)), 0.0);
+        oi[j] = static_cast<int64_t>(row[j * S]);
       } else {
-        xb[j] = ~0ull;
-        id[j] = NO_ID;
-      }
-    }
-#pragma unroll
-    for (int i = 1; i < K; ++i) {
-#pragma unroll
-      for (int j = i; j > 0; --j) {
-        const bool sw = xb[j] < xb[j - 1] || (xb[j] == xb[j - 1] && id[j] < id[j - 1]);
-        const uint64_t tx = xb[j];
-        const uint32_t ti = id[j];
-        xb[j] = sw ? xb[j - 1] : xb[j];
-        id[j] = sw ? id[j - 1] : id[j];
-        xb[j - 1] = sw ? tx : xb[j - 1];
-        id[j - 1] = sw ? ti : id[j - 1];
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < K; ++j) {
-      if (static_cast<uint64_t>(j) < k_) {
-        if (xb[j] != ~0ull) {
-          od[j] = restore<M>(bitsd(xb[j]), 0.0);
-          oi[j] = static_cast<int64_t>(id[j]);
-        } else {
-          od[j] = bitsd(INF_BITS);
-          oi[j] = static_cast<int64_t>(n_points);
-        }
+        od[j] = bitsd(INF_BITS);
+        oi[j] = static_cast<int64_t>(n_points);
       }
     }
   }

@@ -509,10 +509,22 @@ int dispatch_d(const QArgs& a, cudaStream_t st) {
 
 // The packet traversal where it applies (eps = 0, not forced to the reference
 // order), else the reference-order kernels.
-int run_kernels(const QArgs& a, int metric, cudaStream_t st) {
-  if (!a.reference_order && !force_reference_order() &&
-      packet_applicable(a.d, metric, a.k, a.n_points, a.use_eps != 0))
-    return launch_packet_query(a, metric, st);
+// The automatic choice between the two eps = 0 traversals, from measurements on
+// GB300 (uniform and clustered data, N = 1M): one warp per query wins at
+// d >= 8, for k > 16, and for k >= 8 below a few hundred thousand queries (the
+// packet traversal's 32-query warps have long serial chains, which only a
+// large batch hides); the packet traversal wins for small k on big batches.
+bool warp_preferred(const QArgs& a) {
+  return a.d >= 8 || a.k > 16 || (a.k >= 8 && a.nq < 400000);
+}
+
+int run_kernels(const QArgs& a, int metric, cudaStream_t st, int path) {
+  if (!a.reference_order && !force_reference_order()) {
+    if ((path == PATH_WARP || (path == PATH_AUTO && warp_preferred(a))) &&
+        warp_applicable(a.d, metric, a.k, a.n_points, a.use_eps != 0))
+      return launch_warp_query(a, metric, st);
+    if (packet_applicable(a.d, metric, a.k, a.n_points, a.use_eps != 0)) return launch_packet_query(a, metric, st);
+  }
   switch (metric) {
     case M_L1: return dispatch_d<M_L1>(a, st);
     case M_L2: return dispatch_d<M_L2>(a, st);
@@ -541,14 +553,60 @@ void order_by_landing_leaf(const kd_tree* t, const double* d_queries, uint64_t n
   k_scatter_order<<<qb, 256, 0, st>>>(leaf_of, counts, nq, order);
 }
 
+// Width 16 (L2, eps = 0) has two exact paths: the tensor-core filter, which
+// scores whole point tiles, and the warp-per-query traversal, which wins where
+// the tree prunes well.  The first automatic query on a tree times both on
+// a sample of its batch (the first min(n, 16384) queries, written to the
+// caller's outputs -- both paths produce the same values) and the tree keeps
+// the faster for every later call.
+int auto_prefers_tc(kd_tree* t, const double* d_queries, uint64_t nq, const QueryParams& qp, double* d_out_d,
+                    int64_t* d_out_i, cudaStream_t st, uint32_t* d_status, bool* tc) {
+  std::lock_guard<std::mutex> lock(t->choice_mutex);
+  if (t->auto_choice >= 0) {
+    *tc = t->auto_choice == 1;
+    return KD_OK;
+  }
+  const uint64_t ns = std::min<uint64_t>(nq, 16384);
+  QueryParams pq = qp;
+  pq.path = PATH_WARP;
+  cudaEvent_t e[3];
+  for (cudaEvent_t& x : e) KD_TRY_CUDA(cudaEventCreate(&x));
+  int rc = query_tc_on_device(t, d_queries, ns, qp, d_out_d, d_out_i, st, d_status, nullptr);  // warm-up
+  if (!rc) rc = cudaEventRecord(e[0], st) == cudaSuccess ? KD_OK : cuda_fail(cudaErrorUnknown, "cudaEventRecord");
+  if (!rc) rc = query_tc_on_device(t, d_queries, ns, qp, d_out_d, d_out_i, st, d_status, nullptr);
+  if (!rc) cudaEventRecord(e[1], st);
+  if (!rc) rc = query_on_device(t, d_queries, ns, pq, d_out_d, d_out_i, st, d_status, nullptr);
+  if (!rc) cudaEventRecord(e[2], st);
+  float ms_tc = 0.f, ms_pk = 0.f;
+  if (!rc) {
+    cudaError_t err = cudaEventSynchronize(e[2]);
+    if (err != cudaSuccess) rc = cuda_fail(err, "cudaEventSynchronize");
+    cudaEventElapsedTime(&ms_tc, e[0], e[1]);
+    cudaEventElapsedTime(&ms_pk, e[1], e[2]);
+  }
+  for (cudaEvent_t x : e) cudaEventDestroy(x);
+  if (rc) return rc;
+  t->auto_choice = ms_tc <= ms_pk ? 1 : 0;
+  *tc = t->auto_choice == 1;
+  return KD_OK;
+}
+
 int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, const QueryParams& qp,
                     double* d_out_d, int64_t* d_out_i, cudaStream_t st, uint32_t* d_status,
                     unsigned long long* d_survivors) {
-  // d >= 16, L2, eps = 0: the tensor-core filter (the tree stops pruning there)
+  // d >= 16, L2, eps = 0: the tensor-core filter, unless (d = 16, automatic
+  // choice) the warp-per-query traversal measured faster on this tree
   const bool tc_allowed = qp.path == PATH_TENSOR_CORE || (qp.path == PATH_AUTO && !force_reference_order());
-  if (tc_allowed && tc_applicable(t, qp))
-    return query_tc_on_device(const_cast<kd_tree*>(t), d_queries, nq, qp, d_out_d, d_out_i, st, d_status,
-                              d_survivors);
+  if (tc_allowed && tc_applicable(t, qp)) {
+    bool tc = true;
+    if (qp.path == PATH_AUTO && warp_applicable(t->ndim, qp.metric, qp.k, t->n_points, false)) {
+      int rc = auto_prefers_tc(const_cast<kd_tree*>(t), d_queries, nq, qp, d_out_d, d_out_i, st, d_status, &tc);
+      if (rc) return rc;
+    }
+    if (tc)
+      return query_tc_on_device(const_cast<kd_tree*>(t), d_queries, nq, qp, d_out_d, d_out_i, st, d_status,
+                                d_survivors);
+  }
   QArgs a{};
   a.reference_order = qp.path == PATH_REFERENCE_ORDER;
   a.data = t->data;
@@ -594,7 +652,7 @@ int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, cons
       sort_mem = nullptr;
     }
   }
-  const int rc = run_kernels(a, qp.metric, st);
+  const int rc = run_kernels(a, qp.metric, st, qp.path);
   if (axes) cudaFreeAsync(axes, st);
   if (sort_mem) cudaFreeAsync(sort_mem, st);
   return rc;
@@ -624,7 +682,7 @@ int query_on_device_scratch(const kd_tree* t, const double* d_queries, uint64_t 
   a.eps_factor = qp.eps_factor;
   a.use_eps = qp.eps_factor != 1.0;
   a.axes_scratch = d_axes_scratch;
-  return run_kernels(a, qp.metric, st);
+  return run_kernels(a, qp.metric, st, qp.path);
 }
 
 }  // namespace kd

@@ -1,7 +1,9 @@
 // kd_query_packet.cu -- launches of the packet traversal (kd_query_packet.cuh)
-// for the compile-time widths 2, 3, 8 and 16 and the L1 / L2 / L-inf metrics;
+// for the compile-time widths 2, 3, 8 and 16, the L1 / L2 / L-inf metrics and
+// k <= 64 (k-best lists of 1, 4, 8, 16, 32 or 64 slots);
 // a translation unit of its own so it compiles in parallel with the other
 // query kernels.
+#include <cstdlib>
 #include <type_traits>
 
 #include "kd_internal.hpp"
@@ -12,15 +14,54 @@ namespace {
 #include "kd_query_common.cuh"
 #include "kd_lazy_best.cuh"
 #include "kd_query_packet.cuh"
+#include "kd_query_warp.cuh"
+
+// The shared-memory share of the unified L1 / shared storage the packet
+// kernels ask for (cudaFuncAttributePreferredSharedMemoryCarveout, percent):
+// the heaps live in shared memory, the tree's nodes, boxes and rows come
+// through L1.  With 16-slot heaps (26 KB per block) 75 % -- six blocks per SM
+// and the rest for L1 -- measured 11 % faster on GB300 than the driver's choice
+// of eight blocks (N = 1M, d = 3, k = 16).  KD_PACKET_CARVEOUT (0..100)
+// overrides it for every k; unset, the other k keep the driver's choice.
+int carveout_override() {
+  static const int v = [] {
+    const char* e = std::getenv("KD_PACKET_CARVEOUT");
+    return e ? std::atoi(e) : -1;
+  }();
+  return v;
+}
+
+template <int K, typename F>
+void apply_carveout(F* kernel) {
+  int v = carveout_override();
+  if (v < 0 && K == 16) v = 75;
+  if (v >= 0) cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+}
 
 template <int M, int D>
 int launch_k(const QArgs& a, cudaStream_t st) {
   const unsigned blocks = static_cast<unsigned>((a.nq + QUERY_THREADS - 1) / QUERY_THREADS);
-  if (a.k == 1) k_query_packet<M, D, 1><<<blocks, QUERY_THREADS, 0, st>>>(a);
-  else if (a.k <= 4) k_query_packet<M, D, 4><<<blocks, QUERY_THREADS, 0, st>>>(a);
-  else if (a.k <= 8) k_query_packet<M, D, 8><<<blocks, QUERY_THREADS, 0, st>>>(a);
-  else if (a.k <= 16) k_query_packet<M, D, 16><<<blocks, QUERY_THREADS, 0, st>>>(a);
-  else k_query_packet<M, D, 32><<<blocks, QUERY_THREADS, 0, st>>>(a);
+  if (a.k == 1) {
+    apply_carveout<1>(k_query_packet<M, D, 1>);
+    k_query_packet<M, D, 1><<<blocks, QUERY_THREADS, 0, st>>>(a);
+  } else if (a.k <= 4) {
+    apply_carveout<4>(k_query_packet<M, D, 4>);
+    k_query_packet<M, D, 4><<<blocks, QUERY_THREADS, 0, st>>>(a);
+  } else if (a.k <= 8) {
+    apply_carveout<8>(k_query_packet<M, D, 8>);
+    k_query_packet<M, D, 8><<<blocks, QUERY_THREADS, 0, st>>>(a);
+  } else if (a.k <= 16) {
+    apply_carveout<16>(k_query_packet<M, D, 16>);
+    k_query_packet<M, D, 16><<<blocks, QUERY_THREADS, 0, st>>>(a);
+  } else if (a.k <= 32) {
+    apply_carveout<32>(k_query_packet<M, D, 32>);
+    k_query_packet<M, D, 32><<<blocks, QUERY_THREADS, 0, st>>>(a);
+  } else {
+    constexpr size_t smem = sizeof(PacketSmem<64>);
+    KD_TRY_CUDA(cudaFuncSetAttribute(k_query_packet_dyn<M, D, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem)));
+    k_query_packet_dyn<M, D, 64><<<blocks, QUERY_THREADS, smem, st>>>(a);
+  }
   KD_TRY_CUDA(cudaGetLastError());
   return KD_OK;
 }
@@ -35,10 +76,37 @@ int launch_d(const QArgs& a, cudaStream_t st) {
   }
 }
 
+template <int M>
+int launch_warp_d(const QArgs& a, cudaStream_t st) {
+  const unsigned blocks = static_cast<unsigned>((a.nq + QUERY_THREADS / 32 - 1) / (QUERY_THREADS / 32));
+  switch (a.d) {
+    case 2: k_query_warp<M, 2><<<blocks, QUERY_THREADS, 0, st>>>(a); break;
+    case 3: k_query_warp<M, 3><<<blocks, QUERY_THREADS, 0, st>>>(a); break;
+    case 8: k_query_warp<M, 8><<<blocks, QUERY_THREADS, 0, st>>>(a); break;
+    default: k_query_warp<M, 16><<<blocks, QUERY_THREADS, 0, st>>>(a); break;
+  }
+  KD_TRY_CUDA(cudaGetLastError());
+  return KD_OK;
+}
+
 }  // namespace
 
+bool warp_applicable(uint64_t d, int metric, uint64_t k, uint64_t n_points, bool use_eps) {
+  return packet_applicable(d, metric, k, n_points, use_eps) && k <= 32;
+}
+
+int launch_warp_query(const QArgs& a, int metric, cudaStream_t st) {
+  if (!warp_applicable(a.d, metric, a.k, a.n_points, a.use_eps))
+    return fail(KD_ERR_INVALID_ARGUMENT, "the warp-per-query kernel does not cover this query");
+  switch (metric) {
+    case M_L1: return launch_warp_d<M_L1>(a, st);
+    case M_L2: return launch_warp_d<M_L2>(a, st);
+    default: return launch_warp_d<M_LINF>(a, st);
+  }
+}
+
 bool packet_applicable(uint64_t d, int metric, uint64_t k, uint64_t n_points, bool use_eps) {
-  return metric != M_LP && !use_eps && k >= 1 && k <= 32 && n_points < 0xffffffffull &&
+  return metric != M_LP && !use_eps && k >= 1 && k <= 64 && n_points < 0xffffffffull &&
          (d == 2 || d == 3 || d == 8 || d == 16);
 }
 

@@ -142,6 +142,39 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
     best.init(a.k, a.cutoff, &q, a.data, a.indices);
   float thr = filt.threshold(best.b_hi);
 
+  // Seed: each lane first offers the points of its own landing leaf (reached
+  // by comparing FP32 copies; any leaf would be correct, this one is near), so
+  // its bound is tight before the shared traversal starts; the traversal then
+  // skips that leaf for this lane.
+  uint32_t own = NO_ID;
+  if (live) {
+    uint32_t n = 0;
+    DNode nd = a.nodes[0];
+    while (!(nd.meta & KD_NODE_LEAF)) {
+      const uint32_t dim = nd.meta & KD_NODE_DIM_MASK;
+      float qv = filt.q32[0];
+#pragma unroll
+      for (int i = 1; i < D; ++i) qv = (static_cast<uint32_t>(i) == dim) ? filt.q32[i] : qv;
+      n = qv <= __double2float_rn(nd.split) ? n + 1 : nd.right;
+      nd = a.nodes[n];
+    }
+    own = n;
+    const uint64_t se = dbits(nd.split);
+    const uint32_t start = static_cast<uint32_t>(se), end = static_cast<uint32_t>(se >> 32);
+    const uint32_t chunk_end = (D == 8 && M != M_LINF) ? start + (end - start) / 8 * 8 : end;
+    for (uint32_t r = start; r < end; ++r) {
+      const float sr = filt.sum(a.data32 + static_cast<uint64_t>(r) * D);
+      if (!(sr > thr)) {
+        float clo, chi;
+        filt.enclose(sr, &clo, &chi);
+        if (!(clo > best.b_hi)) {
+          best.offer(clo, chi, r, r < chunk_end);
+          thr = filt.threshold(best.b_hi);
+        }
+      }
+    }
+  }
+
   // Every lane pushes the same ids to the same words and pops what it pushed
   // itself, so no lane depends on another's store.
   uint32_t* stack = s_stack + (threadIdx.x >> 5) * PACKET_STACK;
@@ -155,6 +188,8 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
     if (!need_mask) continue;  // every lane's points there exceed its bound
     const DNode nd = a.nodes[node];
     if (nd.meta & KD_NODE_LEAF) {
+      const bool take = need && node != own;  // its own leaf was offered already
+      if (!__any_sync(0xffffffffu, take)) continue;
       const uint64_t se = dbits(nd.split);
       const uint32_t start = static_cast<uint32_t>(se), end = static_cast<uint32_t>(se >> 32);
       const uint32_t chunk_end = (D == 8 && M != M_LINF) ? start + (end - start) / 8 * 8 : end;
@@ -164,7 +199,7 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
         uint32_t pending = 0;
         for (uint32_t r = c0; r < c1; ++r) {
           const float s = filt.sum(a.data32 + static_cast<uint64_t>(r) * D);
-          if (need && !(s > thr)) pending |= 1u << (r - c0);
+          if (take && !(s > thr)) pending |= 1u << (r - c0);
         }
         // 2. offer them, all lanes with a pending point together
         while (__any_sync(0xffffffffu, pending != 0)) {
@@ -204,4 +239,14 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query_packet(QArgs a) {
   __shared__ PacketSmem<K> sm;
   packet_queries<M, D, K>(a, blockIdx.x * static_cast<uint64_t>(QUERY_THREADS) + threadIdx.x, sm.lo, sm.hi,
                           sm.row, sm.stack);
+}
+
+// The same with the shared memory supplied at launch (sizeof(PacketSmem<K>)
+// bytes): for k-best heaps larger than a static allocation may be (K = 64).
+template <int M, int D, int K>
+__global__ void __launch_bounds__(QUERY_THREADS) k_query_packet_dyn(QArgs a) {
+  extern __shared__ __align__(16) unsigned char packet_dyn[];
+  PacketSmem<K>* sm = reinterpret_cast<PacketSmem<K>*>(packet_dyn);
+  packet_queries<M, D, K>(a, blockIdx.x * static_cast<uint64_t>(QUERY_THREADS) + threadIdx.x, sm->lo, sm->hi,
+                          sm->row, sm->stack);
 }

@@ -25,10 +25,15 @@
 // within max_distance -- the reference's answer for eps = 0.
 //
 // Pipeline (one persistent CTA per SM, a 128-query tile at a time):
-//   warp 0  TMA: the query tile once, then 256-point tiles into a ring of stages
+//   warp 0  TMA: the query tile once, then 256-point tiles into a ring of
+//           stages, nearest tiles first; a point tile whose FP32 box bound to
+//           the query tile's box exceeds the largest current bound of the
+//           query tile's rows is skipped (clustered data: the tiles of other
+//           clusters), and an end marker closes the query tile
 //   warp 1  tcgen05.mma: 128 x 256 x d into one of two TMEM accumulators
 //   warps 2-5  epilogue: tcgen05.ld one accumulator row per thread, filter,
-//              refine, offer; free the accumulator for the next tile.
+//              refine, offer; free the accumulator for the next tile; publish
+//              the warp's largest bound for the producer's skip test.
 // Every wait is bounded; a timeout sets an error bit and all roles leave.
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -51,6 +56,7 @@ constexpr int TC_KC = 64;        // BF16 elements per 128-byte swizzled row chun
 constexpr int TC_THREADS = 192;  // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 constexpr uint32_t TC_SPIN = 1u << 22;
 constexpr uint32_t TC_STATUS_TIMEOUT = 2u;
+constexpr uint32_t TC_END = 0xffffffffu;  // stage / accumulator marker: the query tile is done
 
 struct TcArgs {
   const double* queries;  // nq x d, FP64
@@ -64,6 +70,8 @@ struct TcArgs {
   const float* qnorm;     // |q_b| rounded up
   const float* pw;        // per point w (padded to whole tiles with +inf)
   const float* pv;        // per point v (padding 0)
+  const float* qbox;      // per query tile: [lo | hi] FP32 enclosure of its queries (d each)
+  const float* tbox;      // per point tile: [lo | hi] FP32 enclosure of its points (d each)
   double* out_d;
   int64_t* out_i;
   uint32_t* status;
@@ -156,6 +164,20 @@ __device__ __forceinline__ uint32_t zigzag(uint32_t s, uint32_t i, uint32_t n) {
   return right > left ? s + m + off : s - m - off;
 }
 
+// Lower bound of the exact FP64 reduced distance between any query of a tile
+// and any point of a tile, from their FP32 box enclosures ([lo | hi], d each):
+// per-axis gaps rounded down, squared and summed rounded down, then the FP64
+// rounding margin of box_lb.
+__device__ __forceinline__ float tile_lb(const float* qb, const float* tb, uint64_t d) {
+  float lb = 0.f;
+  for (uint64_t i = 0; i < d; ++i) {
+    float o = fmaxf(__fsub_rd(tb[i], qb[d + i]), __fsub_rd(qb[i], tb[d + i]));
+    o = o > 0.f ? o : 0.f;
+    lb = __fadd_rd(lb, __fmul_rd(o, o));
+  }
+  return __fmul_rd(lb, LB_SHRINK);
+}
+
 template <int K>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_query_tc(const __grid_constant__ CUtensorMap tmap_q, const __grid_constant__ CUtensorMap tmap_p, TcArgs a) {
@@ -177,7 +199,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   __shared__ int s_abort;
   __shared__ unsigned long long s_surv;
   __shared__ int s_zero;  // a flag that never rises: the drain waits ignore aborts
+  __shared__ uint32_t s_tile[4];      // per stage: the point tile it holds, or TC_END
+  __shared__ uint32_t s_acc_tile[2];  // per accumulator: the point tile it scored, or TC_END
+  __shared__ float s_wb[4];           // per epilogue warp: the largest bound of its rows ...
+  __shared__ uint32_t s_wq[4];        // ... for the CTA's query tile number s_wq
   volatile int* abort_flag = &s_abort;
+  volatile uint32_t* v_tile = s_tile;
+  volatile uint32_t* v_acc_tile = s_acc_tile;
+  volatile float* v_wb = s_wb;
+  volatile uint32_t* v_wq = s_wq;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -186,8 +216,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       mbar_init(smem_u32(&empty[s]), 1);
     }
     for (int b = 0; b < 2; ++b) {
-      mbar_init(smem_u32(&accf[b]), 1);
+      mbar_init(smem_u32(&accf[b]), 2);  // the MMA thread's arrive (tile id) + the MMA commit
       mbar_init(smem_u32(&acce[b]), 4 * 32);
+    }
+    for (int w = 0; w < 4; ++w) {
+      s_wb[w] = __int_as_float(0x7f800000);
+      s_wq[w] = TC_END;
     }
     mbar_init(smem_u32(qfull), 1);
     mbar_init(smem_u32(qempty), 1);
@@ -208,36 +242,79 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const uint32_t tmem = s_tmem;
 
   if (warp == 0) {
-    // ---------------- TMA producer ----------------
-    if (lane == 0) {
-      uint32_t ld = 0, qj = 0;
-      uint32_t last_use[4] = {0, 0, 0, 0};
-      for (uint32_t qt = blockIdx.x; qt < a.n_qt && !*abort_flag; qt += gridDim.x, ++qj) {
-        if (!mbar_wait(smem_u32(qempty), (qj & 1) ^ 1, abort_flag)) break;
-        mbar_expect_tx(smem_u32(qfull), q_bytes);
-        for (uint32_t kc = 0; kc < kch; ++kc)
-          tma_load_2d(smem_u32(s_q + kc * TC_M * 128), &tmap_q, kc * TC_KC, qt * TC_M, smem_u32(qfull));
-        bool ok = true;
-        for (uint32_t pt = 0; pt < a.n_pt; ++pt, ++ld) {
-          const uint32_t s = ld % nst, u = ld / nst;
-          if (!mbar_wait(smem_u32(&empty[s]), (u & 1) ^ 1, abort_flag)) {
-            ok = false;
-            break;
-          }
-          unsigned char* dst = s_p + s * p_bytes;
-          mbar_expect_tx(smem_u32(&full[s]), p_bytes);
+    // ---------------- TMA producer (the whole warp decides, lane 0 issues) ----------------
+    // A point tile is skipped when its box bound exceeds the largest current
+    // bound of the query tile's rows (published by the epilogue warps for this
+    // query tile; none published yet: nothing is skipped).  Bounds only shrink,
+    // so every skipped pair is farther than its query's final k-th best.
+    uint32_t ld = 0, qj = 0;
+    uint32_t last_use[4] = {0, 0, 0, 0};
+    int ok = 1;
+    for (uint32_t qt = blockIdx.x; qt < a.n_qt && ok; qt += gridDim.x, ++qj) {
+      if (lane == 0) {
+        ok = mbar_wait(smem_u32(qempty), (qj & 1) ^ 1, abort_flag);
+        if (ok) {
+          mbar_expect_tx(smem_u32(qfull), q_bytes);
           for (uint32_t kc = 0; kc < kch; ++kc)
-            tma_load_2d(smem_u32(dst + kc * TC_N * 128), &tmap_p, kc * TC_KC,
-                        zigzag(a.tile_start[qt], pt, a.n_pt) * TC_N, smem_u32(&full[s]));
+            tma_load_2d(smem_u32(s_q + kc * TC_M * 128), &tmap_q, kc * TC_KC, qt * TC_M, smem_u32(qfull));
+        }
+      }
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) break;
+      const float* qb = a.qbox + static_cast<uint64_t>(qt) * 2 * a.d;
+      for (uint32_t p0 = 0; p0 < a.n_pt && ok; p0 += 32) {
+        const uint32_t pt = p0 + lane;
+        uint32_t tile = 0;
+        float lb = __int_as_float(0x7f800000);
+        if (pt < a.n_pt) {
+          tile = zigzag(a.tile_start[qt], pt, a.n_pt);
+          lb = tile_lb(qb, a.tbox + static_cast<uint64_t>(tile) * 2 * a.d, a.d);
+        }
+        for (int j = 0; j < 32 && ok; ++j) {
+          const uint32_t tj = __shfl_sync(0xffffffffu, tile, j);
+          const float lbj = __shfl_sync(0xffffffffu, lb, j);
+          if (p0 + j >= a.n_pt) break;
+          if (lane == 0) {
+            bool cur = true;
+            for (int w = 0; w < 4; ++w) cur = cur && v_wq[w] == qj;
+            __threadfence_block();
+            float bound = __int_as_float(0x7f800000);
+            if (cur) bound = fmaxf(fmaxf(v_wb[0], v_wb[1]), fmaxf(v_wb[2], v_wb[3]));
+            if (!(lbj > bound)) {
+              const uint32_t s = ld % nst, u = ld / nst;
+              ok = mbar_wait(smem_u32(&empty[s]), (u & 1) ^ 1, abort_flag);
+              if (ok) {
+                v_tile[s] = tj;
+                unsigned char* dst = s_p + s * p_bytes;
+                mbar_expect_tx(smem_u32(&full[s]), p_bytes);
+                for (uint32_t kc = 0; kc < kch; ++kc)
+                  tma_load_2d(smem_u32(dst + kc * TC_N * 128), &tmap_p, kc * TC_KC, tj * TC_N, smem_u32(&full[s]));
+                last_use[s] = u + 1;
+              }
+              ++ld;
+            }
+          }
+          ok = __shfl_sync(0xffffffffu, ok, 0);
+        }
+      }
+      if (!ok) break;
+      if (lane == 0) {  // the query tile's end marker
+        const uint32_t s = ld % nst, u = ld / nst;
+        ok = mbar_wait(smem_u32(&empty[s]), (u & 1) ^ 1, abort_flag);
+        if (ok) {
+          v_tile[s] = TC_END;
+          mbar_arrive(smem_u32(&full[s]));
           last_use[s] = u + 1;
         }
-        if (!ok) break;
+        ++ld;
       }
-      if (*abort_flag) {  // let copies already issued land before the CTA leaves
-        for (uint32_t s = 0; s < nst; ++s)
-          if (last_use[s]) mbar_wait(smem_u32(&full[s]), (last_use[s] - 1) & 1, &s_zero);
-      }
+      ok = __shfl_sync(0xffffffffu, ok, 0);
     }
+    if (lane == 0 && *abort_flag) {  // let copies already issued land before the CTA leaves
+      for (uint32_t s = 0; s < nst; ++s)
+        if (last_use[s]) mbar_wait(smem_u32(&full[s]), (last_use[s] - 1) & 1, &s_zero);
+    }
+    if (lane == 0 && !ok) atomicExch(&s_abort, 1);
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
@@ -250,12 +327,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           ok = false;
           break;
         }
-        for (uint32_t pt = 0; pt < a.n_pt; ++pt, ++ld, ++t) {
+        for (;;) {  // the producer's tiles for this query tile, up to its end marker
           const uint32_t b = t & 1, ub = t >> 1;
           const uint32_t s = ld % nst, us = ld / nst;
           if (!mbar_wait(smem_u32(&acce[b]), (ub & 1) ^ 1, abort_flag) ||
               !mbar_wait(smem_u32(&full[s]), us & 1, abort_flag)) {
             ok = false;
+            break;
+          }
+          const uint32_t tile = v_tile[s];
+          ++ld;
+          ++t;
+          if (tile == TC_END) {
+            mbar_arrive(smem_u32(&empty[s]));  // the stage carried no data
+            v_acc_tile[b] = TC_END;
+            mbar_arrive(smem_u32(&accf[b]));
+            mbar_arrive(smem_u32(&accf[b]));
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;");
@@ -267,6 +354,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             for (uint32_t k = 0; k < TC_KC / 16; ++k)
               umma_bf16(d_tmem, ad + 2 * k, bd + 2 * k, idesc, (kc | k) ? 1u : 0u);  // +32 B per K step
           }
+          v_acc_tile[b] = tile;
+          mbar_arrive(smem_u32(&accf[b]));  // publishes the tile id; the commit below completes the phase
           umma_commit(smem_u32(&empty[s]));
           umma_commit(smem_u32(&accf[b]));
         }
@@ -278,10 +367,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // ---------------- epilogue: one query row per thread ----------------
     const uint32_t quarter = static_cast<uint32_t>(warp & 3);  // TMEM lanes this warp may read
     const uint32_t row = quarter * 32 + lane;
-    uint32_t t = 0;
+    uint32_t t = 0, qj = 0;
     unsigned long long surv = 0;
     bool ok = true;
-    for (uint32_t qt = blockIdx.x; qt < a.n_qt && ok; qt += gridDim.x) {
+    for (uint32_t qt = blockIdx.x; qt < a.n_qt && ok; qt += gridDim.x, ++qj) {
       const uint64_t srow = static_cast<uint64_t>(qt) * TC_M + row;  // sorted row
       const bool active = srow < a.nq;
       const uint64_t qrow = active ? srow : 0;
@@ -297,14 +386,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const float qn2 = a.qn2[qrow], qnorm = a.qnorm[qrow];
       float m2r, thr;
       tc_threshold(set.b_hi, qn2, qnorm, &m2r, &thr);
-      for (uint32_t pt = 0; pt < a.n_pt; ++pt, ++t) {
+      if (lane == 0) {  // this query tile's bound: none yet
+        v_wb[warp - 2] = __int_as_float(0x7f800000);
+        __threadfence_block();
+        v_wq[warp - 2] = qj;
+      }
+      for (;;) {
         const uint32_t b = t & 1, ub = t >> 1;
-        if (!mbar_wait(smem_u32(&accf[b]), ub & 1, abort_flag)) {
+        // warp-uniform outcome: the lanes below shuffle and load TMEM together
+        if (!__all_sync(0xffffffffu, mbar_wait(smem_u32(&accf[b]), ub & 1, abort_flag))) {
           ok = false;
           break;
         }
+        const uint32_t tile = v_acc_tile[b];
+        ++t;
+        if (tile == TC_END) {
+          mbar_arrive(smem_u32(&acce[b]));
+          break;
+        }
         asm volatile("tcgen05.fence::after_thread_sync;");
-        const uint32_t base = zigzag(a.tile_start[qt], pt, a.n_pt) * TC_N;
+        const uint32_t base = tile * TC_N;
         for (uint32_t c = 0; c < TC_N; c += 32) {
           uint32_t r[32];
           tmem_ld32(tmem + ((quarter * 32) << 16) + b * TC_N + c, r);
@@ -353,6 +454,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         asm volatile("tcgen05.fence::before_thread_sync;");
         mbar_arrive(smem_u32(&acce[b]));
+        // publish the largest bound of this warp's rows
+        float mb = active ? set.b_hi : 0.f;
+#pragma unroll
+        for (int off = 16; off; off >>= 1) mb = fmaxf(mb, __shfl_xor_sync(0xffffffffu, mb, off));
+        if (lane == 0) v_wb[warp - 2] = mb;
       }
       if (ok && active) set.write(a.out_d + qi * a.k, a.out_i + qi * a.k, a.k, a.n_points);
     }
@@ -422,6 +528,25 @@ __global__ void k_f32_gather(const double* src, const uint32_t* order, uint64_t 
   dst[f] = __double2float_rn(src[static_cast<uint64_t>(order[r]) * d + j]);
 }
 
+// FP32 box enclosure ([lo | hi], d each) of each tile of `rows` consecutive
+// rows of a row-major FP32 array: every coordinate's round-to-nearest copy x32
+// stands for a value in [x32 - e, x32 + e] (rn_enclose).  One block per tile,
+// thread j takes dimension j (blockDim >= d).
+__global__ void k_tile_boxes(const float* x32, uint64_t n, uint64_t d, uint32_t rows, float* box) {
+  const uint64_t t = blockIdx.x, j = threadIdx.x;
+  if (j >= d) return;
+  float lo = __int_as_float(0x7f800000), hi = __int_as_float(0xff800000);
+  const uint64_t r0 = t * rows, r1 = min(n, r0 + rows);
+  for (uint64_t r = r0; r < r1; ++r) {
+    float l, h;
+    rn_enclose(x32[r * d + j], &l, &h);
+    lo = fminf(lo, l);
+    hi = fmaxf(hi, h);
+  }
+  box[t * 2 * d + j] = lo;
+  box[t * 2 * d + d + j] = hi;
+}
+
 // Point tile of each query tile's middle query's landing leaf.
 __global__ void k_tile_start(const DNode* nodes, const uint32_t* leaf_of, const uint32_t* order, uint64_t nq,
                              uint32_t n_qt, uint32_t* tile_start) {
@@ -478,25 +603,30 @@ int ensure_tc_points(kd_tree* t, cudaStream_t st) {
   const uint64_t n = t->n_points, d = t->ndim;
   const uint32_t dpad = static_cast<uint32_t>((d + TC_KC - 1) / TC_KC * TC_KC);
   const uint64_t n_pad = (n + TC_N - 1) / TC_N * TC_N;
+  const uint64_t n_pt = n_pad / TC_N;
   uint16_t* pts = nullptr;
-  float *w = nullptr, *v = nullptr;
+  float *w = nullptr, *v = nullptr, *tbox = nullptr;
   double* centre = nullptr;
   if (cudaMalloc(&pts, n * dpad * sizeof(uint16_t)) != cudaSuccess ||
       cudaMalloc(&w, n_pad * sizeof(float)) != cudaSuccess || cudaMalloc(&v, n_pad * sizeof(float)) != cudaSuccess ||
-      cudaMalloc(&centre, d * sizeof(double)) != cudaSuccess) {
+      cudaMalloc(&centre, d * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&tbox, n_pt * 2 * d * sizeof(float)) != cudaSuccess) {
     cudaGetLastError();
     cudaFree(pts);
     cudaFree(w);
     cudaFree(v);
     cudaFree(centre);
+    cudaFree(tbox);
     return fail(KD_ERR_OUT_OF_MEMORY, "device allocation failed");
   }
   k_centre<<<static_cast<unsigned>((d + 127) / 128), 128, 0, st>>>(t->boxes, d, centre);
   k_tc_rows<<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(t->data, nullptr, n, d, dpad, centre, pts,
                                                                      nullptr, nullptr, w, v);
   if (n_pad > n) k_tc_pad<<<1, 256, 0, st>>>(w, v, n, n_pad);
+  k_tile_boxes<<<static_cast<unsigned>(n_pt), 128, 0, st>>>(t->data32, n, d, TC_N, tbox);
   KD_TRY_CUDA(cudaGetLastError());
   KD_TRY_CUDA(cudaStreamSynchronize(st));
+  t->tc_tbox = tbox;
   t->tc_points = pts;
   t->tc_w = w;
   t->tc_v = v;
@@ -525,7 +655,8 @@ int query_tc_on_device(kd_tree* t, const double* d_queries, uint64_t nq, const Q
   const uint64_t qbytes = nq * dpad * sizeof(uint16_t), fbytes = nq * sizeof(float);
   const uint64_t q32_bytes = nq * d * sizeof(float);
   const uint64_t sort_words = 2 * nq + order_scratch_words(t) + n_qt;
-  const uint64_t total = qbytes + 2 * fbytes + q32_bytes + sort_words * sizeof(uint32_t) + 256;
+  const uint64_t qbox_bytes = static_cast<uint64_t>(n_qt) * 2 * d * sizeof(float);
+  const uint64_t total = qbytes + 2 * fbytes + q32_bytes + qbox_bytes + sort_words * sizeof(uint32_t) + 256;
   if (dev_alloc(&mem, total, st) != cudaSuccess) {
     cudaGetLastError();
     return fail(KD_ERR_OUT_OF_MEMORY, "device allocation failed");
@@ -534,7 +665,8 @@ int query_tc_on_device(kd_tree* t, const double* d_queries, uint64_t nq, const Q
   float* qn2 = reinterpret_cast<float*>(static_cast<unsigned char*>(mem) + qbytes);
   float* qnorm = qn2 + nq;
   float* q32 = qnorm + nq;
-  uint32_t* leaf_of = reinterpret_cast<uint32_t*>(q32 + nq * d);
+  float* qbox = q32 + nq * d;
+  uint32_t* leaf_of = reinterpret_cast<uint32_t*>(qbox + static_cast<uint64_t>(n_qt) * 2 * d);
   uint32_t* order = leaf_of + nq;
   uint32_t* tile_start = order + nq;
   uint32_t* scratch = tile_start + n_qt;
@@ -543,6 +675,7 @@ int query_tc_on_device(kd_tree* t, const double* d_queries, uint64_t nq, const Q
   k_tc_rows<<<static_cast<unsigned>((nq + 255) / 256), 256, 0, st>>>(d_queries, order, nq, d, dpad, t->tc_centre, qb,
                                                                       qn2, qnorm, nullptr, nullptr);
   k_f32_gather<<<static_cast<unsigned>((nq * d + 255) / 256), 256, 0, st>>>(d_queries, order, nq, d, q32);
+  k_tile_boxes<<<n_qt, 128, 0, st>>>(q32, nq, d, TC_M, qbox);
   CUtensorMap mq, mp;
   if ((rc = make_rows_map(&mq, qb, nq, dpad, TC_M)) || (rc = make_rows_map(&mp, t->tc_points, t->n_points, dpad, TC_N))) {
     cudaFreeAsync(mem, st);
@@ -560,6 +693,8 @@ int query_tc_on_device(kd_tree* t, const double* d_queries, uint64_t nq, const Q
   a.qnorm = qnorm;
   a.pw = t->tc_w;
   a.pv = t->tc_v;
+  a.qbox = qbox;
+  a.tbox = t->tc_tbox;
   a.out_d = d_out_d;
   a.out_i = d_out_i;
   a.status = d_status;

@@ -88,16 +88,35 @@ def _path_query(tree, q, k, p, path):
 
 @pytest.mark.parametrize("p", [1.0, 2.0, float("inf")])
 @pytest.mark.parametrize("dist", ["uniform", "gmm"])
-@pytest.mark.parametrize("k", [1, 4, 8, 16, 32])
+@pytest.mark.parametrize("k", [1, 4, 8, 16, 32, 50])
 def test_packet_width16(oracle, p, dist, k):
     """Width 16 through the packet traversal (Folded L1 / L2 order,
-    kernel.rs:343-354): bit-exact with the oracle."""
+    kernel.rs:343-354) and, for k <= 32, the warp-per-query kernel: bit-exact
+    with the oracle."""
     from kdtree import KDTree
 
     rng = np.random.default_rng(1600 + k)
     data = rng.uniform(size=(30_000, 16)) if dist == "uniform" else gmm(30_000, 16, rng)
     q = data[rng.integers(0, 30_000, 1500)] + 0.02 * rng.standard_normal((1500, 16))
     t = KDTree(data, leafsize=16)
-    got = _path_query(t, q, k, p, 2)  # KD_PATH_PACKET
     o = oracle.OracleKDTree(data, leafsize=16).query(q, k=k, p=p, parallel=True)
-    assert_bit_exact(got, o)
+    assert_bit_exact(_path_query(t, q, k, p, 2), o)  # KD_PATH_PACKET
+    if k <= 32:
+        assert_bit_exact(_path_query(t, q, k, p, 4), o)  # KD_PATH_WARP
+
+
+@pytest.mark.parametrize("d", [2, 3, 8])
+@pytest.mark.parametrize("p", [1.0, 2.0, float("inf")])
+@pytest.mark.parametrize("k", [1, 7, 16, 32])
+def test_warp_per_query(oracle, d, p, k):
+    """The warp-per-query kernel on uniform and clustered data, queries inside
+    and outside the root box, ties on an integer grid."""
+    from kdtree import KDTree
+
+    rng = np.random.default_rng(400 + 10 * d + k)
+    for data, q in ((rng.uniform(size=(40_000, d)), rng.uniform(size=(2000, d)) * 1.2 - 0.1),
+                    (gmm(40_000, d, rng), gmm(2000, d, rng)),
+                    (rng.integers(0, 4, size=(5000, d)).astype(float), rng.integers(0, 4, size=(500, d)).astype(float))):
+        t = KDTree(data, leafsize=16)
+        o = oracle.OracleKDTree(data, leafsize=16).query(q, k=k, p=p, parallel=True)
+        assert_bit_exact(_path_query(t, q, k, p, 4), o)

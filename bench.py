@@ -150,12 +150,16 @@ def measured_peak():
 
 
 def profiled_traffic():
-    p = ROOT / "profiles" / "roofline_traffic.json"
+    """DRAM bytes (read + write) of one launch of the query kernel on this
+    workload, from the committed ncu summary (`traffic_bytes_per_launch: N`)."""
+    p = ROOT / "profiles" / "k_query_packet_uniform_n1m_d3_k16.md"
     if p.exists():
-        try:
-            return json.loads(p.read_text()).get("query_kernel_dram_bytes_per_launch")
-        except Exception:
-            return None
+        for line in p.read_text().splitlines():
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                try:
+                    return int(line.split(":", 1)[1].strip().split()[0])
+                except ValueError:
+                    return None
     return None
 
 
@@ -669,6 +673,8 @@ def main():
     torch.cuda.synchronize()
     events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     sampler = ClockSampler(local)
+    lib.kd_last_query_kernel_ms.restype = ctypes.c_double
+    kernel_ms = []
     with sampler:
         t_wall0 = time.perf_counter()
         with torch.cuda.stream(stream):
@@ -677,6 +683,7 @@ def main():
                 e0.record(stream)
                 step()
                 e1.record(stream)
+                kernel_ms.append(lib.kd_last_query_kernel_ms())  # step() returned: its kernel is done
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall0
     if ws > 1:
@@ -737,7 +744,9 @@ def main():
     roofline = None
     if counts:
         per_launch = algorithmic_bytes(counts, N_QUERIES)
-        mean_s = total_s / args.steps
+        # the query kernel's own device time (CUDA events the library records on
+        # the launching stream around it), averaged over the timed steps
+        mean_s = (sum(kernel_ms) / len(kernel_ms) / 1e3) if min(kernel_ms) > 0 else total_s / args.steps
         achieved = per_launch / mean_s / 1e9
         traffic = profiled_traffic()
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -745,7 +754,8 @@ def main():
                     "algorithmic_bytes_per_launch": per_launch,
                     "per_query": {"nodes_visited": counts[0] / N_QUERIES, "rows_scanned": counts[1] / N_QUERIES,
                                   "boxes_evaluated": counts[2] / N_QUERIES},
-                    "kernel": "k_query<L2, d=3, K=16>"}
+                    "kernel": "k_query_packet<L2, d=3, K=16>", "kernel_ms": mean_s * 1e3,
+                    "traffic_note": "DRAM read+write bytes per launch from ncu (profiles/)"}
     line = {
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,

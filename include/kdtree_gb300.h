@@ -97,7 +97,7 @@ int kd_query_device(const kd_tree* tree, const double* d_queries, uint64_t n_val
  *                           (L2, eps = 0, 16 <= d <= 128, k <= 32)
  *   KD_PATH_WARP            one warp per query, rows and dimensions split
  *                           across the lanes (d in {2, 3, 8, 16}, eps = 0,
- *                           k <= 32): for queries that scan many leaf rows
+ *                           k <= 64): for queries that scan many leaf rows
  * A path that does not apply to a call falls back to the reference order. */
 enum kd_query_path {
   KD_PATH_AUTO = 0,
@@ -219,6 +219,12 @@ int kd_server_wait(kd_server* server, uint64_t ticket, double* latency_s);
 
 /* Finish every queued request, stop the threads, release everything. */
 void kd_server_free(kd_server* server);
+
+/* Device time in milliseconds of the last query kernel this thread launched
+ * (the traversal or the tensor-core filter; the sort and set-up kernels
+ * around it excluded), from CUDA events recorded on its stream; -1 when there
+ * is none.  No reference counterpart: a measurement aid. */
+double kd_last_query_kernel_ms(void);
 
 /* Getters: `Tree::ndim`, `Tree::n_points`, `Tree::leafsize`
  * (src/tree.rs:48-58).  kd_n_nodes has no Python getter in the reference. */

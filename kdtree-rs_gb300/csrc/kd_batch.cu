@@ -14,7 +14,7 @@
 //     one by one with the warp-per-query traversal (kd_query_warp.cuh) for the
 //     job's width.  Jobs are laid out widest (most expensive) first, so the
 //     long tasks start early and the short ones fill the tail;
-//  3. jobs outside the fused kernel's envelope (general L^p, eps > 0, k > 32,
+//  3. jobs outside the fused kernel's envelope (general L^p, eps > 0, k > 64,
 //     widths other than 2, 3, 8 and 16, the reference-order switch) run as
 //     ordinary per-job launches of the kernels kd_query_device uses, on side
 //     streams beside the fused kernel -- the packet traversal for k <= 64,
@@ -57,15 +57,17 @@ constexpr uint32_t CLS_OTHER = 0xffffffffu;
 constexpr uint64_t SORT_MIN_QUERIES = 1024;
 constexpr uint32_t TASK_QUERIES = 4;  // queries per task: one after another on one warp
 
-// Class of a job in the fused kernel (its width index), or CLS_OTHER.
+// Class of a job in the fused kernel (width index, + 4 for k > 32: two list
+// slots per lane), or CLS_OTHER.
 uint32_t fused_class(const kd_tree* t, const QueryParams& qp, uint64_t k, bool reference_order) {
-  if (qp.metric == M_LP || qp.eps_factor != 1.0 || k > 32 || t->n_points >= ROW_NONE || reference_order)
+  if (qp.metric == M_LP || qp.eps_factor != 1.0 || k > 64 || t->n_points >= ROW_NONE || reference_order)
     return CLS_OTHER;
+  const uint32_t wide = k > 32 ? 4 : 0;
   switch (t->ndim) {
-    case 2: return 0;
-    case 3: return 1;
-    case 8: return 2;
-    case 16: return 3;
+    case 2: return 0 + wide;
+    case 3: return 1 + wide;
+    case 8: return 2 + wide;
+    case 16: return 3 + wide;
     default: return CLS_OTHER;
   }
 }
@@ -135,9 +137,9 @@ __global__ void k_batch_scatter(const uint32_t* q_start, uint32_t n_jobs, uint32
   order[atomicAdd(&bins[bin_of[g]], 1u)] = g - q_start[j];
 }
 
-template <int M, int D>
+template <int M, int D, int KS>
 __device__ __forceinline__ void batch_query(const QArgs* a, uint64_t w, uint32_t* stack_n, float* stack_lb) {
-  warp_query<M, D>(*a, w, stack_n, stack_lb);
+  warp_query<M, D, KS>(*a, w, stack_n, stack_lb);
 }
 
 // The persistent kernel: warps take tasks -- TASK_QUERIES consecutive
@@ -159,10 +161,14 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query_batch(BatchArgs b) {
     const uint64_t last = min(first + TASK_QUERIES, J->a.nq);
     for (uint64_t w = first; w < last; ++w) {
       switch (J->cls) {
-        case 0: batch_query<M, 2>(&J->a, w, s_node[wid], s_lb[wid]); break;
-        case 1: batch_query<M, 3>(&J->a, w, s_node[wid], s_lb[wid]); break;
-        case 2: batch_query<M, 8>(&J->a, w, s_node[wid], s_lb[wid]); break;
-        default: batch_query<M, 16>(&J->a, w, s_node[wid], s_lb[wid]); break;
+        case 0: batch_query<M, 2, 1>(&J->a, w, s_node[wid], s_lb[wid]); break;
+        case 1: batch_query<M, 3, 1>(&J->a, w, s_node[wid], s_lb[wid]); break;
+        case 2: batch_query<M, 8, 1>(&J->a, w, s_node[wid], s_lb[wid]); break;
+        case 3: batch_query<M, 16, 1>(&J->a, w, s_node[wid], s_lb[wid]); break;
+        case 4: batch_query<M, 2, 2>(&J->a, w, s_node[wid], s_lb[wid]); break;
+        case 5: batch_query<M, 3, 2>(&J->a, w, s_node[wid], s_lb[wid]); break;
+        case 6: batch_query<M, 8, 2>(&J->a, w, s_node[wid], s_lb[wid]); break;
+        default: batch_query<M, 16, 2>(&J->a, w, s_node[wid], s_lb[wid]); break;
       }
     }
   }
@@ -243,7 +249,7 @@ void make_layout(const std::vector<JobSpec>& specs, const QueryParams& qp, bool 
   }
   // most expensive first: wider points, then larger k
   std::stable_sort(L->packet.begin(), L->packet.end(), [&](uint32_t x, uint32_t y) {
-    if (cls[x] != cls[y]) return cls[x] > cls[y];
+    if (cls[x] % 4 != cls[y] % 4) return cls[x] % 4 > cls[y] % 4;
     return specs[x].k > specs[y].k;
   });
   const size_t n = L->packet.size();

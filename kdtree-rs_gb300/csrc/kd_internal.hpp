@@ -142,7 +142,7 @@ void order_by_landing_leaf(const kd_tree* t, const double* d_queries, uint64_t n
 // L-inf, widths 2, 3, 8, 16): whether it covers a query, and its launch.
 bool packet_applicable(uint64_t d, int metric, uint64_t k, uint64_t n_points, bool use_eps);
 int launch_packet_query(const QArgs& a, int metric, cudaStream_t stream);
-// One warp per query (the same envelope with k <= 32): for trees whose queries
+// One warp per query (the same envelope, k <= 64): for trees whose queries
 // scan many leaf rows.
 bool warp_applicable(uint64_t d, int metric, uint64_t k, uint64_t n_points, bool use_eps);
 int launch_warp_query(const QArgs& a, int metric, cudaStream_t stream);

@@ -518,7 +518,50 @@ bool warp_preferred(const QArgs& a) {
   return a.d >= 8 || a.k > 16 || (a.k >= 8 && a.nq < 400000);
 }
 
+// Events around the last query kernel launched by this thread (not while the
+// stream is being captured), read by kd_last_query_kernel_ms.
+struct KernelClock {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int dev = -1;
+  bool valid = false;
+};
+KernelClock& kernel_clock() {
+  thread_local KernelClock c;
+  return c;
+}
+
+struct KernelTimer {
+  cudaStream_t st;
+  bool on = false;
+  explicit KernelTimer(cudaStream_t s) : st(s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+      cudaGetLastError();
+      return;
+    }
+    KernelClock& c = kernel_clock();
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (c.dev != dev) {
+      if (c.e0) cudaEventDestroy(c.e0);
+      if (c.e1) cudaEventDestroy(c.e1);
+      c.e0 = c.e1 = nullptr;
+      if (cudaEventCreate(&c.e0) != cudaSuccess || cudaEventCreate(&c.e1) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+      }
+      c.dev = dev;
+    }
+    on = cudaEventRecord(c.e0, st) == cudaSuccess;
+  }
+  ~KernelTimer() {
+    KernelClock& c = kernel_clock();
+    c.valid = on && cudaEventRecord(c.e1, st) == cudaSuccess;
+  }
+};
+
 int run_kernels(const QArgs& a, int metric, cudaStream_t st, int path) {
+  KernelTimer timer(st);
   if (!a.reference_order && !force_reference_order()) {
     if ((path == PATH_WARP || (path == PATH_AUTO && warp_preferred(a))) &&
         warp_applicable(a.d, metric, a.k, a.n_points, a.use_eps != 0))
@@ -603,9 +646,11 @@ int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, cons
       int rc = auto_prefers_tc(const_cast<kd_tree*>(t), d_queries, nq, qp, d_out_d, d_out_i, st, d_status, &tc);
       if (rc) return rc;
     }
-    if (tc)
+    if (tc) {
+      KernelTimer timer(st);
       return query_tc_on_device(const_cast<kd_tree*>(t), d_queries, nq, qp, d_out_d, d_out_i, st, d_status,
                                 d_survivors);
+    }
   }
   QArgs a{};
   a.reference_order = qp.path == PATH_REFERENCE_ORDER;
@@ -686,3 +731,14 @@ int query_on_device_scratch(const kd_tree* t, const double* d_queries, uint64_t 
 }
 
 }  // namespace kd
+
+extern "C" double kd_last_query_kernel_ms(void) {
+  kd::KernelClock& c = kd::kernel_clock();
+  if (!c.valid) return -1.0;
+  float ms = 0.f;
+  if (cudaEventSynchronize(c.e1) != cudaSuccess || cudaEventElapsedTime(&ms, c.e0, c.e1) != cudaSuccess) {
+    cudaGetLastError();
+    return -1.0;
+  }
+  return ms;
+}

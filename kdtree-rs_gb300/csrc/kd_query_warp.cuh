@@ -1,4 +1,4 @@
-// kd_query_warp.cuh -- exact k-NN with one warp per query (eps = 0, k <= 32,
+// kd_query_warp.cuh -- exact k-NN with one warp per query (eps = 0, k <= 64,
 // L1 / L2 / L-inf, compile-time widths 2, 3, 8, 16).  Included by
 // kd_query_packet.cu.
 //
@@ -8,10 +8,11 @@
 // walks the union of 32 queries' leaves.  Here the 32 lanes work on ONE query:
 // every leaf's rows are split across the lanes (row r + lane), every box's
 // dimensions too (lane i takes dimension i), and the k best (exact FP64 reduced
-// distance bits, original index) live one per lane, sorted, lane j holding the
-// j-th.  The traversal is best-first at each node (the child with the smaller
-// box bound first) and prunes a subtree whose rigorous FP32 lower bound exceeds
-// the FP32 upper enclosure of the exact bound min(k-th best, cutoff).
+// distance bits, original index) live one or two per lane, sorted, lane j
+// holding the j-th (and the (32 + j)-th).  The traversal is best-first at each
+// node (the child with the smaller box bound first) and prunes a subtree whose
+// rigorous FP32 lower bound exceeds the FP32 upper enclosure of the exact bound
+// min(k-th best, cutoff).
 //
 // Candidate points pass the same rigorous FP32 filter as the packet traversal
 // (PointFilter), get their exact FP64 distance in the reference's summation
@@ -61,11 +62,13 @@ __device__ __forceinline__ uint64_t shfl_up_u64(uint64_t v) {
   return (static_cast<uint64_t>(hi) << 32) | lo;
 }
 
-// The warp's sorted k best: lane j < k holds the j-th (key = exact distance
-// bits, id = original index); EMPTY_KEY sorts after everything.
+// The warp's sorted k best, KS slots per lane (k <= 32 KS): rank r lives in
+// lane r % 32, slot r / 32 (key = exact distance bits, id = original index);
+// EMPTY_KEY sorts after everything.
+template <int KS>
 struct WarpList {
-  uint64_t key = EMPTY_KEY;
-  uint32_t id = NO_ID;
+  uint64_t key[KS];
+  uint32_t id[KS];
   uint32_t k;
   uint32_t lane;
   uint64_t cut_bits;
@@ -73,34 +76,68 @@ struct WarpList {
   float bound32;        // an FP32 upper enclosure of it
 
   __device__ __forceinline__ void init(uint32_t k_, double cutoff, uint32_t lane_) {
+#pragma unroll
+    for (int s = 0; s < KS; ++s) {
+      key[s] = EMPTY_KEY;
+      id[s] = NO_ID;
+    }
     k = k_;
     lane = lane_;
     cut_bits = dbits(cutoff);
     refresh();
   }
   __device__ __forceinline__ void refresh() {
-    const uint64_t kth = shfl_u64(key, static_cast<int>(k - 1));
+    const uint32_t r = k - 1;
+    uint64_t kth = shfl_u64(key[0], static_cast<int>(r & 31));
+    if (KS > 1) {
+      const uint64_t k1 = shfl_u64(key[KS - 1], static_cast<int>(r & 31));
+      if (r >= 32) kth = k1;
+    }
     bound_bits = kth < cut_bits ? kth : cut_bits;
     bound32 = mag_up32(bound_bits);
   }
   // Insert candidate (cb, cid) if it is among the k smallest; warp-uniform.
   __device__ __forceinline__ void insert(uint64_t cb, uint32_t cid) {
-    const bool before = lane < k && (key < cb || (key == cb && id < cid));
-    const uint32_t pos = __popc(__ballot_sync(FULL_MASK, before));
+    uint32_t pos = 0;
+#pragma unroll
+    for (int s = 0; s < KS; ++s) {
+      const uint32_t r = lane + 32u * s;
+      const bool before = r < k && (key[s] < cb || (key[s] == cb && id[s] < cid));
+      pos += __popc(__ballot_sync(FULL_MASK, before));
+    }
     if (pos >= k) return;  // uniform
-    const uint64_t up_key = shfl_up_u64(key);
-    const uint32_t up_id = __shfl_up_sync(FULL_MASK, id, 1);
-    if (lane > pos && lane < k) {
-      key = up_key;
-      id = up_id;
-    } else if (lane == pos) {
-      key = cb;
-      id = cid;
+    // ranks above pos move up by one: from the lane below, or (lane 0 of
+    // slot 1) from lane 31 of slot 0
+    uint64_t up_key[KS];
+    uint32_t up_id[KS];
+#pragma unroll
+    for (int s = 0; s < KS; ++s) {
+      up_key[s] = shfl_up_u64(key[s]);
+      up_id[s] = __shfl_up_sync(FULL_MASK, id[s], 1);
+    }
+    if (KS > 1) {
+      const uint64_t wrap_key = shfl_u64(key[0], 31);
+      const uint32_t wrap_id = __shfl_sync(FULL_MASK, id[0], 31);
+      if (lane == 0) {
+        up_key[KS - 1] = wrap_key;
+        up_id[KS - 1] = wrap_id;
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < KS; ++s) {
+      const uint32_t r = lane + 32u * s;
+      if (r > pos && r < k) {
+        key[s] = up_key[s];
+        id[s] = up_id[s];
+      } else if (r == pos) {
+        key[s] = cb;
+        id[s] = cid;
+      }
     }
   }
 };
 
-template <int M, int D>
+template <int M, int D, int KS>
 __device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, uint32_t* stack_n, float* stack_lb) {
   static_assert(D > 0 && M != M_LP, "warp path: compile-time width, metric without pow()");
   const uint32_t lane = threadIdx.x & 31;
@@ -125,7 +162,7 @@ __device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, uint32_t*
   for (int i = 0; i < D; ++i)
     if (lane == static_cast<uint32_t>(i)) rn_enclose(filt.q32[i], &my_qlo, &my_qhi);
 
-  WarpList best;
+  WarpList<KS> best;
   best.init(static_cast<uint32_t>(a.k), a.cutoff, lane);
   float thr = filt.threshold(best.bound32);
 
@@ -196,19 +233,23 @@ __device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, uint32_t*
       }
     }
   }
-  if (lane < a.k) {
-    const bool real = best.key != EMPTY_KEY;
-    a.out_d[qi * a.k + lane] = real ? restore<M>(bitsd(best.key), 0.0) : bitsd(INF_BITS);
-    a.out_i[qi * a.k + lane] = real ? static_cast<int64_t>(best.id) : static_cast<int64_t>(a.n_points);
+#pragma unroll
+  for (int s = 0; s < KS; ++s) {
+    const uint32_t r = lane + 32u * s;
+    if (r < a.k) {
+      const bool real = best.key[s] != EMPTY_KEY;
+      a.out_d[qi * a.k + r] = real ? restore<M>(bitsd(best.key[s]), 0.0) : bitsd(INF_BITS);
+      a.out_i[qi * a.k + r] = real ? static_cast<int64_t>(best.id[s]) : static_cast<int64_t>(a.n_points);
+    }
   }
 }
 
 // One warp per query; the block's warps keep their stacks in shared memory
 // (every lane writes the same entry and reads back what it wrote).
-template <int M, int D>
+template <int M, int D, int KS>
 __global__ void __launch_bounds__(QUERY_THREADS) k_query_warp(QArgs a) {
   __shared__ uint32_t s_node[QUERY_THREADS / 32][WARP_STACK];
   __shared__ float s_lb[QUERY_THREADS / 32][WARP_STACK];
   const uint32_t wid = threadIdx.x >> 5;
-  warp_query<M, D>(a, blockIdx.x * static_cast<uint64_t>(QUERY_THREADS / 32) + wid, s_node[wid], s_lb[wid]);
+  warp_query<M, D, KS>(a, blockIdx.x * static_cast<uint64_t>(QUERY_THREADS / 32) + wid, s_node[wid], s_lb[wid]);
 }

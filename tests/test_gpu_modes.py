@@ -101,13 +101,12 @@ def test_packet_width16(oracle, p, dist, k):
     t = KDTree(data, leafsize=16)
     o = oracle.OracleKDTree(data, leafsize=16).query(q, k=k, p=p, parallel=True)
     assert_bit_exact(_path_query(t, q, k, p, 2), o)  # KD_PATH_PACKET
-    if k <= 32:
-        assert_bit_exact(_path_query(t, q, k, p, 4), o)  # KD_PATH_WARP
+    assert_bit_exact(_path_query(t, q, k, p, 4), o)  # KD_PATH_WARP
 
 
 @pytest.mark.parametrize("d", [2, 3, 8])
 @pytest.mark.parametrize("p", [1.0, 2.0, float("inf")])
-@pytest.mark.parametrize("k", [1, 7, 16, 32])
+@pytest.mark.parametrize("k", [1, 7, 16, 32, 33, 64])
 def test_warp_per_query(oracle, d, p, k):
     """The warp-per-query kernel on uniform and clustered data, queries inside
     and outside the root box, ties on an integer grid."""

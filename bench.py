@@ -368,9 +368,10 @@ def serving_case(torch, duration_s=2.0, n_templates=256):
     64-component Gaussian mixture (centres uniform in [0,1)^d, sigma 0.01),
     leafsize 32; requests: tree uniform, Q log-uniform in [1, 1e5] queries from
     the tree's mixture, k log-uniform in [1, 64] rounded, L2; seed 500.  Served
-    by kdtree.Server (continuous batching).  Peak load: a burst of all request
-    templates; then Poisson arrivals at 50/70/90% of that rate for duration_s
-    each: p50/p99 latency (submission to completion) and sustained queries/s."""
+    by kdtree.Server (continuous batching).  Peak load: a closed loop keeping 64
+    requests in flight for duration_s; then Poisson arrivals at 50/70/90% of that
+    rate for duration_s each: p50/p99 latency (submission to completion) and
+    sustained queries/s."""
     import threading
 
     from kdtree import KDTree, Server
@@ -408,31 +409,15 @@ def serving_case(torch, duration_s=2.0, n_templates=256):
     for ti, q, k, od, oi in templates[:3]:
         d_, i_ = trees[ti].query(q, k=k)
         identical &= bool(np.array_equal(d_.view(np.int64), od.view(np.int64)) and np.array_equal(i_, oi))
-    # peak: everything at once
-    best = None
-    for _ in range(2):
-        t0 = time.perf_counter()
-        tickets = [srv.submit(ti, q, k, out=(od, oi)) for ti, q, k, od, oi in templates]
-        for tk in tickets:
-            srv.wait(tk)
-        el = time.perf_counter() - t0
-        best = el if best is None else min(best, el)
     total_q = sum(t[1].shape[0] for t in templates)
-    peak_rps = n_templates / best
-    out = {"trees": n_trees, "points": int(ns.sum()), "build_all_s": build_s, "templates": n_templates,
-           "identical_to_lone_queries": identical,
-           "peak": {"requests_per_s": peak_rps, "queries_per_s": total_q / best}}
-    for frac in (0.5, 0.7, 0.9):
-        rate = frac * peak_rps
-        gaps = rng.exponential(1.0 / rate, int(rate * duration_s) + 1)
-        order = rng.integers(0, n_templates, len(gaps))
+
+    def run_load(rate, duration, window=None):
+        """Submit requests at Poisson times (rate/s, for `duration` s), or -- with
+        `window` -- keep that many in flight as fast as the server allows, until
+        `duration` s have passed; return (latencies, queries done, elapsed)."""
         busy = [False] * n_templates
-        lock = threading.Lock()
-        pending = []
-        lat = []
-        done_q = [0]
-        cv = threading.Condition(lock)
-        finished = [False]
+        cv = threading.Condition()
+        pending, lat, done_q, finished = [], [], [0], [False]
 
         def waiter():
             while True:
@@ -447,35 +432,57 @@ def serving_case(torch, duration_s=2.0, n_templates=256):
                     busy[j] = False
                     lat.append(l)
                     done_q[0] += templates[j][1].shape[0]
+                    cv.notify_all()
 
         th = threading.Thread(target=waiter)
         th.start()
         t_start = time.perf_counter()
         t_next = t_start
-        for g, j in zip(gaps, order):
-            t_next += g
-            while time.perf_counter() < t_next:
-                pass
-            j = int(j)
+        n_sub = 0
+        while True:
+            if window is None:
+                t_next += rng.exponential(1.0 / rate)
+                if t_next - t_start > duration:
+                    break
+                while time.perf_counter() < t_next:
+                    pass
+            elif time.perf_counter() - t_start > duration:
+                break
             with cv:
+                # a template's buffers serve one request at a time; with `window`,
+                # at most that many requests are in flight
+                while all(busy) or (window is not None and sum(busy) >= window):
+                    cv.wait()
+                j = int(rng.integers(0, n_templates))
                 while busy[j]:
                     j = (j + 1) % n_templates
                 busy[j] = True
             ti, q, k, od, oi = templates[j]
             tk = srv.submit(ti, q, k, out=(od, oi))
+            n_sub += 1
             with cv:
                 pending.append((tk, j))
-                cv.notify()
+                cv.notify_all()
         with cv:
             finished[0] = True
-            cv.notify()
+            cv.notify_all()
         th.join()
-        el = time.perf_counter() - t_start
-        lat_ms = np.array(lat) * 1e3
+        return np.array(lat) * 1e3, done_q[0], time.perf_counter() - t_start
+
+    # peak: a closed loop keeping 64 requests in flight for 2 s
+    lat, q_done, el = run_load(None, duration_s, window=64)
+    peak_rps = len(lat) / el
+    out = {"trees": n_trees, "points": int(ns.sum()), "build_all_s": build_s, "templates": n_templates,
+           "mean_queries_per_request": total_q / n_templates, "identical_to_lone_queries": identical,
+           "peak": {"requests_per_s": peak_rps, "queries_per_s": q_done / el, "in_flight": 64,
+                    "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))}}
+    for frac in (0.5, 0.7, 0.9):
+        rate = frac * peak_rps
+        lat, q_done, el = run_load(rate, duration_s)
         out[f"load_{int(frac * 100)}"] = {"offered_requests_per_s": rate, "requests": len(lat),
-                                          "p50_ms": float(np.percentile(lat_ms, 50)),
-                                          "p99_ms": float(np.percentile(lat_ms, 99)),
-                                          "sustained_queries_per_s": done_q[0] / el}
+                                          "p50_ms": float(np.percentile(lat, 50)),
+                                          "p99_ms": float(np.percentile(lat, 99)),
+                                          "sustained_queries_per_s": q_done / el}
     srv.close()
     del trees
     return out
@@ -780,11 +787,16 @@ def main():
         ct = None
         if not args.no_cpu:
             ct = kdtree_oracle.max_threads()
-        line["cases"] = {"plain_scale": plain_scale_cases(lib, torch, stream, dev),
-                         "precision": precision_cases(lib, torch, stream, dev, ct),
-                         "grid": grid_case(lib, torch, stream, dev, ct),
-                         "batched": batched_case(torch, dev, stream),
-                         "serving": serving_case(torch)}
+        cases = {}
+        for name, fn in (("plain_scale", lambda: plain_scale_cases(lib, torch, stream, dev)),
+                         ("precision", lambda: precision_cases(lib, torch, stream, dev, ct)),
+                         ("grid", lambda: grid_case(lib, torch, stream, dev, ct)),
+                         ("batched", lambda: batched_case(torch, dev, stream)),
+                         ("serving", lambda: serving_case(torch))):
+            t0 = time.perf_counter()
+            cases[name] = fn()
+            print(f"[bench] case {name}: {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
+        line["cases"] = cases
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()

@@ -181,6 +181,17 @@ int status_word(uint32_t h) {
   return KD_OK;
 }
 
+// Device-accessible address of page-locked (pinned) host memory, or nullptr
+// for pageable memory.
+void* mapped_host(const void* p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 int query_common(const kd_tree* t, const double* queries, bool on_device, uint64_t n_values, uint64_t k,
                  double p, int has_max, double max_distance, double eps, double* out_d, int64_t* out_i,
                  cudaStream_t st, int path = PATH_AUTO, unsigned long long* d_survivors = nullptr) {
@@ -224,22 +235,28 @@ int query_common(const kd_tree* t, const double* queries, bool on_device, uint64
     KD_TRY_CUDA(cudaStreamSynchronize(st));
     return status_word(h);
   }
-  // Host buffers: device staging for the queries and the results.
+  // Host buffers: the queries are uploaded.  Page-locked outputs that the
+  // chosen kernel writes as whole rows receive the results directly over the
+  // host link while the kernel runs (the transfer overlaps the compute);
+  // otherwise the results are staged in device memory and downloaded.
   DevMem mq, md, mi;
-  if ((rc = mq.alloc(n_values * sizeof(double), st)) || (rc = md.alloc(nq * k * sizeof(double), st)) ||
-      (rc = mi.alloc(nq * k * sizeof(int64_t), st)))
-    return rc;
+  if ((rc = mq.alloc(n_values * sizeof(double), st))) return rc;
   double* dq = static_cast<double*>(mq.p);
-  double* dd = static_cast<double*>(md.p);
-  int64_t* di = static_cast<int64_t*>(mi.p);
   uint32_t* ds = static_cast<uint32_t*>(status.p);
-  // One batch: splitting it into concurrent pieces to overlap the download
-  // measured slower (each piece sorts fewer queries, so its warps are less
-  // coherent), and so did kernels writing page-locked outputs directly.
+  double* dd = static_cast<double*>(mapped_host(out_d));
+  int64_t* di = static_cast<int64_t*>(mapped_host(out_i));
+  const bool direct = dd && di && writes_whole_rows(t, qp);
+  if (!direct) {
+    if ((rc = md.alloc(nq * k * sizeof(double), st)) || (rc = mi.alloc(nq * k * sizeof(int64_t), st))) return rc;
+    dd = static_cast<double*>(md.p);
+    di = static_cast<int64_t*>(mi.p);
+  }
   KD_TRY_CUDA(cudaMemcpyAsync(dq, queries, n_values * sizeof(double), cudaMemcpyHostToDevice, st));
   if ((rc = query_on_device(t, dq, nq, qp, dd, di, st, ds, d_survivors))) return rc;
-  KD_TRY_CUDA(cudaMemcpyAsync(out_d, dd, nq * k * sizeof(double), cudaMemcpyDeviceToHost, st));
-  KD_TRY_CUDA(cudaMemcpyAsync(out_i, di, nq * k * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  if (!direct) {
+    KD_TRY_CUDA(cudaMemcpyAsync(out_d, dd, nq * k * sizeof(double), cudaMemcpyDeviceToHost, st));
+    KD_TRY_CUDA(cudaMemcpyAsync(out_i, di, nq * k * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  }
   uint32_t h = 0;
   KD_TRY_CUDA(cudaMemcpyAsync(&h, status.p, sizeof h, cudaMemcpyDeviceToHost, st));
   KD_TRY_CUDA(cudaStreamSynchronize(st));

@@ -131,6 +131,11 @@ int query_on_device_scratch(const kd_tree* t, const double* d_queries, uint64_t 
                             const QueryParams& qp, double* d_out_d, int64_t* d_out_i,
                             cudaStream_t stream, uint32_t* d_status, double* d_axes_scratch);
 
+// Whether the query kernels that query_on_device would run for these
+// parameters write each query's result row as whole contiguous segments (so
+// results may go straight to page-locked host memory over the host link).
+bool writes_whole_rows(const kd_tree* t, const QueryParams& qp);
+
 // Sort a batch by landing leaf (the leaf each query's descent reaches first):
 // leaf_of[i] = that leaf's node id, order = query indices grouped by leaf in
 // preorder.  `scratch` holds order_scratch_words(t) u32.  Work on `stream`.

@@ -600,7 +600,8 @@ struct LazyHeap {
       j = c;
     }
   }
-  __device__ __forceinline__ void write(double* od, int64_t* oi, uint64_t k_, uint64_t n_points) {
+  // Exact keys in place, heap-sorted ascending (one lane's own column).
+  __device__ __forceinline__ void sort_exact() {
     for (uint32_t j = 0; j < n; ++j) {
       const uint32_t rj = row[j * S];
       const uint64_t xb = dbits(exact_of(rj, chunk_of(lo[j * S])));
@@ -613,13 +614,34 @@ struct LazyHeap {
       swap_slots(0, m - 1);
       sift_exact(0, m - 1);
     }
-    for (uint32_t j = 0; j < k_; ++j) {
-      if (j < n) {
-        od[j] = restore<M>(bitsd(key_at(j)), 0.0);
-        oi[j] = static_cast<int64_t>(row[j * S]);
-      } else {
-        od[j] = bitsd(INF_BITS);
-        oi[j] = static_cast<int64_t>(n_points);
+  }
+  // The whole warp writes its lanes' results, one query row at a time, lane j
+  // storing element j: every row of distances (and of indices) goes out as
+  // whole contiguous segments.  Every lane of the warp calls it; `live` says
+  // whether this lane has a query whose results to write (sorted already).
+  __device__ __forceinline__ void write_warp(bool live, double* od, int64_t* oi, uint64_t k_, uint64_t n_points) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t live_mask = __ballot_sync(0xffffffffu, live);
+    __syncwarp();
+    const uint32_t col0 = threadIdx.x - lane;  // this warp's first heap column
+    for (uint32_t m = live_mask; m; m &= m - 1) {
+      const uint32_t r = __ffs(m) - 1;
+      double* od_r = reinterpret_cast<double*>(__shfl_sync(0xffffffffu, reinterpret_cast<uintptr_t>(od), r));
+      int64_t* oi_r = reinterpret_cast<int64_t*>(__shfl_sync(0xffffffffu, reinterpret_cast<uintptr_t>(oi), r));
+      const uint32_t n_r = __shfl_sync(0xffffffffu, n, r);
+      const float* lo_r = lo - threadIdx.x + col0 + r;
+      const float* hi_r = hi - threadIdx.x + col0 + r;
+      const uint32_t* row_r = row - threadIdx.x + col0 + r;
+      for (uint32_t j = lane; j < k_; j += 32) {
+        if (j < n_r) {
+          const uint64_t key =
+              (static_cast<uint64_t>(__float_as_uint(hi_r[j * S])) << 32) | __float_as_uint(lo_r[j * S]);
+          od_r[j] = restore<M>(bitsd(key), 0.0);
+          oi_r[j] = static_cast<int64_t>(row_r[j * S]);
+        } else {
+          od_r[j] = bitsd(INF_BITS);
+          oi_r[j] = static_cast<int64_t>(n_points);
+        }
       }
     }
   }

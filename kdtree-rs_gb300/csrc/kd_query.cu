@@ -578,6 +578,13 @@ int run_kernels(const QArgs& a, int metric, cudaStream_t st, int path) {
 
 }  // namespace
 
+bool writes_whole_rows(const kd_tree* t, const QueryParams& qp) {
+  if (qp.path == PATH_REFERENCE_ORDER || qp.path == PATH_TENSOR_CORE || force_reference_order()) return false;
+  if (qp.path == PATH_AUTO && tc_applicable(t, qp)) return false;  // may run the tensor-core filter
+  if (!packet_applicable(t->ndim, qp.metric, qp.k, t->n_points, qp.eps_factor != 1.0)) return false;
+  return qp.k >= 5;  // the packet traversal's heaps (k >= 5) and the warp path write rows whole
+}
+
 uint64_t order_scratch_words(const kd_tree* t) {
   return t->n_nodes + (t->n_nodes + SCAN_TILE - 1) / SCAN_TILE;
 }

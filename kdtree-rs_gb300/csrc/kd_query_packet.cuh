@@ -231,7 +231,12 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
     stack[sp++] = left_first ? nd.right : node + 1;
     stack[sp++] = left_first ? node + 1 : nd.right;
   }
-  if (live) best.write(a.out_d + qi * a.k, a.out_i + qi * a.k, a.k, a.n_points);
+  if constexpr (K >= 8) {
+    if (live) best.sort_exact();
+    best.write_warp(live, a.out_d + qi * a.k, a.out_i + qi * a.k, a.k, a.n_points);
+  } else {
+    if (live) best.write(a.out_d + qi * a.k, a.out_i + qi * a.k, a.k, a.n_points);
+  }
 }
 
 template <int M, int D, int K>

@@ -15,9 +15,10 @@
 // min(k-th best, cutoff).
 //
 // Candidate points pass the same rigorous FP32 filter as the packet traversal
-// (PointFilter), get their exact FP64 distance in the reference's summation
-// order, and enter the list by (distance, index) -- BestK's order
-// (query.rs:461-481).  The result is therefore the k smallest (exact distance,
+// (PointFilter) and enter the list by their exact (distance, index) order --
+// BestK's (query.rs:461-481) -- decided on FP32 enclosures of the exact FP64
+// distance in the reference's summation order, with the exact value computed
+// only when enclosures overlap (GB300 runs FP64 at 1/58 of the FP32 rate).  The result is therefore the k smallest (exact distance,
 // index) among the points within max_distance, as for the packet traversal.
 #pragma once
 
@@ -63,75 +64,151 @@ __device__ __forceinline__ uint64_t shfl_up_u64(uint64_t v) {
 }
 
 // The warp's sorted k best, KS slots per lane (k <= 32 KS): rank r lives in
-// lane r % 32, slot r / 32 (key = exact distance bits, id = original index);
-// EMPTY_KEY sorts after everything.
-template <int KS>
-struct WarpList {
-  uint64_t key[KS];
-  uint32_t id[KS];
-  uint32_t k;
-  uint32_t lane;
+// lane r % 32, slot r / 32.  Like the packet traversal's heap, an entry keeps
+// an FP32 enclosure [lo, hi] of its exact FP64 distance (a one-point enclosure
+// once that is known), its tree row and original index; entries are in exact
+// (distance, index) order.  A candidate's rank comes from enclosure
+// comparisons; only entries whose enclosure overlaps the candidate's compute
+// exact values (one lane each, in parallel), and the candidate's own exact
+// value is computed then too.  Empty slots: row ROW_NONE, after everything.
+template <int M, int D, int KS>
+struct WarpLazyList {
+  float lo[KS], hi[KS];
+  uint32_t row[KS], id[KS];
+  bool chunk[KS];  // the point lies in a full Packed d8 chunk (kernel.rs:540-562)
+  uint32_t k, lane;
   uint64_t cut_bits;
-  uint64_t bound_bits;  // min(k-th key, cutoff)
-  float bound32;        // an FP32 upper enclosure of it
+  float cut_lo, cut_hi;
+  float bound32;  // FP32 upper bound of min(k-th best, cutoff)
+  const QVec<D>* q;
+  const double* data;
 
-  __device__ __forceinline__ void init(uint32_t k_, double cutoff, uint32_t lane_) {
+  __device__ __forceinline__ double exact_of(uint32_t r, bool in_chunk) const {
+    return exact_dist<M, D>(*q, data + static_cast<uint64_t>(r) * D, D, S_PACKED, in_chunk, 0.0);
+  }
+  __device__ __forceinline__ void init(uint32_t k_, double cutoff, uint32_t lane_, const QVec<D>* qv,
+                                       const double* data_) {
 #pragma unroll
     for (int s = 0; s < KS; ++s) {
-      key[s] = EMPTY_KEY;
+      lo[s] = hi[s] = __int_as_float(0x7f800000);
+      row[s] = ROW_NONE;
       id[s] = NO_ID;
+      chunk[s] = false;
     }
     k = k_;
     lane = lane_;
     cut_bits = dbits(cutoff);
+    cut_lo = mag_dn32(cut_bits);
+    cut_hi = mag_up32(cut_bits);
+    q = qv;
+    data = data_;
     refresh();
   }
   __device__ __forceinline__ void refresh() {
     const uint32_t r = k - 1;
-    uint64_t kth = shfl_u64(key[0], static_cast<int>(r & 31));
+    float kth = __shfl_sync(FULL_MASK, hi[0], static_cast<int>(r & 31));
     if (KS > 1) {
-      const uint64_t k1 = shfl_u64(key[KS - 1], static_cast<int>(r & 31));
+      const float k1 = __shfl_sync(FULL_MASK, hi[KS - 1], static_cast<int>(r & 31));
       if (r >= 32) kth = k1;
     }
-    bound_bits = kth < cut_bits ? kth : cut_bits;
-    bound32 = mag_up32(bound_bits);
+    bound32 = fminf(kth, cut_hi);
   }
-  // Insert candidate (cb, cid) if it is among the k smallest; warp-uniform.
-  __device__ __forceinline__ void insert(uint64_t cb, uint32_t cid) {
-    uint32_t pos = 0;
+  // Offer the candidate at tree row cr (original index cid) whose exact
+  // distance lies in [cl, ch]; warp-uniform arguments.
+  __device__ __forceinline__ void offer(float cl, float ch, uint32_t cr, uint32_t cid, bool cchunk) {
+    if (cl > bound32) return;
+    uint64_t cx_bits = 0;
+    bool have_x = false;
+    if (!(ch <= cut_lo)) {  // the cutoff test, unless clearly inside
+      if (cl > cut_hi) return;
+      cx_bits = dbits(exact_of(cr, cchunk));
+      have_x = true;
+      if (cx_bits > cut_bits) return;
+    }
+    bool before[KS], amb[KS];
+    bool any_amb = false;
 #pragma unroll
     for (int s = 0; s < KS; ++s) {
       const uint32_t r = lane + 32u * s;
-      const bool before = r < k && (key[s] < cb || (key[s] == cb && id[s] < cid));
-      pos += __popc(__ballot_sync(FULL_MASK, before));
+      const bool valid = r < k && row[s] != ROW_NONE;
+      before[s] = valid && hi[s] < cl;
+      amb[s] = valid && !before[s] && !(lo[s] > ch);
+      any_amb |= amb[s];
     }
-    if (pos >= k) return;  // uniform
-    // ranks above pos move up by one: from the lane below, or (lane 0 of
-    // slot 1) from lane 31 of slot 0
-    uint64_t up_key[KS];
-    uint32_t up_id[KS];
+    if (__any_sync(FULL_MASK, any_amb)) {  // too close to call on enclosures
+      if (!have_x) cx_bits = dbits(exact_of(cr, cchunk));
+#pragma unroll
+      for (int s = 0; s < KS; ++s) {
+        if (amb[s]) {
+          const uint64_t xb = dbits(exact_of(row[s], chunk[s]));
+          lo[s] = mag_dn32(xb);
+          hi[s] = mag_up32(xb);
+          before[s] = xb < cx_bits || (xb == cx_bits && id[s] < cid);
+        }
+      }
+      cl = mag_dn32(cx_bits);
+      ch = mag_up32(cx_bits);
+    }
+    uint32_t pos = 0;
+#pragma unroll
+    for (int s = 0; s < KS; ++s) pos += __popc(__ballot_sync(FULL_MASK, before[s]));
+    if (pos >= k) {
+      refresh();  // enclosures may have tightened
+      return;
+    }
+    float up_lo[KS], up_hi[KS];
+    uint32_t up_row[KS], up_id[KS];
+    bool up_chunk[KS];
 #pragma unroll
     for (int s = 0; s < KS; ++s) {
-      up_key[s] = shfl_up_u64(key[s]);
+      up_lo[s] = __shfl_up_sync(FULL_MASK, lo[s], 1);
+      up_hi[s] = __shfl_up_sync(FULL_MASK, hi[s], 1);
+      up_row[s] = __shfl_up_sync(FULL_MASK, row[s], 1);
       up_id[s] = __shfl_up_sync(FULL_MASK, id[s], 1);
+      up_chunk[s] = __shfl_up_sync(FULL_MASK, static_cast<int>(chunk[s]), 1);
     }
     if (KS > 1) {
-      const uint64_t wrap_key = shfl_u64(key[0], 31);
-      const uint32_t wrap_id = __shfl_sync(FULL_MASK, id[0], 31);
+      const float wl = __shfl_sync(FULL_MASK, lo[0], 31), wh = __shfl_sync(FULL_MASK, hi[0], 31);
+      const uint32_t wr = __shfl_sync(FULL_MASK, row[0], 31), wi = __shfl_sync(FULL_MASK, id[0], 31);
+      const bool wc = __shfl_sync(FULL_MASK, static_cast<int>(chunk[0]), 31);
       if (lane == 0) {
-        up_key[KS - 1] = wrap_key;
-        up_id[KS - 1] = wrap_id;
+        up_lo[KS - 1] = wl;
+        up_hi[KS - 1] = wh;
+        up_row[KS - 1] = wr;
+        up_id[KS - 1] = wi;
+        up_chunk[KS - 1] = wc;
       }
     }
 #pragma unroll
     for (int s = 0; s < KS; ++s) {
       const uint32_t r = lane + 32u * s;
       if (r > pos && r < k) {
-        key[s] = up_key[s];
+        lo[s] = up_lo[s];
+        hi[s] = up_hi[s];
+        row[s] = up_row[s];
         id[s] = up_id[s];
+        chunk[s] = up_chunk[s];
       } else if (r == pos) {
-        key[s] = cb;
+        lo[s] = cl;
+        hi[s] = ch;
+        row[s] = cr;
         id[s] = cid;
+        chunk[s] = cchunk;
+      }
+    }
+    refresh();
+  }
+  // write_results (query.rs:421-429, 483-493): lane j writes rank j (and
+  // 32 + j); the entries are in exact order already, their exact values are
+  // computed once here.
+  __device__ __forceinline__ void write(double* od, int64_t* oi, uint64_t n_points) const {
+#pragma unroll
+    for (int s = 0; s < KS; ++s) {
+      const uint32_t r = lane + 32u * s;
+      if (r < k) {
+        const bool real = row[s] != ROW_NONE;
+        od[r] = real ? restore<M>(exact_of(row[s], chunk[s]), 0.0) : bitsd(INF_BITS);
+        oi[r] = real ? static_cast<int64_t>(id[s]) : static_cast<int64_t>(n_points);
       }
     }
   }
@@ -162,8 +239,8 @@ __device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, uint32_t*
   for (int i = 0; i < D; ++i)
     if (lane == static_cast<uint32_t>(i)) rn_enclose(filt.q32[i], &my_qlo, &my_qhi);
 
-  WarpList<KS> best;
-  best.init(static_cast<uint32_t>(a.k), a.cutoff, lane);
+  WarpLazyList<M, D, KS> best;
+  best.init(static_cast<uint32_t>(a.k), a.cutoff, lane, &q, a.data);
   float thr = filt.threshold(best.bound32);
 
   int sp = 0;
@@ -198,26 +275,24 @@ __device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, uint32_t*
       for (uint32_t c0 = start; c0 < end; c0 += 32) {
         const uint32_t r = c0 + lane;
         bool cand = false;
+        float clo = 0.f, chi = 0.f;
         if (r < end) {
           const float s = filt.sum(a.data32 + static_cast<uint64_t>(r) * D);
-          cand = !(s > thr);
-        }
-        uint64_t xb = EMPTY_KEY;
-        uint32_t xid = NO_ID;
-        if (cand) {
-          xb = dbits(exact_dist<M, D>(q, a.data + static_cast<uint64_t>(r) * D, D, S_PACKED, r < chunk_end, 0.0));
-          xid = a.indices[r];
-          cand = xb <= best.bound_bits;
+          if (!(s > thr)) {
+            filt.enclose(s, &clo, &chi);
+            cand = !(clo > best.bound32);
+          }
         }
         uint32_t mask = __ballot_sync(FULL_MASK, cand);
         if (!mask) continue;
+        const uint32_t my_id = cand ? a.indices[r] : NO_ID;
         while (mask) {
           const int c = __ffs(mask) - 1;
           mask &= mask - 1;
-          const uint64_t cb = shfl_u64(xb, c);
-          const uint32_t cid = __shfl_sync(FULL_MASK, xid, c);
-          if (cb <= best.bound_bits) best.insert(cb, cid);
-          best.refresh();
+          const float cl = __shfl_sync(FULL_MASK, clo, c), ch = __shfl_sync(FULL_MASK, chi, c);
+          const uint32_t cid = __shfl_sync(FULL_MASK, my_id, c);
+          const uint32_t cr = c0 + static_cast<uint32_t>(c);
+          best.offer(cl, ch, cr, cid, cr < chunk_end);
         }
         thr = filt.threshold(best.bound32);
       }
@@ -233,15 +308,7 @@ __device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, uint32_t*
       }
     }
   }
-#pragma unroll
-  for (int s = 0; s < KS; ++s) {
-    const uint32_t r = lane + 32u * s;
-    if (r < a.k) {
-      const bool real = best.key[s] != EMPTY_KEY;
-      a.out_d[qi * a.k + r] = real ? restore<M>(bitsd(best.key[s]), 0.0) : bitsd(INF_BITS);
-      a.out_i[qi * a.k + r] = real ? static_cast<int64_t>(best.id[s]) : static_cast<int64_t>(a.n_points);
-    }
-  }
+  best.write(a.out_d + qi * a.k, a.out_i + qi * a.k, a.n_points);
 }
 
 // One warp per query; the block's warps keep their stacks in shared memory

@@ -65,6 +65,20 @@ def dist_env():
     return ws, rank, local
 
 
+def whole_job_rate(local_s, steps, ws, device):
+    """Queries/s of the whole job: every rank ran N_QUERIES x steps queries;
+    the job took as long as its slowest rank (max over ranks).  Returns
+    (rate, slowest seconds)."""
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+
+        tt = torch.tensor([local_s], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        local_s = float(tt.item())
+    return ws * N_QUERIES * steps / local_s, local_s
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -696,12 +710,7 @@ def main():
     if ws > 1:
         dist.barrier()
     step_ms = [e0.elapsed_time(e1) for e0, e1 in events]
-    total_s = sum(step_ms) / 1e3
-    if ws > 1:
-        tt = torch.tensor([total_s], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_s = float(tt.item())
-    value = ws * N_QUERIES * args.steps / total_s
+    value, total_s = whole_job_rate(sum(step_ms) / 1e3, args.steps, ws, dev)
     clocks = sampler.summary()
 
     # end to end through the C ABI with pinned host buffers
@@ -725,12 +734,7 @@ def main():
         t0 = time.perf_counter()
         e2e_step()
         e2e_times.append(time.perf_counter() - t0)
-    e2e_s = sum(e2e_times)
-    if ws > 1:
-        tt = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
-    e2e_value = ws * N_QUERIES * args.steps / e2e_s
+    e2e_value, e2e_s = whole_job_rate(sum(e2e_times), args.steps, ws, dev)
 
     if rank != 0:
         if ws > 1:

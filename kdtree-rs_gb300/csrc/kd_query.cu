@@ -511,11 +511,12 @@ int dispatch_d(const QArgs& a, cudaStream_t st) {
 // order), else the reference-order kernels.
 // The automatic choice between the two eps = 0 traversals, from measurements on
 // GB300 (uniform and clustered data, N = 1M): one warp per query wins at
-// d >= 8, for k > 16, and for k >= 8 below a few hundred thousand queries (the
-// packet traversal's 32-query warps have long serial chains, which only a
-// large batch hides); the packet traversal wins for small k on big batches.
+// d >= 8, for k > 16, for k >= 8 below a few hundred thousand queries, and for
+// any k on small batches (the packet traversal's 32-query warps have long
+// serial chains, which only a large batch hides); the packet traversal wins for
+// small k on big batches.
 bool warp_preferred(const QArgs& a) {
-  return a.d >= 8 || a.k > 16 || (a.k >= 8 && a.nq < 400000);
+  return a.d >= 8 || a.k > 16 || (a.k >= 8 && a.nq < 400000) || a.nq < 32768;
 }
 
 // Events around the last query kernel launched by this thread (not while the

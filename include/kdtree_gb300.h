@@ -217,7 +217,9 @@ int kd_server_submit(kd_server* server, uint64_t tree, const double* queries, ui
  * submission to the completion of its batch.  Each ticket is waited for once. */
 int kd_server_wait(kd_server* server, uint64_t ticket, double* latency_s);
 
-/* Finish every queued request, stop the threads, release everything. */
+/* Finish every queued request, stop the threads, release everything.  No
+ * other thread may be inside kd_server_submit / kd_server_wait on this server
+ * when it is called; tickets not yet waited for are dropped. */
 void kd_server_free(kd_server* server);
 
 /* Device time in milliseconds of the last query kernel this thread launched

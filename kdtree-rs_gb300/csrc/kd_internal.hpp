@@ -61,6 +61,7 @@ struct QArgs {
   double* axes_scratch;   // nq * d, dynamic-d CellBound (unused for static d)
   uint32_t* status;       // bit 0: non-finite query
   const uint32_t* order;  // optional: thread t runs query order[t] (spatially sorted)
+  const uint32_t* leaf_of;  // optional: landing leaf node of each query (by query index)
   bool reference_order;   // run the reference-order descent even where eps = 0
   uint64_t nq;
   uint64_t d;

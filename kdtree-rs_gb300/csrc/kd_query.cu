@@ -700,6 +700,7 @@ int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, cons
       uint32_t* order = leaf_of + nq;
       order_by_landing_leaf(t, d_queries, nq, leaf_of, order, order + nq, st);
       a.order = order;
+      a.leaf_of = leaf_of;
     } else {
       cudaGetLastError();  // run unordered: same results, less coherence
       sort_mem = nullptr;

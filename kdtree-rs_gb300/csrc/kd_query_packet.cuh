@@ -32,6 +32,16 @@ constexpr int PACKET_STACK = 2 * KD_MAX_DEPTH;
 //   T(b) = (1 + 2^-20) (b + d E) + d 2^-148                (L1),
 //   T(b) = (1 + 2^-20) (b + E) + 2^-148                    (L-inf),
 // all rounded up, proves the exact distance exceeds b.  NaN never rejects.
+// An FP32 upper bound of sqrt(b) from the hardware reciprocal square root:
+// b * rsqrtf(b) is within 3 units in the last place of sqrt(b) (rsqrtf: 2,
+// the product: 1/2), so growing it by 2^-19 and rounding up covers it (a
+// directed-rounding square root is a long instruction sequence).
+__device__ __forceinline__ float sqrt_up(float b) {
+  if (!(b > 0.f)) return 0.f;
+  if (!(b <= 3.4e38f)) return b;  // +inf (or larger than any finite bound)
+  return __fmul_ru(b * rsqrtf(b), 1.0000020f /* 1 + 2^-19 */);
+}
+
 template <int M, int D>
 struct PointFilter {
   float q32[D];
@@ -50,7 +60,7 @@ struct PointFilter {
   __device__ __forceinline__ float threshold(float b) const {
     constexpr float abs_slack = D * 2.9e-45f;
     if (M == M_L2) {
-      const float r = __fadd_ru(__fsqrt_ru(b), spread);
+      const float r = __fadd_ru(sqrt_up(b), spread);
       return __fadd_ru(__fmul_ru(__fmul_ru(r, r), UB_GROW), abs_slack);
     }
     return __fadd_ru(__fmul_ru(__fadd_ru(b, spread), UB_GROW), abs_slack);
@@ -133,6 +143,7 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
   for (int i = 0; i < D; ++i) rn_enclose(__double2float_rn(q.v[i]), &qlo[i], &qhi[i]);
   PointFilter<M, D> filt;
   filt.init(q, a.coord_max);
+  auto row_sum = [&](uint32_t r) { return filt.sum(a.data32 + static_cast<uint64_t>(r) * D); };
 
   // k-best set: a shared-memory heap from K = 8 up, register slots below
   std::conditional_t<(K >= 8), LazyHeap<M, D, K>, LazySet<M, D, K>> best;
@@ -149,21 +160,27 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
   uint32_t own = NO_ID;
   if (live) {
     uint32_t n = 0;
-    DNode nd = a.nodes[0];
-    while (!(nd.meta & KD_NODE_LEAF)) {
-      const uint32_t dim = nd.meta & KD_NODE_DIM_MASK;
-      float qv = filt.q32[0];
-#pragma unroll
-      for (int i = 1; i < D; ++i) qv = (static_cast<uint32_t>(i) == dim) ? filt.q32[i] : qv;
-      n = qv <= __double2float_rn(nd.split) ? n + 1 : nd.right;
+    DNode nd;
+    if (a.leaf_of) {  // the batch sort found it already
+      n = a.leaf_of[qi];
       nd = a.nodes[n];
+    } else {
+      nd = a.nodes[0];
+      while (!(nd.meta & KD_NODE_LEAF)) {
+        const uint32_t dim = nd.meta & KD_NODE_DIM_MASK;
+        float qv = filt.q32[0];
+#pragma unroll
+        for (int i = 1; i < D; ++i) qv = (static_cast<uint32_t>(i) == dim) ? filt.q32[i] : qv;
+        n = qv <= __double2float_rn(nd.split) ? n + 1 : nd.right;
+        nd = a.nodes[n];
+      }
     }
     own = n;
     const uint64_t se = dbits(nd.split);
     const uint32_t start = static_cast<uint32_t>(se), end = static_cast<uint32_t>(se >> 32);
     const uint32_t chunk_end = (D == 8 && M != M_LINF) ? start + (end - start) / 8 * 8 : end;
     for (uint32_t r = start; r < end; ++r) {
-      const float sr = filt.sum(a.data32 + static_cast<uint64_t>(r) * D);
+      const float sr = row_sum(r);
       if (!(sr > thr)) {
         float clo, chi;
         filt.enclose(sr, &clo, &chi);
@@ -198,7 +215,7 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
         // 1. which of these points can this lane's bound admit?
         uint32_t pending = 0;
         for (uint32_t r = c0; r < c1; ++r) {
-          const float s = filt.sum(a.data32 + static_cast<uint64_t>(r) * D);
+          const float s = row_sum(r);
           if (take && !(s > thr)) pending |= 1u << (r - c0);
         }
         // 2. offer them, all lanes with a pending point together
@@ -206,7 +223,7 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
           if (pending) {
             const uint32_t r = c0 + __ffs(pending) - 1;
             pending &= pending - 1;
-            const float sr = filt.sum(a.data32 + static_cast<uint64_t>(r) * D);
+            const float sr = row_sum(r);
             if (!(sr > thr)) {  // the bound may have tightened meanwhile
               float clo, chi;
               filt.enclose(sr, &clo, &chi);

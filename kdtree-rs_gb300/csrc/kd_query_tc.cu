@@ -143,9 +143,11 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// Filter constants of one query from its current bound enclosure b.
+// Filter constants of one query from its current bound enclosure b (sqrt(b)
+// bounded above from rsqrtf, within 3 units in the last place, grown by 2^-19).
 __device__ __forceinline__ void tc_threshold(float b, float qn2, float qnorm, float* m2r, float* thr) {
-  const float r = __fadd_ru(__fsqrt_ru(b), __fmaf_ru(qnorm, 0.00390625f /* 2^-8 */, 1.1754944e-38f /* 2^-126 */));
+  const float sb = !(b > 0.f) ? 0.f : (!(b <= 3.4e38f) ? b : __fmul_ru(b * rsqrtf(b), 1.0000020f /* 1 + 2^-19 */));
+  const float r = __fadd_ru(sb, __fmaf_ru(qnorm, 0.00390625f /* 2^-8 */, 1.1754944e-38f /* 2^-126 */));
   *m2r = -2.f * r;
   *thr = __fsub_ru(__fmul_ru(r, r), __fmul_rd(qn2, 0.99975586f /* 1 - 2^-12 */));
 }

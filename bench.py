@@ -277,8 +277,9 @@ def plain_scale_cases(lib, torch, stream, dev):
 def precision_cases(lib, torch, stream, dev, cpu_threads):
     """Config 3: N=1M, d in {16, 64}, standard normal x per-dimension scale
     log-uniform in [0.1, 10], 100k queries, k=32, L2: the tensor-core filter path
-    against the reference-order FP64 path (on a 1,000-query sample), the filter's
-    survivors per pair, and the BF16 score's error against FP64."""
+    against the reference-order FP64 path (on a 1,000-query sample at d=16, 200 at
+    d=64), the filter's survivors per pair, and the BF16 score's error against
+    FP64."""
     from kdtree import KDTree
 
     out = {}
@@ -294,9 +295,10 @@ def precision_cases(lib, torch, stream, dev, cpu_threads):
         surv = torch.zeros(1, dtype=torch.int64, device=dev)
         ms_tc, (od, oi) = time_path(lib, tree, dq, 32, 2.0, PATH_TENSOR_CORE, 3, torch, stream, surv)
         pairs = 3 * q.shape[0] * data.shape[0]
-        sample = dq[:1000].contiguous()
+        n_ref = 1000 if d == 16 else 200  # the FP64 reference-order path: 1.6k q/s at d=16, 28 q/s at d=64
+        sample = dq[:n_ref].contiguous()
         ms_ref, (rd_, ri_) = time_path(lib, tree, sample, 32, 2.0, PATH_REFERENCE_ORDER, 1, torch, stream)
-        same = bool(torch.equal(oi[:1000], ri_) and torch.equal(od[:1000], rd_))
+        same = bool(torch.equal(oi[:n_ref], ri_) and torch.equal(od[:n_ref], rd_))
         # BF16 score error against FP64 on the true neighbours of 200 queries
         c = (data.min(0) + data.max(0)) / 2
         qi = np.repeat(np.arange(200), 32)
@@ -307,8 +309,8 @@ def precision_cases(lib, torch, stream, dev, cpu_threads):
         exact = ((q[qi] - data[pi]) ** 2).sum(1)
         rel = np.abs(approx - exact) / exact
         case = {"build_s": build_s, "tc_qps": q.shape[0] / ms_tc * 1e3, "tc_ms_100k": ms_tc,
-                "reference_order_fp64_qps": 1000 / ms_ref * 1e3, "reference_order_sample": 1000,
-                "speedup_tc_vs_fp64_path": (q.shape[0] / ms_tc) / (1000 / ms_ref),
+                "reference_order_fp64_qps": n_ref / ms_ref * 1e3, "reference_order_sample": n_ref,
+                "speedup_tc_vs_fp64_path": (q.shape[0] / ms_tc) / (n_ref / ms_ref),
                 "sample_identical": same, "rerank_fraction": int(surv.item()) / pairs,
                 "filter_rel_err_max": float(rel.max()), "filter_rel_err_median": float(np.median(rel))}
         if d == 16:  # the packet traversal on a 10,000-query sample (the tree barely prunes here)

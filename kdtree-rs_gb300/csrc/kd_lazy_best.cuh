@@ -22,11 +22,11 @@ struct LazyBest {
   float b_lo, b_hi;  // enclosure of the pruning bound min(k-th best, cutoff)
   float cut_lo, cut_hi;
   uint64_t cut_bits;
-  const QVec<D>* q;
+  QMem<D> q;
   const double* data;
   const uint32_t* indices;
 
-  __device__ __forceinline__ void init(uint64_t k, double cutoff, const QVec<D>* qv, const double* data_,
+  __device__ __forceinline__ void init(uint64_t k, double cutoff, const double* qg, const double* data_,
                                        const uint32_t* indices_) {
 #pragma unroll
     for (int j = 0; j < K; ++j) {
@@ -39,7 +39,7 @@ struct LazyBest {
     cut_bits = dbits(cutoff);
     cut_lo = mag_dn32(cut_bits);
     cut_hi = mag_up32(cut_bits);
-    q = qv;
+    q.g = qg;
     data = data_;
     indices = indices_;
     refresh();
@@ -49,7 +49,7 @@ struct LazyBest {
     b_hi = fminf(hi[K - 1], cut_hi);
   }
   __device__ __forceinline__ double exact_of(uint32_t r, bool in_chunk) const {
-    return exact_dist<M, D>(*q, data + static_cast<uint64_t>(r) * D, D, S_PACKED, in_chunk, 0.0);
+    return exact_dist<M, D>(q, data + static_cast<uint64_t>(r) * D, D, S_PACKED, in_chunk, 0.0);
   }
   __device__ __forceinline__ void slot_exact(int j, double* x, uint32_t* id) const {
     if (row[j] == ROW_NONE) {
@@ -223,11 +223,11 @@ struct LazySet {
   float b_lo, b_hi;  // enclosure of the pruning bound min(k-th best, cutoff)
   float cut_lo, cut_hi;
   uint64_t cut_bits;
-  const QVec<D>* q;
+  QMem<D> q;
   const double* data;
   const uint32_t* indices;
 
-  __device__ __forceinline__ void init(uint64_t k, double cutoff, const QVec<D>* qv, const double* data_,
+  __device__ __forceinline__ void init(uint64_t k, double cutoff, const double* qg, const double* data_,
                                        const uint32_t* indices_) {
 #pragma unroll
     for (int j = 0; j < K; ++j) {
@@ -241,7 +241,7 @@ struct LazySet {
     cut_bits = dbits(cutoff);
     cut_lo = mag_dn32(cut_bits);
     cut_hi = mag_up32(cut_bits);
-    q = qv;
+    q.g = qg;
     data = data_;
     indices = indices_;
     rescan();
@@ -274,7 +274,7 @@ struct LazySet {
     b_hi = fminf(mh, cut_hi);
   }
   __device__ __forceinline__ double exact_of(uint32_t r, bool in_chunk) const {
-    return exact_dist<M, D>(*q, data + static_cast<uint64_t>(r) * D, D, S_PACKED, in_chunk, 0.0);
+    return exact_dist<M, D>(q, data + static_cast<uint64_t>(r) * D, D, S_PACKED, in_chunk, 0.0);
   }
   __device__ __forceinline__ float slot_lo(int w) const {
     float v = lo[0];
@@ -446,11 +446,11 @@ struct LazyHeap {
   float b_hi;  // upper bound of the pruning bound min(k-th best, cutoff)
   float cut_lo, cut_hi;
   uint64_t cut_bits;
-  const QVec<D>* q;
+  QMem<D> q;
   const double* data;
   const uint32_t* indices;
 
-  __device__ __forceinline__ void init(uint64_t k_, double cutoff, const QVec<D>* qv, const double* data_,
+  __device__ __forceinline__ void init(uint64_t k_, double cutoff, const double* qg, const double* data_,
                                        const uint32_t* indices_, float* s_lo, float* s_hi, uint32_t* s_row) {
     lo = s_lo + threadIdx.x;
     hi = s_hi + threadIdx.x;
@@ -460,7 +460,7 @@ struct LazyHeap {
     cut_bits = dbits(cutoff);
     cut_lo = mag_dn32(cut_bits);
     cut_hi = mag_up32(cut_bits);
-    q = qv;
+    q.g = qg;
     data = data_;
     indices = indices_;
     b_hi = cut_hi;
@@ -470,7 +470,7 @@ struct LazyHeap {
   }
   static __device__ __forceinline__ bool chunk_of(float tagged) { return __float_as_uint(tagged) >> 31; }
   __device__ __forceinline__ double exact_of(uint32_t r, bool in_chunk) const {
-    return exact_dist<M, D>(*q, data + static_cast<uint64_t>(r) * D, D, S_PACKED, in_chunk, 0.0);
+    return exact_dist<M, D>(q, data + static_cast<uint64_t>(r) * D, D, S_PACKED, in_chunk, 0.0);
   }
   __device__ __forceinline__ void put(uint32_t j, float tl, float h, uint32_t r) {
     lo[j * S] = tl;
@@ -540,7 +540,12 @@ struct LazyHeap {
   // Enclosures too close to call: exact values of the candidate and of every
   // slot that can be the worst (hi >= lo[0]); those slots keep their tightened
   // enclosures; the candidate replaces the exact worst if it is before it.
-  __device__ __noinline__ void offer_exact(uint32_t r, bool in_chunk, bool have_x, double cx) {
+  // Inline although rare: out of line, as a member call, it put the heap
+  // object in local memory, so every access to its fields (and, through them,
+  // to the shared-memory slots) on the hot path became a local or generic
+  // load; as a call on a copy, the call's register convention cost more
+  // registers than the inlined code does.
+  __device__ __forceinline__ void offer_exact(uint32_t r, bool in_chunk, bool have_x, double cx) {
     if (!have_x) cx = exact_of(r, in_chunk);
     const uint32_t cid = indices[r];
     const float rl = fabsf(lo[0]);

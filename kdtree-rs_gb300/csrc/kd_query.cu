@@ -439,7 +439,10 @@ __global__ void k_landing_leaf(const DNode* nodes, const double* queries, uint64
   for (;;) {
     const DNode nd = nodes[node];
     if (nd.meta & KD_NODE_LEAF) break;
-    node = (q[nd.meta & KD_NODE_DIM_MASK] <= nd.split) ? node + 1 : nd.right;
+    // the order of IEEE keys (integer work; GB300's FP64 pipe is narrow): the
+    // same side as q <= split except for signed zeros, which only moves a query
+    // between neighbouring leaves of the sort
+    node = (ieee_key(dbits(q[nd.meta & KD_NODE_DIM_MASK])) <= ieee_key(dbits(nd.split))) ? node + 1 : nd.right;
   }
   leaf_of[i] = node;
   atomicAdd(&counts[node], 1u);

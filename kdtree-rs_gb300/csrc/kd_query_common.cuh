@@ -46,13 +46,23 @@ struct QVec {
   }
 };
 
+// A query read from memory at each use.  The k-best lists of the filtered
+// traversals need the FP64 query only for the rare exact distances; holding
+// it in registers across their FP32 row loops keeps 2 D registers live that
+// the FP32 copies were derived from.
+template <int D>
+struct QMem {
+  const double* g;
+  __device__ __forceinline__ double operator[](uint64_t i) const { return g[i]; }
+};
+
 // ---------------------------------------------------------------------------
 // Exact reduced point distance (src/kernel.rs:163-218, 343-354, 411-562).
 // `in_chunk`: the point lies inside a full Packed chunk of its leaf (d4: pairs,
 // d8: groups of 8); only then do d4 / d8 use their pairwise orders.
 // ---------------------------------------------------------------------------
-template <int M, int D>
-__device__ __forceinline__ double exact_dist(const QVec<D>& q, const double* p, uint64_t d, int strat, bool in_chunk,
+template <int M, int D, class Q>
+__device__ __forceinline__ double exact_dist(const Q& q, const double* p, uint64_t d, int strat, bool in_chunk,
                                              double pexp) {
   if (M == M_LP) {
     double dist = 0.0;

@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query_fast(QArgs a) {
 
   // the k best, as enclosures of their exact distances
   LazyBest<M, D, K> best;
-  best.init(a.k, a.cutoff, &q, a.data, a.indices);
+  best.init(a.k, a.cutoff, q.g, a.data, a.indices);
   const float& b_lo = best.b_lo;
   const float& b_hi = best.b_hi;
   auto bound_exact = [&]() -> uint64_t { return best.bound_exact(); };

@@ -89,11 +89,36 @@ struct PointFilter {
     *clo = __fmul_rd(lo, LB_SHRINK);
     *chi = __fmul_ru(hi, UB_GROW);
   }
+  // FP32 reduced distance of the row at p32, summed in dimension order.  The
+  // FP32 copy starts on an allocation boundary, so rows of a width divisible
+  // by 4 (2) are 16 (8) byte aligned and load as vectors: a quarter (half)
+  // of the load instructions.
   __device__ __forceinline__ float sum(const float* p32) const {
+    float p[D];
+    if constexpr (D % 4 == 0) {
+#pragma unroll
+      for (int c = 0; c < D / 4; ++c) {
+        const float4 v = reinterpret_cast<const float4*>(p32)[c];
+        p[4 * c] = v.x;
+        p[4 * c + 1] = v.y;
+        p[4 * c + 2] = v.z;
+        p[4 * c + 3] = v.w;
+      }
+    } else if constexpr (D % 2 == 0) {
+#pragma unroll
+      for (int c = 0; c < D / 2; ++c) {
+        const float2 v = reinterpret_cast<const float2*>(p32)[c];
+        p[2 * c] = v.x;
+        p[2 * c + 1] = v.y;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < D; ++i) p[i] = p32[i];
+    }
     float s = 0.f;
 #pragma unroll
     for (int i = 0; i < D; ++i) {
-      const float t = __fsub_rn(p32[i], q32[i]);
+      const float t = __fsub_rn(p[i], q32[i]);
       if (M == M_L2) s = __fmaf_rn(t, t, s);
       else if (M == M_L1) s = __fadd_rn(s, fabsf(t));
       else s = fmaxf(s, fabsf(t));
@@ -139,8 +164,12 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
     for (int i = 0; i < D; ++i) q.v[i] = 0.0;
   }
   float qlo[D], qhi[D];
+  uint64_t qkey[D];  // order keys of the coordinates, for exact side tests against splits
 #pragma unroll
-  for (int i = 0; i < D; ++i) rn_enclose(__double2float_rn(q.v[i]), &qlo[i], &qhi[i]);
+  for (int i = 0; i < D; ++i) {
+    rn_enclose(__double2float_rn(q.v[i]), &qlo[i], &qhi[i]);
+    qkey[i] = ieee_key(dbits(q.v[i]));
+  }
   PointFilter<M, D> filt;
   filt.init(q, a.coord_max);
   auto row_sum = [&](uint32_t r) { return filt.sum(a.data32 + static_cast<uint64_t>(r) * D); };
@@ -148,13 +177,13 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
   // k-best set: a shared-memory heap from K = 8 up, register slots below
   std::conditional_t<(K >= 8), LazyHeap<M, D, K>, LazySet<M, D, K>> best;
   if constexpr (K >= 8)
-    best.init(a.k, a.cutoff, &q, a.data, a.indices, s_lo, s_hi, s_row);
+    best.init(a.k, a.cutoff, q.g, a.data, a.indices, s_lo, s_hi, s_row);
   else
-    best.init(a.k, a.cutoff, &q, a.data, a.indices);
+    best.init(a.k, a.cutoff, q.g, a.data, a.indices);
   float thr = filt.threshold(best.b_hi);
 
-  // Seed: each lane first offers the points of its own landing leaf (reached
-  // by comparing FP32 copies; any leaf would be correct, this one is near), so
+  // Seed: each lane first offers the points of its own landing leaf (the
+  // leaf the reference's descent reaches; any leaf would be correct), so
   // its bound is tight before the shared traversal starts; the traversal then
   // skips that leaf for this lane.
   uint32_t own = NO_ID;
@@ -168,10 +197,10 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
       nd = a.nodes[0];
       while (!(nd.meta & KD_NODE_LEAF)) {
         const uint32_t dim = nd.meta & KD_NODE_DIM_MASK;
-        float qv = filt.q32[0];
+        uint64_t kq = qkey[0];
 #pragma unroll
-        for (int i = 1; i < D; ++i) qv = (static_cast<uint32_t>(i) == dim) ? filt.q32[i] : qv;
-        n = qv <= __double2float_rn(nd.split) ? n + 1 : nd.right;
+        for (int i = 1; i < D; ++i) kq = (static_cast<uint32_t>(i) == dim) ? qkey[i] : kq;
+        n = kq <= ieee_key(dbits(nd.split)) ? n + 1 : nd.right;
         nd = a.nodes[n];
       }
     }
@@ -239,10 +268,10 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
     }
     // near child first, by majority of the lanes that need this node
     const uint32_t dim = nd.meta & KD_NODE_DIM_MASK;
-    double qd = q.v[0];
+    uint64_t kq = qkey[0];
 #pragma unroll
-    for (int i = 1; i < D; ++i) qd = (static_cast<uint32_t>(i) == dim) ? q.v[i] : qd;
-    const bool left = ieee_key(dbits(qd)) <= ieee_key(dbits(nd.split));
+    for (int i = 1; i < D; ++i) kq = (static_cast<uint32_t>(i) == dim) ? qkey[i] : kq;
+    const bool left = kq <= ieee_key(dbits(nd.split));
     const uint32_t left_votes = __popc(__ballot_sync(0xffffffffu, need && left));
     const bool left_first = 2 * left_votes >= static_cast<uint32_t>(__popc(need_mask));
     stack[sp++] = left_first ? nd.right : node + 1;

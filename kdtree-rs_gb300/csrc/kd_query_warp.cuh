@@ -80,13 +80,13 @@ struct WarpLazyList {
   uint64_t cut_bits;
   float cut_lo, cut_hi;
   float bound32;  // FP32 upper bound of min(k-th best, cutoff)
-  const QVec<D>* q;
+  QMem<D> q;
   const double* data;
 
   __device__ __forceinline__ double exact_of(uint32_t r, bool in_chunk) const {
-    return exact_dist<M, D>(*q, data + static_cast<uint64_t>(r) * D, D, S_PACKED, in_chunk, 0.0);
+    return exact_dist<M, D>(q, data + static_cast<uint64_t>(r) * D, D, S_PACKED, in_chunk, 0.0);
   }
-  __device__ __forceinline__ void init(uint32_t k_, double cutoff, uint32_t lane_, const QVec<D>* qv,
+  __device__ __forceinline__ void init(uint32_t k_, double cutoff, uint32_t lane_, const double* qg,
                                        const double* data_) {
 #pragma unroll
     for (int s = 0; s < KS; ++s) {
@@ -100,7 +100,7 @@ struct WarpLazyList {
     cut_bits = dbits(cutoff);
     cut_lo = mag_dn32(cut_bits);
     cut_hi = mag_up32(cut_bits);
-    q = qv;
+    q.g = qg;
     data = data_;
     refresh();
   }
@@ -234,13 +234,19 @@ __device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, uint32_t*
   }
   PointFilter<M, D> filt;
   filt.init(q, a.coord_max);
+  // Every lane holds the same query.  Taking the FP32 copies out of shuffles
+  // pins them in registers: left as conversions of the FP64 query, they were
+  // recomputed inside the row loop, one FP64-pipe conversion per dimension
+  // and row (the FP64 pipe issues one warp instruction per 16 cycles).
+#pragma unroll
+  for (int i = 0; i < D; ++i) filt.q32[i] = __shfl_sync(FULL_MASK, filt.q32[i], 0);
   float my_qlo = 0.f, my_qhi = 0.f;
 #pragma unroll
   for (int i = 0; i < D; ++i)
     if (lane == static_cast<uint32_t>(i)) rn_enclose(filt.q32[i], &my_qlo, &my_qhi);
 
   WarpLazyList<M, D, KS> best;
-  best.init(static_cast<uint32_t>(a.k), a.cutoff, lane, &q, a.data);
+  best.init(static_cast<uint32_t>(a.k), a.cutoff, lane, q.g, a.data);
   float thr = filt.threshold(best.bound32);
 
   int sp = 0;
@@ -273,16 +279,13 @@ __device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, uint32_t*
       const uint32_t start = static_cast<uint32_t>(se), end = static_cast<uint32_t>(se >> 32);
       const uint32_t chunk_end = (D == 8 && M != M_LINF) ? start + (end - start) / 8 * 8 : end;
       for (uint32_t c0 = start; c0 < end; c0 += 32) {
+        // lanes past the leaf's end re-read its last row and drop it: no
+        // divergent branch around the row sum
         const uint32_t r = c0 + lane;
-        bool cand = false;
-        float clo = 0.f, chi = 0.f;
-        if (r < end) {
-          const float s = filt.sum(a.data32 + static_cast<uint64_t>(r) * D);
-          if (!(s > thr)) {
-            filt.enclose(s, &clo, &chi);
-            cand = !(clo > best.bound32);
-          }
-        }
+        const float s = filt.sum(a.data32 + static_cast<uint64_t>(min(r, end - 1)) * D);
+        float clo, chi;
+        filt.enclose(s, &clo, &chi);
+        const bool cand = r < end && !(s > thr) && !(clo > best.bound32);
         uint32_t mask = __ballot_sync(FULL_MASK, cand);
         if (!mask) continue;
         const uint32_t my_id = cand ? a.indices[r] : NO_ID;

@@ -35,21 +35,27 @@ struct Log2Ceil<1> {
   static constexpr int value = 0;
 };
 
-// Lower bound of the exact box distance: lane i < D takes dimension i; the
-// terms are combined with downward-rounded folds (any order gives a lower
-// bound) and the result broadcast from lane 0.
+// Lower bounds of the exact box distances of a node's two children, both at
+// once: lanes 0-15 take box bl, lanes 16-31 box br, lane i of a half
+// dimension i (my_qlo / my_qhi: the query's enclosure in dimension lane % 16).
+// Each term is rounded down and the terms are combined with downward-rounded
+// folds (any order gives a lower bound), which stay inside each half (D <= 16).
 template <int M, int D>
-__device__ __forceinline__ float warp_box_lb(const float* b32, float my_qlo, float my_qhi, uint32_t lane) {
+__device__ __forceinline__ void warp_box_lb2(const float* bl, const float* br, float my_qlo, float my_qhi,
+                                             uint32_t lane, float* lb_l, float* lb_r) {
+  static_assert(D <= 16, "one 16-lane half per box");
+  const uint32_t i = lane & 15;
+  const float* b = lane < 16 ? bl : br;
   float o = 0.f;
-  if (lane < static_cast<uint32_t>(D)) {
-    o = fmaxf(__fsub_rd(b32[lane], my_qhi), __fsub_rd(my_qlo, b32[D + lane]));
+  if (i < static_cast<uint32_t>(D)) {
+    o = fmaxf(__fsub_rd(b[i], my_qhi), __fsub_rd(my_qlo, b[D + i]));
     o = o > 0.f ? o : 0.f;
     o = red_lb<M>(o);
   }
 #pragma unroll
   for (int s = Log2Ceil<D>::value - 1; s >= 0; --s) o = fold_lb<M>(o, __shfl_xor_sync(FULL_MASK, o, 1 << s));
-  o = __shfl_sync(FULL_MASK, o, 0);
-  return __fmul_rd(o, LB_SHRINK);
+  *lb_l = __fmul_rd(__shfl_sync(FULL_MASK, o, 0), LB_SHRINK);
+  *lb_r = __fmul_rd(__shfl_sync(FULL_MASK, o, 16), LB_SHRINK);
 }
 
 __device__ __forceinline__ uint64_t shfl_u64(uint64_t v, int src) {
@@ -243,7 +249,7 @@ __device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, uint32_t*
   float my_qlo = 0.f, my_qhi = 0.f;
 #pragma unroll
   for (int i = 0; i < D; ++i)
-    if (lane == static_cast<uint32_t>(i)) rn_enclose(filt.q32[i], &my_qlo, &my_qhi);
+    if ((lane & 15) == static_cast<uint32_t>(i)) rn_enclose(filt.q32[i], &my_qlo, &my_qhi);
 
   WarpLazyList<M, D, KS> best;
   best.init(static_cast<uint32_t>(a.k), a.cutoff, lane, q.g, a.data);
@@ -257,8 +263,9 @@ __device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, uint32_t*
     DNode nd = a.nodes[node];
     while (!(nd.meta & KD_NODE_LEAF)) {
       const uint32_t l = node + 1, r = nd.right;
-      const float lb_l = warp_box_lb<M, D>(a.boxes32 + static_cast<uint64_t>(l) * 2 * D, my_qlo, my_qhi, lane);
-      const float lb_r = warp_box_lb<M, D>(a.boxes32 + static_cast<uint64_t>(r) * 2 * D, my_qlo, my_qhi, lane);
+      float lb_l, lb_r;
+      warp_box_lb2<M, D>(a.boxes32 + static_cast<uint64_t>(l) * 2 * D, a.boxes32 + static_cast<uint64_t>(r) * 2 * D,
+                         my_qlo, my_qhi, lane, &lb_l, &lb_r);
       const bool left_first = lb_l <= lb_r;
       const uint32_t nn = left_first ? l : r, fn = left_first ? r : l;
       const float lb_n = left_first ? lb_l : lb_r, lb_f = left_first ? lb_r : lb_l;

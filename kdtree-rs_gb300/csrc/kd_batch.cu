@@ -138,8 +138,8 @@ __global__ void k_batch_scatter(const uint32_t* q_start, uint32_t n_jobs, uint32
 }
 
 template <int M, int D, int KS>
-__device__ __forceinline__ void batch_query(const QArgs* a, uint64_t w, uint32_t* stack_n, float* stack_lb) {
-  warp_query<M, D, KS>(*a, w, stack_n, stack_lb);
+__device__ __forceinline__ void batch_query(const QArgs* a, uint64_t w, WarpStack* stack) {
+  warp_query<M, D, KS>(*a, w, stack);
 }
 
 // The persistent kernel: warps take tasks -- TASK_QUERIES consecutive
@@ -147,8 +147,7 @@ __device__ __forceinline__ void batch_query(const QArgs* a, uint64_t w, uint32_t
 // warp-per-query traversal (kd_query_warp.cuh) for the job's width.
 template <int M>
 __global__ void __launch_bounds__(QUERY_THREADS) k_query_batch(BatchArgs b) {
-  __shared__ uint32_t s_node[QUERY_THREADS / 32][WARP_STACK];
-  __shared__ float s_lb[QUERY_THREADS / 32][WARP_STACK];
+  __shared__ WarpStack s_stack[QUERY_THREADS / 32];
   const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (;;) {
     uint32_t t = 0;
@@ -161,14 +160,14 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query_batch(BatchArgs b) {
     const uint64_t last = min(first + TASK_QUERIES, J->a.nq);
     for (uint64_t w = first; w < last; ++w) {
       switch (J->cls) {
-        case 0: batch_query<M, 2, 1>(&J->a, w, s_node[wid], s_lb[wid]); break;
-        case 1: batch_query<M, 3, 1>(&J->a, w, s_node[wid], s_lb[wid]); break;
-        case 2: batch_query<M, 8, 1>(&J->a, w, s_node[wid], s_lb[wid]); break;
-        case 3: batch_query<M, 16, 1>(&J->a, w, s_node[wid], s_lb[wid]); break;
-        case 4: batch_query<M, 2, 2>(&J->a, w, s_node[wid], s_lb[wid]); break;
-        case 5: batch_query<M, 3, 2>(&J->a, w, s_node[wid], s_lb[wid]); break;
-        case 6: batch_query<M, 8, 2>(&J->a, w, s_node[wid], s_lb[wid]); break;
-        default: batch_query<M, 16, 2>(&J->a, w, s_node[wid], s_lb[wid]); break;
+        case 0: batch_query<M, 2, 1>(&J->a, w, &s_stack[wid]); break;
+        case 1: batch_query<M, 3, 1>(&J->a, w, &s_stack[wid]); break;
+        case 2: batch_query<M, 8, 1>(&J->a, w, &s_stack[wid]); break;
+        case 3: batch_query<M, 16, 1>(&J->a, w, &s_stack[wid]); break;
+        case 4: batch_query<M, 2, 2>(&J->a, w, &s_stack[wid]); break;
+        case 5: batch_query<M, 3, 2>(&J->a, w, &s_stack[wid]); break;
+        case 6: batch_query<M, 8, 2>(&J->a, w, &s_stack[wid]); break;
+        default: batch_query<M, 16, 2>(&J->a, w, &s_stack[wid]); break;
       }
     }
   }

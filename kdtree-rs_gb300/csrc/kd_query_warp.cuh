@@ -220,8 +220,18 @@ struct WarpLazyList {
   }
 };
 
+// A warp's traversal stack in shared memory: subtree id, the lower bound of
+// its box distance and its node record (read with its box when its parent was
+// expanded, so a pop costs no global load).  Every lane writes the same entry
+// and reads back what it wrote.
+struct WarpStack {
+  uint32_t node[WARP_STACK];
+  float lb[WARP_STACK];
+  DNode nd[WARP_STACK];
+};
+
 template <int M, int D, int KS>
-__device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, uint32_t* stack_n, float* stack_lb) {
+__device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, WarpStack* stack) {
   static_assert(D > 0 && M != M_LP, "warp path: compile-time width, metric without pow()");
   const uint32_t lane = threadIdx.x & 31;
   if (w >= a.nq) return;  // uniform per warp
@@ -257,29 +267,31 @@ __device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, uint32_t*
 
   int sp = 0;
   uint32_t node = 0;
+  DNode nd = a.nodes[0];
   bool have = true;
   while (have) {
-    // descend: the child with the smaller bound first, the other one stacked
-    DNode nd = a.nodes[node];
+    // descend: the child with the smaller bound first, the other one stacked;
+    // both children's records load with their boxes (one round trip a level)
     while (!(nd.meta & KD_NODE_LEAF)) {
       const uint32_t l = node + 1, r = nd.right;
+      const DNode nd_l = a.nodes[l], nd_r = a.nodes[r];
       float lb_l, lb_r;
       warp_box_lb2<M, D>(a.boxes32 + static_cast<uint64_t>(l) * 2 * D, a.boxes32 + static_cast<uint64_t>(r) * 2 * D,
                          my_qlo, my_qhi, lane, &lb_l, &lb_r);
       const bool left_first = lb_l <= lb_r;
-      const uint32_t nn = left_first ? l : r, fn = left_first ? r : l;
       const float lb_n = left_first ? lb_l : lb_r, lb_f = left_first ? lb_r : lb_l;
       if (!(lb_f > best.bound32)) {
-        stack_n[sp] = fn;
-        stack_lb[sp] = lb_f;
+        stack->node[sp] = left_first ? r : l;
+        stack->lb[sp] = lb_f;
+        stack->nd[sp] = left_first ? nd_r : nd_l;
         ++sp;
       }
       if (lb_n > best.bound32) {
         nd.meta = 0;  // nothing below the near child either: go pop
         break;
       }
-      node = nn;
-      nd = a.nodes[node];
+      node = left_first ? l : r;
+      nd = left_first ? nd_l : nd_r;
     }
     if (nd.meta & KD_NODE_LEAF) {
       const uint64_t se = dbits(nd.split);
@@ -311,8 +323,9 @@ __device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, uint32_t*
     have = false;
     while (sp > 0) {
       --sp;
-      if (!(stack_lb[sp] > best.bound32)) {
-        node = stack_n[sp];
+      if (!(stack->lb[sp] > best.bound32)) {
+        node = stack->node[sp];
+        nd = stack->nd[sp];
         have = true;
         break;
       }
@@ -321,12 +334,10 @@ __device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, uint32_t*
   best.write(a.out_d + qi * a.k, a.out_i + qi * a.k, a.n_points);
 }
 
-// One warp per query; the block's warps keep their stacks in shared memory
-// (every lane writes the same entry and reads back what it wrote).
+// One warp per query; the block's warps keep their stacks in shared memory.
 template <int M, int D, int KS>
 __global__ void __launch_bounds__(QUERY_THREADS) k_query_warp(QArgs a) {
-  __shared__ uint32_t s_node[QUERY_THREADS / 32][WARP_STACK];
-  __shared__ float s_lb[QUERY_THREADS / 32][WARP_STACK];
+  __shared__ WarpStack s_stack[QUERY_THREADS / 32];
   const uint32_t wid = threadIdx.x >> 5;
-  warp_query<M, D, KS>(a, blockIdx.x * static_cast<uint64_t>(QUERY_THREADS / 32) + wid, s_node[wid], s_lb[wid]);
+  warp_query<M, D, KS>(a, blockIdx.x * static_cast<uint64_t>(QUERY_THREADS / 32) + wid, &s_stack[wid]);
 }

@@ -144,9 +144,12 @@ __device__ __forceinline__ void batch_query(const QArgs* a, uint64_t w, WarpStac
 
 // The persistent kernel: warps take tasks -- TASK_QUERIES consecutive
 // positions of one job -- until none is left, and run each query with the
-// warp-per-query traversal (kd_query_warp.cuh) for the job's width.
-template <int M>
-__global__ void __launch_bounds__(QUERY_THREADS) k_query_batch(BatchArgs b) {
+// warp-per-query traversal (kd_query_warp.cuh) for the job's width.  W16: the
+// batch holds 16-wide jobs; without them the kernel is held to 72 registers,
+// 7 blocks an SM instead of 5 (measured faster on the mixed 2/3/8-wide batch
+// than the 87 registers the compiler picks unbounded).
+template <int M, bool W16>
+__global__ void __launch_bounds__(QUERY_THREADS, W16 ? 5 : 7) k_query_batch(BatchArgs b) {
   __shared__ WarpStack s_stack[QUERY_THREADS / 32];
   const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (;;) {
@@ -163,29 +166,39 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query_batch(BatchArgs b) {
         case 0: batch_query<M, 2, 1>(&J->a, w, &s_stack[wid]); break;
         case 1: batch_query<M, 3, 1>(&J->a, w, &s_stack[wid]); break;
         case 2: batch_query<M, 8, 1>(&J->a, w, &s_stack[wid]); break;
-        case 3: batch_query<M, 16, 1>(&J->a, w, &s_stack[wid]); break;
         case 4: batch_query<M, 2, 2>(&J->a, w, &s_stack[wid]); break;
         case 5: batch_query<M, 3, 2>(&J->a, w, &s_stack[wid]); break;
         case 6: batch_query<M, 8, 2>(&J->a, w, &s_stack[wid]); break;
-        default: batch_query<M, 16, 2>(&J->a, w, &s_stack[wid]); break;
+        default:  // classes 3 and 7, present only when W16
+          if constexpr (W16) {
+            if (J->cls == 3) batch_query<M, 16, 1>(&J->a, w, &s_stack[wid]);
+            else batch_query<M, 16, 2>(&J->a, w, &s_stack[wid]);
+          }
+          break;
       }
     }
   }
 }
 
-template <int M>
+template <int M, bool W16>
 int max_blocks_per_sm() {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_query_batch<M>, QUERY_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_query_batch<M, W16>, QUERY_THREADS, 0);
   return std::max(n, 1);
 }
 
-int resident_blocks_per_sm(int metric) {
+int resident_blocks_per_sm(int metric, bool w16) {
   switch (metric) {
-    case M_L1: return max_blocks_per_sm<M_L1>();
-    case M_L2: return max_blocks_per_sm<M_L2>();
-    default: return max_blocks_per_sm<M_LINF>();
+    case M_L1: return w16 ? max_blocks_per_sm<M_L1, true>() : max_blocks_per_sm<M_L1, false>();
+    case M_L2: return w16 ? max_blocks_per_sm<M_L2, true>() : max_blocks_per_sm<M_L2, false>();
+    default: return w16 ? max_blocks_per_sm<M_LINF, true>() : max_blocks_per_sm<M_LINF, false>();
   }
+}
+
+template <int M>
+void launch_batch(bool w16, unsigned blocks, cudaStream_t st, const BatchArgs& a) {
+  if (w16) k_query_batch<M, true><<<blocks, QUERY_THREADS, 0, st>>>(a);
+  else k_query_batch<M, false><<<blocks, QUERY_THREADS, 0, st>>>(a);
 }
 
 // ---------------------------------------------------------------------------
@@ -209,6 +222,7 @@ struct Layout {
   std::vector<BatchJob> table;
   uint64_t n_bins = 1;
   uint32_t total_q = 0, n_tasks = 0;
+  bool wide16 = false;  // some fused job is 16 wide
 };
 
 void fill_args(QArgs* a, const JobSpec& J, const QueryParams& qp) {
@@ -261,6 +275,7 @@ void make_layout(const std::vector<JobSpec>& specs, const QueryParams& qp, bool 
     BatchJob& B = L->table[i];
     fill_args(&B.a, J, qp);
     B.cls = cls[L->packet[i]];
+    L->wide16 |= B.cls % 4 == 3;
     B.sorted = sort && J.nq >= SORT_MIN_QUERIES;
     B.a.order = B.sorted ? order + L->q_start[i] : nullptr;
     B.bin_start = bins;
@@ -346,9 +361,9 @@ int enqueue_packet(const Layout& L, const Buffers& B, int table, int metric, uns
   KD_TRY_CUDA(cudaMemsetAsync(B.counter, 0, sizeof(uint32_t), st));
   BatchArgs a{B.jobs[table], B.task_start, n, L.n_tasks, B.counter};
   switch (metric) {
-    case M_L1: k_query_batch<M_L1><<<blocks, QUERY_THREADS, 0, st>>>(a); break;
-    case M_L2: k_query_batch<M_L2><<<blocks, QUERY_THREADS, 0, st>>>(a); break;
-    default: k_query_batch<M_LINF><<<blocks, QUERY_THREADS, 0, st>>>(a); break;
+    case M_L1: launch_batch<M_L1>(L.wide16, blocks, st, a); break;
+    case M_L2: launch_batch<M_L2>(L.wide16, blocks, st, a); break;
+    default: launch_batch<M_LINF>(L.wide16, blocks, st, a); break;
   }
   KD_TRY_CUDA(cudaGetLastError());
   return KD_OK;
@@ -495,7 +510,7 @@ int finish_plan(kd_batch* b, cudaStream_t st) {
 // The autotuner: every candidate launch shape runs the plan once to warm up
 // and twice timed; the fastest is kept.  Results are identical for all.
 int tune(kd_batch* b, cudaStream_t st) {
-  const int per_sm = resident_blocks_per_sm(b->qp.metric);
+  const int per_sm = resident_blocks_per_sm(b->qp.metric, b->layout[0].wide16);
   std::vector<unsigned> grids;
   for (int m : {1, 2, 4, 8})
     if (m <= per_sm) grids.push_back(static_cast<unsigned>(b->sms * m));
@@ -666,7 +681,7 @@ int stage_batch(kd_server* s, Slot* sl) {
   int rc = enqueue_others(specs, L.other, s->qp, sl->side, st, nullptr, {});
   if (rc) return rc;
   if (np) {
-    const unsigned blocks = static_cast<unsigned>(s->sms * resident_blocks_per_sm(s->qp.metric));
+    const unsigned blocks = static_cast<unsigned>(s->sms * resident_blocks_per_sm(s->qp.metric, L.wide16));
     rc = enqueue_packet(L, sl->buf, 0, s->qp.metric, blocks, st);
   }
   join_others(sl->side, L.other.size(), st);
@@ -866,7 +881,7 @@ int kd_batch_create(const kd_batch_job* jobs, uint64_t n_jobs, double p, int has
     release_plan(b);
     return rc;
   }
-  b->blocks = static_cast<unsigned>(b->sms * resident_blocks_per_sm(qp.metric));
+  b->blocks = static_cast<unsigned>(b->sms * resident_blocks_per_sm(qp.metric, b->layout[0].wide16));
   *out = b;
   return KD_OK;
 }

@@ -313,11 +313,12 @@ def precision_cases(lib, torch, stream, dev, cpu_threads):
                 "speedup_tc_vs_fp64_path": (q.shape[0] / ms_tc) / (n_ref / ms_ref),
                 "sample_identical": same, "rerank_fraction": int(surv.item()) / pairs,
                 "filter_rel_err_max": float(rel.max()), "filter_rel_err_median": float(np.median(rel))}
-        if d == 16:  # the packet traversal on a 10,000-query sample (the tree barely prunes here)
+        if d == 16:  # the two traversals on a 10,000-query sample (the tree barely prunes here)
             ps = dq[:10_000].contiguous()
-            ms_pk, (pd_, pi_) = time_path(lib, tree, ps, 32, 2.0, PATH_PACKET, 1, torch, stream)
-            case["packet_qps"] = 10_000 / ms_pk * 1e3
-            case["packet_identical"] = bool(torch.equal(pi_, oi[:10_000]) and torch.equal(pd_, od[:10_000]))
+            for name, path in (("packet", PATH_PACKET), ("warp", PATH_WARP)):
+                ms_pk, (pd_, pi_) = time_path(lib, tree, ps, 32, 2.0, path, 1, torch, stream)
+                case[name + "_qps"] = 10_000 / ms_pk * 1e3
+                case[name + "_identical"] = bool(torch.equal(pi_, oi[:10_000]) and torch.equal(pd_, od[:10_000]))
         if cpu_threads:
             sys.path.insert(0, str(ROOT / "oracle"))
             import kdtree_oracle

@@ -6,20 +6,22 @@
 // dimensions: the reference's own descent reads 3.8k rows per query at d = 8
 // and 14.5k at d = 16 on a 64-cluster mixture), the packet traversal's warp
 // walks the union of 32 queries' leaves.  Here the 32 lanes work on ONE query:
-// every leaf's rows are split across the lanes (row r + lane), every box's
-// dimensions too (lane i takes dimension i), and the k best (exact FP64 reduced
-// distance bits, original index) live one or two per lane, sorted, lane j
-// holding the j-th (and the (32 + j)-th).  The traversal is best-first at each
-// node (the child with the smaller box bound first) and prunes a subtree whose
-// rigorous FP32 lower bound exceeds the FP32 upper enclosure of the exact bound
+// every leaf's rows are split across the lanes (row r + lane), a node's two
+// children's boxes across the two half-warps (lane i of a half takes dimension
+// i), and the k best (FP32 enclosures of the exact FP64 reduced distances, tree
+// row, original index) live one or two per lane, sorted, lane j holding the
+// j-th (and the (32 + j)-th).  The traversal is best-first at each node (the
+// child with the smaller box bound first) and prunes a subtree whose rigorous
+// FP32 lower bound exceeds the FP32 upper enclosure of the exact bound
 // min(k-th best, cutoff).
 //
 // Candidate points pass the same rigorous FP32 filter as the packet traversal
 // (PointFilter) and enter the list by their exact (distance, index) order --
 // BestK's (query.rs:461-481) -- decided on FP32 enclosures of the exact FP64
 // distance in the reference's summation order, with the exact value computed
-// only when enclosures overlap (GB300 runs FP64 at 1/58 of the FP32 rate).  The result is therefore the k smallest (exact distance,
-// index) among the points within max_distance, as for the packet traversal.
+// only when enclosures overlap (GB300 runs FP64 at 1/58 of the FP32 rate).
+// The result is therefore the k smallest (exact distance, index) among the
+// points within max_distance, as for the packet traversal.
 #pragma once
 
 constexpr int WARP_STACK = 2 * KD_MAX_DEPTH;

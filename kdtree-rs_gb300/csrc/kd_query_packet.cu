@@ -23,7 +23,7 @@ namespace {
 // SM, the rest for L1 -- measured best on GB300 (N = 1M, d = 3, k = 16, 1M
 // queries: 2.69 ms a step against 2.79 ms at 75 %, 2.99 ms at 60 % and
 // 2.70 ms at 100 %).  KD_PACKET_CARVEOUT (0..100) overrides it for every k;
-// unset, the other k keep the driver's choice.
+// unset, the other k keep the CUDA runtime's default.
 int carveout_override() {
   static const int v = [] {
     const char* e = std::getenv("KD_PACKET_CARVEOUT");

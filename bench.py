@@ -221,6 +221,23 @@ def gmm_points(rng, centres, n, sigma=0.01):
     return centres[rng.integers(0, len(centres), n)] + sigma * rng.standard_normal((n, centres.shape[1]))
 
 
+def build_line(build_s, cpu_s, hbm_peak):
+    """The build's report: host wall time of kd_build (incl. the upload) and its
+    algorithmic bytes -- per split level, every row's box pass (8d B read) and
+    the partition's row and index read + write (2 (8d + 4) B) -- over that time."""
+    levels, n = 0, N_POINTS
+    while n > LEAFSIZE:  # the largest segment at each depth is ceil(n / 2^depth)
+        n = (n + 1) // 2
+        levels += 1
+    b = levels * N_POINTS * (3 * 8 * DIM + 8)
+    gbs = b / build_s / 1e9
+    return {"gpu_s": build_s, "cpu_oracle_s": cpu_s, "levels": levels, "algorithmic_bytes": b,
+            "achieved_gbs": gbs, "frac_of_hbm": gbs / hbm_peak if hbm_peak else None,
+            "note": "host wall time of kd_build incl. the 24 MB upload; oracle build on all host cores; "
+                    "per level the build is a few dependent launches over L2-resident data, so it is "
+                    "launch- and latency-bound, not HBM-bound"}
+
+
 def time_path(lib, tree, dq, k, p, path, reps, torch, stream, survivors=None):
     """Mean ms of kd_query_device_path over `reps` calls (events on `stream`)."""
     n = dq.shape[0]
@@ -783,8 +800,7 @@ def main():
         "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),
                 "d2h_bytes_per_step": int(N_QUERIES * K * 16)},
         "roofline": roofline,
-        "build": {"gpu_s": build_s, "cpu_oracle_s": cpu["build_s"] if cpu else None,
-                  "note": "host wall time of kd_build incl. the 24 MB upload; oracle build on all host cores"},
+        "build": build_line(build_s, cpu["build_s"] if cpu else None, peak),
         "cpu_baseline": None if cpu is None else {
             "value": cpu["qps"], "unit": "queries/s", "cores": kdtree_oracle.max_threads(), "kind": "port",
             "sample": "the full 1,000,000-query step, best of 3 runs (oracle restatement of the reference)"},

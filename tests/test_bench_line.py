@@ -1,0 +1,38 @@
+"""Host-side pieces of the bench line (no GPU): the roofline's algorithmic
+bytes, the DRAM traffic read from the committed ncu summary, the measured peak,
+and the build's level count and bytes."""
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT))
+
+import bench  # noqa: E402
+
+
+def test_algorithmic_bytes_formula():
+    # B_q = 8d + 16k + 8d*S_q + 24*V_q + 16d*X_q, summed: one query, 2 nodes, 5 rows, 1 box
+    d, k = bench.DIM, bench.K
+    assert bench.algorithmic_bytes((2, 5, 1), 1) == 8 * d + 16 * k + 8 * d * 5 + 24 * 2 + 16 * d * 1
+
+
+def test_profiled_traffic_matches_summary():
+    t = bench.profiled_traffic()
+    assert isinstance(t, int) and t > 0
+    text = (ROOT / "profiles" / "k_query_packet_uniform_n1m_d3_k16.md").read_text()
+    assert f"traffic_bytes_per_launch: {t}" in text
+
+
+def test_measured_peak_is_positive():
+    peak, kind = bench.measured_peak()
+    assert peak > 0 and kind in ("measured", "fallback")
+
+
+def test_build_line_levels_and_bytes():
+    b = bench.build_line(0.005, 0.04, 6000.0)
+    # 1M rows, leafsize 16: segments of ceil(1M / 2^t) rows split while above 16 -> 16 levels
+    assert b["levels"] == 16
+    assert b["algorithmic_bytes"] == 16 * bench.N_POINTS * (3 * 8 * bench.DIM + 8)
+    assert abs(b["achieved_gbs"] - b["algorithmic_bytes"] / 0.005 / 1e9) < 1e-6
+    assert b["frac_of_hbm"] == b["achieved_gbs"] / 6000.0
+    assert bench.build_line(0.005, None, None)["frac_of_hbm"] is None

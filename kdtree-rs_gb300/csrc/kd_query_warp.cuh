@@ -26,7 +26,6 @@
 
 constexpr int WARP_STACK = 2 * KD_MAX_DEPTH;
 constexpr uint32_t FULL_MASK = 0xffffffffu;
-constexpr uint64_t EMPTY_KEY = ~0ull;
 
 template <int D>
 struct Log2Ceil {
@@ -58,17 +57,6 @@ __device__ __forceinline__ void warp_box_lb2(const float* bl, const float* br, f
   for (int s = Log2Ceil<D>::value - 1; s >= 0; --s) o = fold_lb<M>(o, __shfl_xor_sync(FULL_MASK, o, 1 << s));
   *lb_l = __fmul_rd(__shfl_sync(FULL_MASK, o, 0), LB_SHRINK);
   *lb_r = __fmul_rd(__shfl_sync(FULL_MASK, o, 16), LB_SHRINK);
-}
-
-__device__ __forceinline__ uint64_t shfl_u64(uint64_t v, int src) {
-  const uint32_t lo = __shfl_sync(FULL_MASK, static_cast<uint32_t>(v), src);
-  const uint32_t hi = __shfl_sync(FULL_MASK, static_cast<uint32_t>(v >> 32), src);
-  return (static_cast<uint64_t>(hi) << 32) | lo;
-}
-__device__ __forceinline__ uint64_t shfl_up_u64(uint64_t v) {
-  const uint32_t lo = __shfl_up_sync(FULL_MASK, static_cast<uint32_t>(v), 1);
-  const uint32_t hi = __shfl_up_sync(FULL_MASK, static_cast<uint32_t>(v >> 32), 1);
-  return (static_cast<uint64_t>(hi) << 32) | lo;
 }
 
 // The warp's sorted k best, KS slots per lane (k <= 32 KS): rank r lives in

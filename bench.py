@@ -238,8 +238,20 @@ def build_line(build_s, cpu_s, hbm_peak):
                     "launch- and latency-bound, not HBM-bound"}
 
 
-def time_path(lib, tree, dq, k, p, path, reps, torch, stream, survivors=None):
-    """Mean ms of kd_query_device_path over `reps` calls (events on `stream`)."""
+def path_lib():
+    """The library with kd_query_device_path's signature declared."""
+    from kdtree import _core
+
+    lib = _core._lib
+    P_, u64_, d_ = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double
+    lib.kd_query_device_path.argtypes = [P_, P_, u64_, u64_, d_, ctypes.c_int, d_, d_, P_, P_, P_, ctypes.c_int, P_]
+    lib.kd_query_device_path.restype = ctypes.c_int
+    return lib
+
+
+def time_path(lib, tree, dq, k, p, path, reps, torch, stream, survivors=None, warm=True):
+    """Mean ms of kd_query_device_path over `reps` calls (events on `stream`),
+    after one untimed call unless `warm` is False."""
     n = dq.shape[0]
     od = torch.empty((n, k), dtype=torch.float64, device=dq.device)
     oi = torch.empty((n, k), dtype=torch.int64, device=dq.device)
@@ -252,7 +264,8 @@ def time_path(lib, tree, dq, k, p, path, reps, torch, stream, survivors=None):
         if st:
             raise RuntimeError(f"kd_query_device_path failed: {st}")
 
-    call()  # warm-up (and, for the tensor-core path, the one-time BF16 copy of the tree)
+    if warm:
+        call()  # warm-up (and, for the tensor-core path, the one-time BF16 copy of the tree)
     if survivors is not None:
         survivors.zero_()
     torch.cuda.synchronize()
@@ -294,9 +307,8 @@ def plain_scale_cases(lib, torch, stream, dev):
 def precision_cases(lib, torch, stream, dev, cpu_threads):
     """Config 3: N=1M, d in {16, 64}, standard normal x per-dimension scale
     log-uniform in [0.1, 10], 100k queries, k=32, L2: the tensor-core filter path
-    against the reference-order FP64 path (on a 1,000-query sample at d=16, 200 at
-    d=64), the filter's survivors per pair, and the BF16 score's error against
-    FP64."""
+    against the reference-order FP64 path (on a 4,864-query sample), the
+    filter's survivors per pair, and the BF16 score's error against FP64."""
     from kdtree import KDTree
 
     out = {}
@@ -312,9 +324,13 @@ def precision_cases(lib, torch, stream, dev, cpu_threads):
         surv = torch.zeros(1, dtype=torch.int64, device=dev)
         ms_tc, (od, oi) = time_path(lib, tree, dq, 32, 2.0, PATH_TENSOR_CORE, 3, torch, stream, surv)
         pairs = 3 * q.shape[0] * data.shape[0]
-        n_ref = 1000 if d == 16 else 200  # the FP64 reference-order path: 1.6k q/s at d=16, 28 q/s at d=64
+        # The FP64 reference-order path runs one thread per query; its sample is
+        # 38 blocks of 128 queries (38 SMs with 4 warps each), enough to measure
+        # throughput rather than one warp's latency, in about half a minute at d=64.
+        n_ref = 38 * 128
         sample = dq[:n_ref].contiguous()
-        ms_ref, (rd_, ri_) = time_path(lib, tree, sample, 32, 2.0, PATH_REFERENCE_ORDER, 1, torch, stream)
+        ms_ref, (rd_, ri_) = time_path(lib, tree, sample, 32, 2.0, PATH_REFERENCE_ORDER, 1, torch, stream,
+                                       warm=False)
         same = bool(torch.equal(oi[:n_ref], ri_) and torch.equal(od[:n_ref], rd_))
         # BF16 score error against FP64 on the true neighbours of 200 queries
         c = (data.min(0) + data.max(0)) / 2
@@ -637,6 +653,8 @@ def main():
     ap.add_argument("--no-cases", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--batched-only", action="store_true", help="only run the batched multi-tree case")
     ap.add_argument("--serving-only", action="store_true", help="only run the serving case")
+    ap.add_argument("--precision-only", action="store_true",
+                    help="only run the precision case (d=16 and d=64, tensor-core vs FP64 paths), no CPU leg")
     ap.add_argument("--profile-warp", action="store_true",
                     help="only run the warp-per-query path on a profiling-sized case (d=16 mixture, N=1M, "
                          "20,000 queries, k=16), 3 calls")
@@ -654,6 +672,13 @@ def main():
         import torch
 
         print(json.dumps({"serving": serving_case(torch)}), flush=True)
+        return 0
+    if args.precision_only:
+        import torch
+
+        stream = torch.cuda.Stream()
+        dev = torch.device("cuda", 0)
+        print(json.dumps({"precision": precision_cases(path_lib(), torch, stream, dev, 0)}), flush=True)
         return 0
     if args.batched_only:
         import torch

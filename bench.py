@@ -600,12 +600,8 @@ def run_profile_tc():
     import torch
 
     from kdtree import KDTree
-    from kdtree import _core
 
-    lib = _core._lib
-    P_, u64_, d_ = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double
-    lib.kd_query_device_path.argtypes = [P_, P_, u64_, u64_, d_, ctypes.c_int, d_, d_, P_, P_, P_, ctypes.c_int, P_]
-    lib.kd_query_device_path.restype = ctypes.c_int
+    lib = path_lib()
     rng = np.random.default_rng(364)
     scale = np.exp(rng.uniform(np.log(0.1), np.log(10), 64))
     data = rng.standard_normal((100_000, 64)) * scale
@@ -625,12 +621,8 @@ def run_profile_warp():
     import torch
 
     from kdtree import KDTree
-    from kdtree import _core
 
-    lib = _core._lib
-    P_, u64_, d_ = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double
-    lib.kd_query_device_path.argtypes = [P_, P_, u64_, u64_, d_, ctypes.c_int, d_, d_, P_, P_, P_, ctypes.c_int, P_]
-    lib.kd_query_device_path.restype = ctypes.c_int
+    lib = path_lib()
     rng = np.random.default_rng(716)
     c = rng.uniform(size=(64, 16))
     data = c[rng.integers(0, 64, 1_000_000)] + 0.01 * rng.standard_normal((1_000_000, 16))
@@ -698,10 +690,7 @@ def main():
     from kdtree import KDTree
     from kdtree import _core
 
-    lib = _core._lib
-    P_, u64_, d_ = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double
-    lib.kd_query_device_path.argtypes = [P_, P_, u64_, u64_, d_, ctypes.c_int, d_, d_, P_, P_, P_, ctypes.c_int, P_]
-    lib.kd_query_device_path.restype = ctypes.c_int
+    lib = path_lib()
     data, q = workload(rank)
 
     # build (GPU), timed on the host around the synchronous call

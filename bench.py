@@ -148,6 +148,25 @@ def cpu_baseline(data, q, threads, reps=3):
     return {"qps": len(q) / best, "build_s": build_s, "counts": counts, "tree": t}
 
 
+def scipy_baseline(data, q, k=None, leafsize=None):
+    """SciPy's cKDTree (the reference's own test oracle) on all host cores
+    (workers=-1): a sanity number beside the oracle, not the baseline.  None
+    when SciPy is not installed."""
+    try:
+        from scipy.spatial import cKDTree
+    except ImportError:
+        return None
+    k = K if k is None else k
+    leafsize = LEAFSIZE if leafsize is None else leafsize
+    t0 = time.perf_counter()
+    t = cKDTree(data, leafsize=leafsize)
+    build_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    t.query(q, k=k, p=P, workers=-1)
+    query_s = time.perf_counter() - t0
+    return {"qps": len(q) / query_s, "build_s": build_s, "workers": os.cpu_count()}
+
+
 def algorithmic_bytes(counts, n_queries):
     """Per-query B_q = 8d + 16k + 8d*S_q + 24*V_q + 16d*X_q summed over the batch
     (V = nodes visited, S = leaf rows scanned, X = boxes evaluated)."""
@@ -817,7 +836,8 @@ def main():
         "build": build_line(build_s, cpu["build_s"] if cpu else None, peak),
         "cpu_baseline": None if cpu is None else {
             "value": cpu["qps"], "unit": "queries/s", "cores": kdtree_oracle.max_threads(), "kind": "port",
-            "sample": "the full 1,000,000-query step, best of 3 runs (oracle restatement of the reference)"},
+            "sample": "the full 1,000,000-query step, best of 3 runs (oracle restatement of the reference)",
+            "scipy_ckdtree": scipy_baseline(data, q)},
         "wall_s_timed_region": t_wall,
     }
     if not args.no_cases and ws == 1:

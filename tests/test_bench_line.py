@@ -36,3 +36,13 @@ def test_build_line_levels_and_bytes():
     assert abs(b["achieved_gbs"] - b["algorithmic_bytes"] / 0.005 / 1e9) < 1e-6
     assert b["frac_of_hbm"] == b["achieved_gbs"] / 6000.0
     assert bench.build_line(0.005, None, None)["frac_of_hbm"] is None
+
+
+def test_scipy_baseline_small():
+    import numpy as np
+    import pytest
+
+    pytest.importorskip("scipy")
+    rng = np.random.default_rng(0)
+    r = bench.scipy_baseline(rng.uniform(size=(2000, 3)), rng.uniform(size=(300, 3)), k=4, leafsize=16)
+    assert r["qps"] > 0 and r["build_s"] >= 0 and r["workers"] >= 1

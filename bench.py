@@ -174,6 +174,31 @@ def algorithmic_bytes(counts, n_queries):
     return 8 * DIM * n_queries + 16 * K * n_queries + 8 * DIM * scanned + 24 * visits + 16 * DIM * boxes
 
 
+def count_nodes(n, leafsize=LEAFSIZE):
+    """Nodes of the median-split tree over n points (split at n // 2 while
+    n > leafsize), as the reference's count_nodes."""
+    memo = {}
+
+    def c(m):
+        if m <= leafsize:
+            return 1
+        if m not in memo:
+            memo[m] = 1 + c(m // 2) + c(m - m // 2)
+        return memo[m]
+
+    return c(n)
+
+
+def compulsory_bytes(n_queries=N_QUERIES):
+    """Bytes one query launch cannot avoid: the queries in, the results out,
+    and every tree array the kernel reads once (FP64 rows for the exact
+    values, FP32 rows, original indices, 16-byte nodes, FP32 boxes) plus the
+    sort's order and landing leaf per query."""
+    nodes = count_nodes(N_POINTS)
+    tree = N_POINTS * DIM * 8 + N_POINTS * DIM * 4 + N_POINTS * 4 + nodes * 16 + nodes * 2 * DIM * 4
+    return n_queries * DIM * 8 + n_queries * K * 16 + tree + n_queries * 8
+
+
 def measured_peak():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -818,6 +843,8 @@ def main():
                     "algorithmic_bytes_per_launch": per_launch,
                     "per_query": {"nodes_visited": counts[0] / N_QUERIES, "rows_scanned": counts[1] / N_QUERIES,
                                   "boxes_evaluated": counts[2] / N_QUERIES},
+                    "compulsory_bytes_per_launch": compulsory_bytes(),
+                    "traffic_over_compulsory": (traffic / compulsory_bytes()) if traffic else None,
                     "kernel": "k_query_packet<L2, d=3, K=16>", "kernel_ms": mean_s * 1e3,
                     "traffic_note": "DRAM read+write bytes per launch from ncu (profiles/)"}
     line = {

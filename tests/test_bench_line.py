@@ -46,3 +46,18 @@ def test_scipy_baseline_small():
     rng = np.random.default_rng(0)
     r = bench.scipy_baseline(rng.uniform(size=(2000, 3)), rng.uniform(size=(300, 3)), k=4, leafsize=16)
     assert r["qps"] > 0 and r["build_s"] >= 0 and r["workers"] >= 1
+
+
+def test_count_nodes_matches_the_reference_sizes():
+    # the node counts the reference's layout gives (N=1M leafsize 16, N=10k leafsize 32)
+    assert bench.count_nodes(1_000_000, 16) == 131_071
+    assert bench.count_nodes(10_000, 32) == 1_023
+    assert bench.count_nodes(5, 32) == 1
+
+
+def test_compulsory_bytes_close_to_profiled_traffic():
+    c = bench.compulsory_bytes()
+    # queries 24 MB + results 256 MB + the tree once
+    assert c > bench.N_QUERIES * (bench.DIM * 8 + bench.K * 16)
+    t = bench.profiled_traffic()
+    assert 0.5 < t / c < 2.0

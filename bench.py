@@ -158,12 +158,15 @@ def scipy_baseline(data, q, k=None, leafsize=None):
         return None
     k = K if k is None else k
     leafsize = LEAFSIZE if leafsize is None else leafsize
-    t0 = time.perf_counter()
-    t = cKDTree(data, leafsize=leafsize)
-    build_s = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    t.query(q, k=k, p=P, workers=-1)
-    query_s = time.perf_counter() - t0
+    try:
+        t0 = time.perf_counter()
+        t = cKDTree(data, leafsize=leafsize)
+        build_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        t.query(q, k=k, p=P, workers=-1)
+        query_s = time.perf_counter() - t0
+    except Exception as e:  # a sanity number only: never fail the bench line over it
+        return {"error": f"{type(e).__name__}: {e}"}
     return {"qps": len(q) / query_s, "build_s": build_s, "workers": os.cpu_count()}
 
 

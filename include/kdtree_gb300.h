@@ -15,7 +15,9 @@
  *    doubles, as the reference's `&[f64]` slices are (src/tree.rs:39-46,
  *    src/query.rs:29-37).
  *  - A tree is immutable once built; concurrent queries on one tree from many
- *    host threads are safe (each call owns its scratch and stream work).
+ *    host threads are safe (each call owns its scratch and stream work),
+ *    except kd_query_device_noalloc, whose calls share one fixed scratch
+ *    array (see there).
  *  - `parallel` is accepted for API parity and has no effect: the GPU path
  *    computes the same result either way, as the reference's serial and rayon
  *    paths do (src/build.rs:345-359).
@@ -134,9 +136,16 @@ int kd_query_device_path(const kd_tree* tree, const double* d_queries, uint64_t 
  *  - every call on a device uses the same array, which keeps the last call's
  *    contents (each call clears what must start at zero): calls whose work
  *    overlaps on the GPU race, so issue them from one stream or serialise them;
- *  - the first call on each device looks up the array's device address (a
- *    one-time set-up with that device current); make that first call before any
- *    stream capture. */
+ *  - the array's device address is looked up once per device, with that
+ *    device current, at the end of the first kd_build / kd_build_device on it
+ *    (which allocates anyway).  That lookup is also when the CUDA runtime
+ *    places the array in device memory if it loads modules lazily (the
+ *    default).  Should that set-up have failed, the first call on the device
+ *    repeats it (and may then allocate the array); make that first call before
+ *    any stream capture;
+ *  - it never runs the tensor-core filter that kd_query_device takes for L2
+ *    at 16 <= ndim <= 128: the CUDA-core traversals it runs instead give the
+ *    same results. */
 int kd_query_device_noalloc(const kd_tree* tree, const double* d_queries, uint64_t n_values, uint64_t k,
                             double p, int has_max_distance, double max_distance, double eps,
                             double* d_out_distances, int64_t* d_out_indices, void* stream);

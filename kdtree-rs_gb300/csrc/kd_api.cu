@@ -389,6 +389,7 @@ int kd_build(const double* data, uint64_t n_values, uint64_t ndim, uint64_t leaf
     free_tree(t);
     return rc;
   }
+  noalloc_prepare(dev);
   *out = t;
   return KD_OK;
 }
@@ -411,6 +412,7 @@ int kd_build_device(const double* d_data, uint64_t n_values, uint64_t ndim, uint
     free_tree(t);
     return rc;
   }
+  noalloc_prepare(dev);
   *out = t;
   return KD_OK;
 }

@@ -35,9 +35,11 @@ struct kd_tree {
   float* tc_tbox = nullptr;       // per 256-point tile: [lo | hi] FP32 enclosure (ndim each)
   uint32_t tc_dpad = 0;
   // Width 16: which exact path the automatic choice measured faster on this
-  // tree (-1 not yet measured, 0 warp-per-query traversal, 1 tensor-core filter).
+  // tree, per batch-size class (index 0: batches below AUTO_LARGE_BATCH
+  // queries, 1: at or above it); -1 not yet measured, 0 warp-per-query
+  // traversal, 1 tensor-core filter.
   std::mutex choice_mutex;
-  int auto_choice = -1;
+  int auto_choice[2] = {-1, -1};
 };
 
 namespace kd {
@@ -116,6 +118,14 @@ struct QueryParams {
 // and qp filled, or the status with its message in *msg.
 int validate_scalars(uint64_t k, double p, int has_max, double max_distance, double eps, QueryParams* qp,
                      std::string* msg);
+
+// Resolve the device address of kd_query_device_noalloc's fixed scratch array
+// on device `dev` (current), which loads the module holding it.  Called at the
+// end of every tree build, whose allocations this one-time set-up joins, so a
+// later kd_query_device_noalloc call on that device allocates nothing even
+// when CUDA loads modules lazily.  Best effort: a failure here is retried (and
+// reported) by the first kd_query_device_noalloc call.
+void noalloc_prepare(int dev);
 
 // Sets bit 0 of *status when any of the n values is not finite.
 __global__ void k_check_finite(const double* v, uint64_t n, uint32_t* status);

@@ -36,9 +36,12 @@ constexpr int MAX_DEVICES = 64;
 std::mutex g_setup_mutex;
 void* g_scratch_addr[MAX_DEVICES] = {};
 
-// Device address of g_noalloc_scratch on the current device.  In host code the
-// symbol is only a host-side stand-in, so the address is looked up once per
-// device (with that device current) and remembered.
+// Device address of g_noalloc_scratch on device `dev` (current).  In host code
+// the symbol is only a host-side stand-in, so the address is looked up once
+// per device (with that device current) and remembered.  The lookup is also
+// what makes the CUDA runtime load this file's module -- and so place the
+// array in device memory -- when modules load lazily (the default), which is
+// why noalloc_prepare runs it during the allocating set-up of a tree.
 int scratch_address(int dev, void** out) {
   if (dev < 0 || dev >= MAX_DEVICES) return fail(KD_ERR_INVALID_ARGUMENT, "device ordinal out of range");
   std::lock_guard<std::mutex> lock(g_setup_mutex);
@@ -51,6 +54,15 @@ int scratch_address(int dev, void** out) {
   *out = g_scratch_addr[dev];
   return KD_OK;
 }
+
+}  // namespace
+
+void noalloc_prepare(int dev) {
+  void* p = nullptr;
+  if (scratch_address(dev, &p) != KD_OK) set_error("");  // retried by the first kd_query_device_noalloc call
+}
+
+namespace {
 
 struct DeviceScope {
   int prev = -1;

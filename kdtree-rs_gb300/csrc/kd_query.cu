@@ -609,15 +609,20 @@ void order_by_landing_leaf(const kd_tree* t, const double* d_queries, uint64_t n
 
 // Width 16 (L2, eps = 0) has two exact paths: the tensor-core filter, which
 // scores whole point tiles, and the warp-per-query traversal, which wins where
-// the tree prunes well.  The first automatic query on a tree times both on
-// a sample of its batch (the first min(n, 16384) queries, written to the
-// caller's outputs -- both paths produce the same values) and the tree keeps
-// the faster for every later call.
+// the tree prunes well.  Which one is faster also depends on the batch size
+// (the tensor-core path needs whole 128-query tiles on every SM), so the
+// choice is kept per batch-size class: the first automatic query of each class
+// on a tree times both on a sample of its batch (the first min(n, 16384)
+// queries, written to the caller's outputs -- both paths produce the same
+// values) and the tree keeps the faster for every later call of that class.
+constexpr uint64_t AUTO_LARGE_BATCH = 32768;
+
 int auto_prefers_tc(kd_tree* t, const double* d_queries, uint64_t nq, const QueryParams& qp, double* d_out_d,
                     int64_t* d_out_i, cudaStream_t st, uint32_t* d_status, bool* tc) {
   std::lock_guard<std::mutex> lock(t->choice_mutex);
-  if (t->auto_choice >= 0) {
-    *tc = t->auto_choice == 1;
+  int& choice = t->auto_choice[nq >= AUTO_LARGE_BATCH ? 1 : 0];
+  if (choice >= 0) {
+    *tc = choice == 1;
     return KD_OK;
   }
   const uint64_t ns = std::min<uint64_t>(nq, 16384);
@@ -640,8 +645,8 @@ int auto_prefers_tc(kd_tree* t, const double* d_queries, uint64_t nq, const Quer
   }
   for (cudaEvent_t x : e) cudaEventDestroy(x);
   if (rc) return rc;
-  t->auto_choice = ms_tc <= ms_pk ? 1 : 0;
-  *tc = t->auto_choice == 1;
+  choice = ms_tc <= ms_pk ? 1 : 0;
+  *tc = choice == 1;
   return KD_OK;
 }
 

@@ -312,11 +312,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
       ok = __shfl_sync(0xffffffffu, ok, 0);
     }
-    if (lane == 0 && *abort_flag) {  // let copies already issued land before the CTA leaves
+    // Leaving early (its own wait ran out, or another role's did): let the
+    // copies already issued land before the CTA leaves.
+    if (lane == 0 && !ok) atomicExch(&s_abort, 1);
+    if (lane == 0 && (!ok || *abort_flag)) {
       for (uint32_t s = 0; s < nst; ++s)
         if (last_use[s]) mbar_wait(smem_u32(&full[s]), (last_use[s] - 1) & 1, &s_zero);
     }
-    if (lane == 0 && !ok) atomicExch(&s_abort, 1);
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {

@@ -43,34 +43,51 @@ def _call(fn, tree, dq, k, p, has_max, max_distance, eps, stream):
 
 
 @pytest.mark.parametrize(
-    "d,k,p,max_distance",
+    "d,k,p,max_distance,n_points",
     [
-        (3, 16, 2.0, None),     # register path: only the status word is scratch
-        (5, 8, 1.0, None),      # dynamic width: CellBound axes live in the scratch
-        (20, 4, np.inf, 1.5),   # Streamed L-inf with padding
+        (3, 16, 2.0, None, 50_000),     # register path: only the status word is scratch
+        (5, 8, 1.0, None, 50_000),      # dynamic width: CellBound axes live in the scratch
+        (20, 4, np.inf, 1.5, 50_000),   # Streamed L-inf with padding
+        (64, 8, 2.0, None, 20_000),     # kd_query_device takes the tensor-core filter here
     ],
 )
-def test_noalloc_matches_allocating_entry_point(d, k, p, max_distance):
+def test_noalloc_matches_allocating_entry_point(d, k, p, max_distance, n_points):
     import torch
 
     from kdtree import KDTree
 
     L, core = _lib()
     rng = np.random.default_rng(100 + d)
-    data = rng.normal(size=(50_000, d))
+    data = rng.normal(size=(n_points, d))
     tree = KDTree(data, leafsize=16)
     stream = torch.cuda.Stream()
     nq = MAX_VALUES // d
     has_max = max_distance is not None
     md = float(max_distance) if has_max else 0.0
-    for call in range(2):  # two calls in a row share the scratch array
+    P = ctypes.c_void_p
+    # two query sets; the allocating entry point's answers first
+    sets = []
+    for call in range(2):
         q = rng.normal(size=(nq - 17 * call, d)) * 1.2
         dq = torch.from_numpy(q).cuda()
         st_ref, ref_d, ref_i = _call(L.kd_query_device, tree, dq, k, p, int(has_max), md, 0.0, stream.cuda_stream)
         assert st_ref == 0, core._last_error()
-        st, got_d, got_i = _call(L.kd_query_device_noalloc, tree, dq, k, p, int(has_max), md, 0.0,
-                                 stream.cuda_stream)
+        out_d = torch.full((dq.shape[0], k), -1.0, dtype=torch.float64, device="cuda")
+        out_i = torch.full((dq.shape[0], k), -1, dtype=torch.int64, device="cuda")
+        sets.append((dq, ref_d, ref_i, out_d, out_i))
+    torch.cuda.synchronize()
+    free_before = None
+    for call, (dq, ref_d, ref_i, out_d, out_i) in enumerate(sets):  # two calls in a row share the scratch
+        if call == 1:
+            free_before = torch.cuda.mem_get_info()[0]
+        st = L.kd_query_device_noalloc(tree._h, P(dq.data_ptr()), dq.numel(), k, p, int(has_max), md, 0.0,
+                                       P(out_d.data_ptr()), P(out_i.data_ptr()), P(stream.cuda_stream))
         assert st == 0, core._last_error()
+        torch.cuda.synchronize()
+        if call == 1:
+            # the second call maps no device memory (its kernels were loaded by the first)
+            assert torch.cuda.mem_get_info()[0] == free_before
+        got_d, got_i = out_d.cpu().numpy(), out_i.cpu().numpy()
         np.testing.assert_array_equal(got_i, ref_i)
         assert np.array_equal(got_d, ref_d), "distances differ from kd_query_device"
 

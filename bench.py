@@ -234,24 +234,24 @@ def run_reference(args):
     threads = kdtree_oracle.max_threads()
     data, q = workload(0)
     t = kdtree_oracle.OracleKDTree(data, leafsize=LEAFSIZE, parallel=True)
-    sample = q[:200_000]
     for _ in range(args.warmup):
-        t.query(sample, k=K, p=P, threads=threads)
+        t.query(q, k=K, p=P, threads=threads)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        t.query(sample, k=K, p=P, threads=threads)
+        t.query(q, k=K, p=P, threads=threads)
         times.append(time.perf_counter() - t0)
-    qps = len(sample) * len(times) / sum(times)
+    qps = len(q) * len(times) / sum(times)
     line = {
         "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (numpy default_rng seeds 2 / 3)",
-        "config": {"workload": WORKLOAD, "sample_queries_per_step": len(sample)},
+        "config": {"workload": WORKLOAD, "n_points": N_POINTS, "queries_per_step": N_QUERIES, "d": DIM, "k": K,
+                   "p": P, "leafsize": LEAFSIZE, "parallelism": "rank 0 only, all host threads"},
         "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
-                         "sample": f"{len(sample)} of the 1,000,000 queries per step (first rows), "
-                                   "oracle restatement of the reference (Rust crate not buildable here)"},
+                         "sample": "every step is the full 1,000,000-query batch; oracle restatement of the "
+                                   "reference (the Rust crate cannot be built here)"},
         "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -641,6 +641,53 @@ def grid_case(lib, torch, stream, dev, cpu_threads):
     return out
 
 
+def _sig(x, n=4):
+    """x rounded to n significant digits (for the compact case summary)."""
+    if isinstance(x, bool) or x is None:
+        return x
+    if isinstance(x, float):
+        return float(f"{x:.{n}g}")
+    return x
+
+
+def compact_cases(cases):
+    """The secondary workloads' headline numbers, short enough to stay inside
+    the last 1,500 characters of the bench output (the full details go to
+    stderr as one JSON line)."""
+    out = {}
+    ps = cases.get("plain_scale")
+    if ps:
+        k1 = [v["qps"] for key, v in ps.items() if isinstance(v, dict) and "-k1-" in key]
+        k16 = [v["qps"] for key, v in ps.items() if isinstance(v, dict) and "-k16-" in key]
+        out["plain_scale"] = {"k1_qps_min_max": [_sig(min(k1), 3), _sig(max(k1), 3)],
+                              "k16_qps_min_max": [_sig(min(k16), 3), _sig(max(k16), 3)],
+                              "build_s": [_sig(ps.get("uniform-build_s"), 3), _sig(ps.get("gmm-build_s"), 3)]}
+    pr = cases.get("precision")
+    if pr:
+        out["precision"] = {d: {k: _sig(v, 3) for k, v in c.items()
+                                if k in ("tc_qps", "plain_qps", "tc_over_plain", "reference_order_qps",
+                                         "cpu_oracle_qps", "identical", "rerank_fraction")}
+                            for d, c in pr.items()}
+    ba = cases.get("batched")
+    if ba:
+        out["batched"] = {"graph_qps": _sig(ba["graph"]["qps"], 3),
+                          "per_tree_qps": _sig(ba["per_tree_launches"]["qps"], 3),
+                          "identical": ba.get("identical_across_modes")}
+    sv = cases.get("serving")
+    if sv:
+        out["serving"] = {"peak_qps": _sig(sv["peak"]["queries_per_s"], 3),
+                          "identical": sv.get("identical_to_lone_queries")}
+        for key in ("load_50", "load_70", "load_90"):
+            if key in sv:
+                out["serving"][key] = {k: _sig(sv[key][k], 3) for k in sv[key]
+                                       if k in ("p50_ms", "p99_ms", "p99_ms_le_10k")}
+    gr = cases.get("grid")
+    if gr:
+        q = [v for key, v in gr.items() if key.startswith("query-") and "cpu_ms" in v]
+        out["grid"] = {"query_cases": len(q), "faster_than_cpu": sum(v["gpu_ms"] < v["cpu_ms"] for v in q)}
+    return out
+
+
 def run_profile_tc():
     """A tensor-core-path case small enough for an ncu capture: one CTA-filling
     batch (152 x 128 queries) against 100,000 points, d=64, k=32."""
@@ -883,7 +930,8 @@ def main():
             t0 = time.perf_counter()
             cases[name] = fn()
             print(f"[bench] case {name}: {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
-        line["cases"] = cases
+        print("[bench] cases " + json.dumps(cases), file=sys.stderr, flush=True)
+        line["cases"] = compact_cases(cases)  # last key: it ends the output
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()

@@ -778,6 +778,85 @@ int ork_query(const ork_tree* t, const double* queries, uint64_t n_values, uint6
 }
 
 /* ------------------------------------------------------------------ */
+/* Brute force: the exact top-k without the descent.                   */
+/* ------------------------------------------------------------------ */
+
+/* For each query, the k smallest (reduced distance, original index) over every
+ * point within max_distance, each point's distance computed exactly as the
+ * reference's leaf scan computes it at its tree position (point_dist with the
+ * Packed d4/d8 chunk flag of its leaf, kernel.rs:441-457), kept by BestK's
+ * order (query.rs:461-481).  This is what the reference's descent returns
+ * when none of its FP64 gates -- the root seed (query.rs:169-194), the
+ * split-plane bound (metric.rs:93-98) and the box distance (kernel.rs:565-616)
+ * -- rounds above the distance of a point it would have kept.  The tests use it
+ * to find inputs where one does (tests/golden/make_adversarial.py).  eps = 0
+ * only; same arguments and outputs as ork_query. */
+int ork_query_brute(const ork_tree* t, const double* queries, uint64_t n_values, uint64_t k, double p,
+                    int has_max_distance, double max_distance, double* out_d, int64_t* out_i) {
+  if (k == 0) return ORK_INVALID_K;
+  if (n_values == 0 || n_values % t->ndim) return ORK_INVALID_SHAPE;
+  if (!has_max_distance) max_distance = INFINITY;
+  metric_t m;
+  if (isinf(p) && p > 0) m.kind = M_LINF;
+  else if (!isfinite(p) || p < 1.0) return ORK_INVALID_METRIC;
+  else if (p == 1.0) m.kind = M_L1;
+  else if (p == 2.0) m.kind = M_L2;
+  else m.kind = M_LP;
+  m.p = p;
+  const size_t d = t->ndim;
+  int strat;
+  if (m.kind != M_LP && d <= 8) strat = S_PACKED;
+  else if ((m.kind == M_L1 || m.kind == M_L2) && d <= 16) strat = S_FOLDED;
+  else strat = S_STREAMED;
+  const double cutoff = m_reduce(m, max_distance);
+  /* the Packed chunk flag of every tree row, from its leaf */
+  uint8_t* in_chunk = (uint8_t*)malloc(t->n_points ? t->n_points : 1);
+  if (!in_chunk) return ORK_OUT_OF_MEMORY;
+  for (uint64_t i = 0; i < t->n_nodes; ++i) {
+    const ork_node* n = t->nodes + i;
+    if (!n->is_leaf) continue;
+    size_t len = n->b - n->a, chunk_pts = len;
+    if (strat == S_PACKED && m.kind != M_LINF) {
+      if (d == 4) chunk_pts = len / 2 * 2;
+      else if (d == 8) chunk_pts = len / 8 * 8;
+    }
+    for (size_t j = 0; j < len; ++j) in_chunk[n->a + j] = j < chunk_pts;
+  }
+  const uint64_t nq = n_values / d;
+  best_t b;
+  b.k = k;
+  b.dists = (double*)malloc(k * sizeof(double));
+  b.ids = (uint32_t*)malloc(k * sizeof(uint32_t));
+  if (!b.dists || !b.ids) {
+    free(in_chunk);
+    free(b.dists);
+    free(b.ids);
+    return ORK_OUT_OF_MEMORY;
+  }
+  for (uint64_t qi = 0; qi < nq; ++qi) {
+    const double* q = queries + qi * d;
+    b.len = 0;
+    for (uint64_t r = 0; r < t->n_points; ++r) {
+      double dist = point_dist(m, strat, q, t->data + r * d, d, in_chunk[r]);
+      if (dist <= best_bound(&b, cutoff)) best_consider(&b, dist, t->indices[r]);
+    }
+    for (size_t j = 0; j < k; ++j) {
+      if (j < b.len) {
+        out_d[qi * k + j] = m_restore(m, b.dists[j]);
+        out_i[qi * k + j] = (int64_t)b.ids[j];
+      } else {
+        out_d[qi * k + j] = INFINITY;
+        out_i[qi * k + j] = (int64_t)t->n_points;
+      }
+    }
+  }
+  free(in_chunk);
+  free(b.dists);
+  free(b.ids);
+  return ORK_OK;
+}
+
+/* ------------------------------------------------------------------ */
 /* Accessors for the tests.                                            */
 /* ------------------------------------------------------------------ */
 void ork_info(const ork_tree* t, uint64_t* n_points, uint64_t* ndim, uint64_t* leafsize, uint64_t* n_nodes) {

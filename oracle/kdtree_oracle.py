@@ -61,6 +61,8 @@ def lib():
         L.ork_query.argtypes = [P, P, u64, u64, ctypes.c_double, ctypes.c_int, ctypes.c_double,
                                 ctypes.c_double, ctypes.c_int, P, P, P]
         L.ork_query.restype = ctypes.c_int
+        L.ork_query_brute.argtypes = [P, P, u64, u64, ctypes.c_double, ctypes.c_int, ctypes.c_double, P, P]
+        L.ork_query_brute.restype = ctypes.c_int
         L.ork_free.argtypes = [P]
         L.ork_info.argtypes = [P, P, P, P, P]
         L.ork_export.argtypes = [P, P, P, P, P, P]
@@ -154,6 +156,24 @@ class OracleKDTree:
         if st:
             raise OracleError(st)
         self.last_counts = tuple(int(c) for c in counts)
+        if single:
+            return out_d[0], out_i[0]
+        return out_d, out_i
+
+    def query_brute(self, x, *, k: int = 1, p: float = 2.0, max_distance=None):
+        """The exact top-k over every point (each distance as the reference's
+        leaf scan computes it), without the descent: the reference's answer
+        unless one of its FP64 gates rounds above a point it would keep."""
+        q, single = _as_points(x, True, "query must be one- or two-dimensional")
+        k = int(k)
+        nq = q.shape[0]
+        out_d = np.empty((nq, k), np.float64)
+        out_i = np.empty((nq, k), np.int64)
+        st = lib().ork_query_brute(self._ptr, _ptr(q), q.size, k, float(p), int(max_distance is not None),
+                                   float(max_distance) if max_distance is not None else 0.0, _ptr(out_d),
+                                   _ptr(out_i))
+        if st:
+            raise OracleError(st)
         if single:
             return out_d[0], out_i[0]
         return out_d, out_i

@@ -131,3 +131,41 @@ def test_valid_cases_cover_every_strategy():
     """The row-width cases span Packed (d<=8), Folded (9..16) and Streamed (17)."""
     dims = {c.data.shape[1] for n, c in valid_cases().items() if n.startswith("row-width")}
     assert dims == set(range(1, 18))
+
+
+def _adversarial():
+    from pathlib import Path
+
+    f = np.load(Path(__file__).parent / "golden" / "adversarial.npz")
+    out = []
+    for i in range(int(f["n_cases"])):
+        leaf, k, p, md = f[f"c{i}_params"]
+        out.append((f[f"c{i}_data"], f[f"c{i}_q"], int(leaf), int(k), float(p),
+                    None if np.isnan(md) else float(md), f[f"c{i}_ref_d"], f[f"c{i}_ref_i"]))
+    return out
+
+
+@pytest.mark.parametrize("case", range(19))
+def test_oracle_adversarial_gate_rounding(oracle, case):
+    """tests/golden/adversarial.npz (make_adversarial.py): the oracle still
+    returns the recorded answer, and the brute-force top-k over every point
+    differs on at least one query -- the reference's descent prunes a point
+    there because one of its FP64 gates rounds above that point's distance."""
+    data, q, leaf, k, p, md, ref_d, ref_i = _adversarial()[case]
+    t = oracle.OracleKDTree(data, leafsize=leaf)
+    got = t.query(q, k=k, p=p, max_distance=md)
+    np.testing.assert_array_equal(got[1], ref_i)
+    assert np.array_equal(got[0], ref_d)
+    bru = t.query_brute(q, k=k, p=p, max_distance=md)
+    assert not (np.array_equal(bru[1], ref_i) and np.array_equal(bru[0], ref_d))
+    # and the difference is a tie or near-tie at the k-th place or the cutoff:
+    # the brute force's extra point sits within 2^-40 (relative) of the
+    # distance the two answers disagree at, of the one before it, or of the cutoff
+    rows = np.nonzero((bru[1] != ref_i).any(1))[0]
+    for r in rows:
+        j = int(np.argmax(bru[1][r] != ref_i[r]))
+        b = bru[0][r][j]
+        near = [x for x in (ref_d[r][j], md if md is not None else np.inf) if np.isfinite(x)]
+        if j > 0:
+            near.append(ref_d[r][j - 1])
+        assert any(abs(b - x) <= 2.0 ** -40 * max(abs(x), 1e-300) for x in near)

@@ -16,7 +16,8 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 OUT = HERE / "_build"
 LIB = OUT / "libkdtree_gb300.so"
-SOURCES = ["kd_api.cu", "kd_build.cu", "kd_query.cu", "kd_query_tc.cu", "kd_noalloc.cu", "kd_batch.cu", "kd_query_packet.cu"]
+SOURCES = ["kd_api.cu", "kd_build.cu", "kd_query.cu", "kd_query_tc.cu", "kd_noalloc.cu", "kd_batch.cu",
+           "kd_query_packet.cu", "kd_query_warp.cu", "kd_query_ref.cu"]
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",

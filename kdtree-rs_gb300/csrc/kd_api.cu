@@ -145,6 +145,7 @@ void free_tree(kd_tree* t) {
   cudaFree(t->indices);
   cudaFree(t->nodes);
   cudaFree(t->boxes);
+  if (t->data32w != t->data32) cudaFree(t->data32w);
   cudaFree(t->data32);
   cudaFree(t->boxes32);
   cudaFree(t->tc_points);
@@ -152,6 +153,7 @@ void free_tree(kd_tree* t) {
   cudaFree(t->tc_v);
   cudaFree(t->tc_centre);
   cudaFree(t->tc_tbox);
+  if (t->tc_ready) cudaEventDestroy(t->tc_ready);
   delete t;
 }
 

@@ -51,7 +51,9 @@ namespace {
 #include "kd_scan.cuh"
 #include "kd_lazy_best.cuh"
 #include "kd_query_packet.cuh"
+#include "kd_warp.cuh"
 #include "kd_query_warp.cuh"
+#include "kd_query_ref.cuh"
 
 constexpr uint32_t CLS_OTHER = 0xffffffffu;
 constexpr uint64_t SORT_MIN_QUERIES = 1024;
@@ -139,7 +141,7 @@ __global__ void k_batch_scatter(const uint32_t* q_start, uint32_t n_jobs, uint32
 
 template <int M, int D, int KS>
 __device__ __forceinline__ void batch_query(const QArgs* a, uint64_t w, WarpStack* stack) {
-  warp_query<M, D, KS>(*a, w, stack);
+  warp_query<M, D, KS>(*a, w, stack, nullptr);
 }
 
 // The persistent kernel: warps take tasks -- TASK_QUERIES consecutive
@@ -180,6 +182,34 @@ __global__ void __launch_bounds__(QUERY_THREADS, W16 ? 5 : 7) k_query_batch(Batc
   }
 }
 
+// Near-tie reruns of the fused kernel's queries (kd_warp.cuh): each entry of
+// `list` is (packet job << 32 | query index); warps run them in the
+// reference's order with that job's arguments.
+template <int M>
+__global__ void __launch_bounds__(QUERY_THREADS) k_batch_rerun(const BatchJob* jobs, const uint32_t* count,
+                                                               const uint64_t* list) {
+  __shared__ RefFrame s_fr[QUERY_THREADS / 32][REF_FRAMES];
+  __shared__ double s_axes[QUERY_THREADS / 32][16];
+  const uint32_t wid = threadIdx.x >> 5;
+  const uint64_t n = *count;
+  const uint64_t warps = static_cast<uint64_t>(gridDim.x) * (QUERY_THREADS / 32);
+  for (uint64_t w = blockIdx.x * static_cast<uint64_t>(QUERY_THREADS / 32) + wid; w < n; w += warps) {
+    const uint64_t e = list[w];
+    const BatchJob* J = jobs + (e >> 32);
+    const uint64_t qi = static_cast<uint32_t>(e);
+    switch (J->cls) {
+      case 0: ref_query<M, 2, 1>(J->a, qi, s_fr[wid], s_axes[wid], nullptr); break;
+      case 1: ref_query<M, 3, 1>(J->a, qi, s_fr[wid], s_axes[wid], nullptr); break;
+      case 2: ref_query<M, 8, 1>(J->a, qi, s_fr[wid], s_axes[wid], nullptr); break;
+      case 3: ref_query<M, 16, 1>(J->a, qi, s_fr[wid], s_axes[wid], nullptr); break;
+      case 4: ref_query<M, 2, 2>(J->a, qi, s_fr[wid], s_axes[wid], nullptr); break;
+      case 5: ref_query<M, 3, 2>(J->a, qi, s_fr[wid], s_axes[wid], nullptr); break;
+      case 6: ref_query<M, 8, 2>(J->a, qi, s_fr[wid], s_axes[wid], nullptr); break;
+      default: ref_query<M, 16, 2>(J->a, qi, s_fr[wid], s_axes[wid], nullptr); break;
+    }
+  }
+}
+
 template <int M, bool W16>
 int max_blocks_per_sm() {
   int n = 0;
@@ -196,9 +226,11 @@ int resident_blocks_per_sm(int metric, bool w16) {
 }
 
 template <int M>
-void launch_batch(bool w16, unsigned blocks, cudaStream_t st, const BatchArgs& a) {
+void launch_batch(bool w16, unsigned blocks, cudaStream_t st, const BatchArgs& a, const uint32_t* rerun_count,
+                  const uint64_t* rerun_list, unsigned rerun_blocks) {
   if (w16) k_query_batch<M, true><<<blocks, QUERY_THREADS, 0, st>>>(a);
   else k_query_batch<M, false><<<blocks, QUERY_THREADS, 0, st>>>(a);
+  k_batch_rerun<M><<<rerun_blocks, QUERY_THREADS, 0, st>>>(a.jobs, rerun_count, rerun_list);
 }
 
 // ---------------------------------------------------------------------------
@@ -230,6 +262,8 @@ void fill_args(QArgs* a, const JobSpec& J, const QueryParams& qp) {
   *a = QArgs{};
   a->data = t->data;
   a->data32 = t->data32;
+  a->data32w = t->data32w;
+  a->w32 = t->w32;
   a->indices = t->indices;
   a->nodes = t->nodes;
   a->boxes = t->boxes;
@@ -250,9 +284,11 @@ void fill_args(QArgs* a, const JobSpec& J, const QueryParams& qp) {
 }
 
 // Lay the jobs out.  `order` is the device batch order (total packet queries
-// u32); sort = false gives every job one bin and no order.
+// u32); sort = false gives every job one bin and no order.  The fused jobs
+// flag their near ties into (rerun_count, rerun_list), tagged with their
+// position in the table.
 void make_layout(const std::vector<JobSpec>& specs, const QueryParams& qp, bool sort, uint32_t* order,
-                 Layout* L) {
+                 uint32_t* rerun_count, uint64_t* rerun_list, Layout* L) {
   *L = Layout{};
   const bool ref = reference_order_forced();
   std::vector<uint32_t> cls(specs.size());
@@ -274,6 +310,9 @@ void make_layout(const std::vector<JobSpec>& specs, const QueryParams& qp, bool 
     const JobSpec& J = specs[L->packet[i]];
     BatchJob& B = L->table[i];
     fill_args(&B.a, J, qp);
+    B.a.rerun_count = rerun_count;
+    B.a.rerun_list = rerun_list;
+    B.a.rerun_tag = static_cast<uint32_t>(i);
     B.cls = cls[L->packet[i]];
     L->wide16 |= B.cls % 4 == 3;
     B.sorted = sort && J.nq >= SORT_MIN_QUERIES;
@@ -299,6 +338,8 @@ struct Buffers {
   uint32_t* bins = nullptr;
   uint32_t* tile_sums = nullptr;
   uint32_t* counter = nullptr;
+  uint32_t* rerun_count = nullptr;  // near ties of the fused kernel
+  uint64_t* rerun_list = nullptr;   // cap_q entries
   uint64_t cap_jobs = 0, cap_q = 0, cap_bins = 0;
   ~Buffers() {
     if (mem) cudaFree(mem);
@@ -316,7 +357,8 @@ int alloc_buffers(Buffers* B, uint64_t cap_jobs, uint64_t cap_q, uint64_t cap_bi
   const uint64_t sz_jobs = round256(cap_jobs * sizeof(BatchJob));
   const uint64_t sz_st = round256((cap_jobs + 1) * sizeof(uint32_t));
   const uint64_t total = 2 * sz_jobs + 2 * sz_st + round256(cap_q * 8) + round256(cap_q * 4) +
-                         round256(cap_bins * 4) + round256(n_tiles * 4) + 256 + round256(extra);
+                         round256(cap_bins * 4) + round256(n_tiles * 4) + 256 + round256(cap_q * 8) +
+                         round256(extra);
   cudaError_t e = cudaMalloc(&B->mem, total);
   if (e != cudaSuccess) {
     B->mem = nullptr;
@@ -337,6 +379,8 @@ int alloc_buffers(Buffers* B, uint64_t cap_jobs, uint64_t cap_q, uint64_t cap_bi
   B->bins = reinterpret_cast<uint32_t*>(take(round256(cap_bins * 4)));
   B->tile_sums = reinterpret_cast<uint32_t*>(take(round256(n_tiles * 4)));
   B->counter = reinterpret_cast<uint32_t*>(take(256));
+  B->rerun_count = B->counter + 32;  // same 256-byte block, its own 128 bytes
+  B->rerun_list = reinterpret_cast<uint64_t*>(take(round256(cap_q * 8)));
   if (extra_p) *extra_p = take(round256(extra));
   B->cap_jobs = cap_jobs;
   B->cap_q = cap_q;
@@ -358,12 +402,14 @@ int enqueue_packet(const Layout& L, const Buffers& B, int table, int metric, uns
   k_scan_add<<<static_cast<unsigned>((L.n_bins + 255) / 256), 256, 0, st>>>(B.bins, L.n_bins, B.tile_sums);
   k_batch_scatter<<<qb, 256, 0, st>>>(B.q_start, n, L.total_q, B.bin_of, B.bins, B.order);
   KD_TRY_CUDA(cudaGetLastError());
-  KD_TRY_CUDA(cudaMemsetAsync(B.counter, 0, sizeof(uint32_t), st));
+  KD_TRY_CUDA(cudaMemsetAsync(B.counter, 0, 256, st));  // task counter and rerun count
   BatchArgs a{B.jobs[table], B.task_start, n, L.n_tasks, B.counter};
+  // the reruns: a few warps an SM at most (their count is only known on the device)
+  const unsigned rerun_blocks = std::max(1u, std::min(blocks, (L.total_q + 3) / 4));
   switch (metric) {
-    case M_L1: launch_batch<M_L1>(L.wide16, blocks, st, a); break;
-    case M_L2: launch_batch<M_L2>(L.wide16, blocks, st, a); break;
-    default: launch_batch<M_LINF>(L.wide16, blocks, st, a); break;
+    case M_L1: launch_batch<M_L1>(L.wide16, blocks, st, a, B.rerun_count, B.rerun_list, rerun_blocks); break;
+    case M_L2: launch_batch<M_L2>(L.wide16, blocks, st, a, B.rerun_count, B.rerun_list, rerun_blocks); break;
+    default: launch_batch<M_LINF>(L.wide16, blocks, st, a, B.rerun_count, B.rerun_list, rerun_blocks); break;
   }
   KD_TRY_CUDA(cudaGetLastError());
   return KD_OK;
@@ -417,10 +463,12 @@ void join_others(SideStreams& ss, size_t n_other, cudaStream_t st) {
 
 // Per-job launches of `other` on the side streams, forked from st (join them
 // with join_others once st's own work is enqueued).  scratch != NULL: the
-// allocation-free kernels with that CellBound scratch (offsets axes_off), as a
+// allocation-free kernels with that scratch (byte offsets scratch_off, see
+// query_on_device_scratch) and one rerun counter per job (counters), as a
 // graph capture needs.
 int enqueue_others(const std::vector<JobSpec>& specs, const std::vector<uint32_t>& other, const QueryParams& base,
-                   SideStreams& ss, cudaStream_t st, double* scratch, const std::vector<uint64_t>& axes_off) {
+                   SideStreams& ss, cudaStream_t st, unsigned char* scratch, const std::vector<uint64_t>& scratch_off,
+                   uint32_t* counters) {
   if (other.empty()) return KD_OK;
   const int used = static_cast<int>(std::min<size_t>(SideStreams::N, other.size()));
   KD_TRY_CUDA(cudaEventRecord(ss.fork, st));
@@ -433,7 +481,7 @@ int enqueue_others(const std::vector<JobSpec>& specs, const std::vector<uint32_t
     qp.path = PATH_PACKET;  // never the tensor-core filter inside a batch
     cudaStream_t side = ss.s[o % SideStreams::N];
     rc = scratch ? query_on_device_scratch(J.tree, J.queries, J.nq, qp, J.out_d, J.out_i, side, J.status,
-                                           scratch + axes_off[o])
+                                           scratch + scratch_off[o], counters + o)
                  : query_on_device(J.tree, J.queries, J.nq, qp, J.out_d, J.out_i, side, J.status);
   }
   if (rc) join_others(ss, other.size(), st);  // nothing is left behind on a failure
@@ -467,8 +515,9 @@ struct kd_batch {
   Layout layout[2];            // [0] sorted, [1] unsorted (same jobs and positions)
   Buffers buf;
   uint32_t* status = nullptr;
-  double* axes = nullptr;              // other jobs' CellBound scratch
-  std::vector<uint64_t> axes_off;      // per other job (layout order)
+  unsigned char* scratch = nullptr;    // other jobs' scratch (query_on_device_scratch)
+  std::vector<uint64_t> scratch_off;   // per other job (layout order), bytes
+  uint32_t* counters = nullptr;        // per other job: its near-tie rerun count
   bool tuned = false;
   unsigned blocks = 0;
   int table = 0;
@@ -492,7 +541,7 @@ int enqueue_plan(kd_batch* b, cudaStream_t st, bool per_job, unsigned blocks, in
     }
     return KD_OK;
   }
-  int rc = enqueue_others(b->specs, L.other, b->qp, b->side, st, b->axes, b->axes_off);
+  int rc = enqueue_others(b->specs, L.other, b->qp, b->side, st, b->scratch, b->scratch_off, b->counters);
   if (rc) return rc;
   rc = enqueue_packet(L, b->buf, table, b->qp.metric, blocks, st);
   join_others(b->side, L.other.size(), st);
@@ -663,7 +712,7 @@ int stage_batch(kd_server* s, Slot* sl) {
   }
   KD_TRY_CUDA(cudaMemsetAsync(sl->status, 0, n * sizeof(uint32_t), st));
   Layout L;
-  make_layout(specs, s->qp, true, sl->buf.order, &L);
+  make_layout(specs, s->qp, true, sl->buf.order, sl->buf.rerun_count, sl->buf.rerun_list, &L);
   char* h = static_cast<char*>(sl->host);
   BatchJob* h_jobs = reinterpret_cast<BatchJob*>(h);
   uint32_t* h_qs = reinterpret_cast<uint32_t*>(h + round256(s->cap_jobs * sizeof(BatchJob)));
@@ -678,7 +727,7 @@ int stage_batch(kd_server* s, Slot* sl) {
     KD_TRY_CUDA(cudaMemcpyAsync(sl->buf.task_start, h_ts, (np + 1) * 4, cudaMemcpyHostToDevice, st));
   }
   // the per-job launches fork first, so they run beside the fused kernel
-  int rc = enqueue_others(specs, L.other, s->qp, sl->side, st, nullptr, {});
+  int rc = enqueue_others(specs, L.other, s->qp, sl->side, st, nullptr, {}, nullptr);
   if (rc) return rc;
   if (np) {
     const unsigned blocks = static_cast<unsigned>(s->sms * resident_blocks_per_sm(s->qp.metric, L.wide16));
@@ -835,32 +884,34 @@ int kd_batch_create(const kd_batch_job* jobs, uint64_t n_jobs, double p, int has
   b->device = dev;
   b->qp = qp;
   cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
-  uint64_t total_q = 0, axes_words = 0, bins = 0;
+  uint64_t total_q = 0, scratch_bytes = 0, bins = 0;
   for (uint64_t j = 0; j < n_jobs; ++j) {
     const kd_batch_job& J = jobs[j];
     b->specs.push_back(JobSpec{J.tree, J.d_queries, J.n_queries, J.k, J.d_out_distances, J.d_out_indices, nullptr});
     total_q += J.n_queries;
     bins += J.tree->n_nodes;
-    axes_words += J.n_queries * J.tree->ndim;
+    scratch_bytes += round256(query_scratch_bytes(J.n_queries, J.tree->ndim));
   }
   if (total_q >= 0xffffffffull) {
     delete b;
     return fail(KD_ERR_INVALID_ARGUMENT, "a batch holds at most 2^32 - 1 queries");
   }
   char* extra = nullptr;
-  if ((rc = alloc_buffers(&b->buf, n_jobs, total_q, bins, 256 + axes_words * sizeof(double), &extra))) {
+  const uint64_t counter_bytes = round256(n_jobs * sizeof(uint32_t));
+  if ((rc = alloc_buffers(&b->buf, n_jobs, total_q, bins, 256 + counter_bytes + scratch_bytes, &extra))) {
     delete b;
     return rc;
   }
   b->status = reinterpret_cast<uint32_t*>(extra);
-  b->axes = reinterpret_cast<double*>(extra + 256);
+  b->counters = reinterpret_cast<uint32_t*>(extra + 256);
+  b->scratch = reinterpret_cast<unsigned char*>(extra + 256 + counter_bytes);
   for (JobSpec& J : b->specs) J.status = b->status;
-  make_layout(b->specs, qp, true, b->buf.order, &b->layout[0]);
-  make_layout(b->specs, qp, false, b->buf.order, &b->layout[1]);
+  make_layout(b->specs, qp, true, b->buf.order, b->buf.rerun_count, b->buf.rerun_list, &b->layout[0]);
+  make_layout(b->specs, qp, false, b->buf.order, b->buf.rerun_count, b->buf.rerun_list, &b->layout[1]);
   uint64_t off = 0;
   for (uint32_t j : b->layout[0].other) {
-    b->axes_off.push_back(off);
-    off += b->specs[j].nq * b->specs[j].tree->ndim;
+    b->scratch_off.push_back(off);
+    off += round256(query_scratch_bytes(b->specs[j].nq, b->specs[j].tree->ndim));
   }
   const Layout& L = b->layout[0];
   const size_t np = L.packet.size();

@@ -838,6 +838,15 @@ __global__ void k_make_f32(const double* data, float* data32, uint64_t n_el, con
   }
 }
 
+// Rows of `d` floats copied to rows of `w` (>= d) floats, zero padded: the
+// runtime-width warp kernels load every row as whole float4 vectors.
+__global__ void k_pad_rows(const float* src, uint64_t n, uint64_t d, uint64_t w, float* dst) {
+  const uint64_t f = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  if (f >= n * w) return;
+  const uint64_t r = f / w, j = f - r * w;
+  dst[f] = j < d ? src[r * d + j] : 0.f;
+}
+
 struct DevBuf {
   void* p = nullptr;
   ~DevBuf() {
@@ -1043,6 +1052,20 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
   nodes.p = nullptr;
   t->boxes = reinterpret_cast<double*>(boxes.p);
   boxes.p = nullptr;
+  // FP32 rows padded for the runtime-width warp kernels (widths other than 1,
+  // 2, 3, 4, 8, 16, up to 128): the FP32 copy itself when d is a multiple of 4
+  t->w32 = static_cast<uint32_t>((d + 3) / 4 * 4);
+  if (warp_runtime_width(d) && t->w32 != d) {
+    DevBuf padded;
+    if ((rc = dalloc<float>(padded, n * t->w32))) return rc;
+    k_pad_rows<<<grid1(n * t->w32, 256), 256, 0, st>>>(static_cast<const float*>(data32.p), n, d, t->w32,
+                                                       static_cast<float*>(padded.p));
+    KD_TRY_CUDA(cudaGetLastError());
+    t->data32w = static_cast<float*>(padded.p);
+    padded.p = nullptr;
+  } else {
+    t->data32w = static_cast<float*>(data32.p);
+  }
   t->data32 = static_cast<float*>(data32.p);
   data32.p = nullptr;
   t->boxes32 = static_cast<float*>(boxes32.p);

@@ -25,6 +25,11 @@ struct kd_tree {
   float* data32 = nullptr;      // n_points * ndim, round-to-nearest FP32 copy (filters)
   float* boxes32 = nullptr;     // n_nodes * 2 * ndim, [lo rounded down | hi rounded up]
   float coord_max32 = 0.f;      // FP32 upper bound of every |coordinate| (the root box)
+  // FP32 rows padded to w32 = ndim rounded up to a multiple of 4 floats, for
+  // the runtime-width warp kernels (made by the build; data32 itself when
+  // ndim is a multiple of 4 or the width has compile-time kernels).
+  float* data32w = nullptr;
+  uint32_t w32 = 0;
   // Tensor-core filter inputs, made on first use (guarded by tc_mutex):
   // centred BF16 rows padded to tc_dpad, and the per-point filter terms.
   std::mutex tc_mutex;
@@ -34,6 +39,7 @@ struct kd_tree {
   double* tc_centre = nullptr;    // ndim, the root box centre
   float* tc_tbox = nullptr;       // per 256-point tile: [lo | hi] FP32 enclosure (ndim each)
   uint32_t tc_dpad = 0;
+  cudaEvent_t tc_ready = nullptr;  // recorded after the kernels that fill them; later users wait on it
   // Width 16: which exact path the automatic choice measured faster on this
   // tree, per batch-size class (index 0: batches below AUTO_LARGE_BATCH
   // queries, 1: at or above it); -1 not yet measured, 0 warp-per-query
@@ -43,6 +49,12 @@ struct kd_tree {
 };
 
 namespace kd {
+
+// Widths the warp kernels take: compile-time kernels for 1, 2, 3, 4, 8 and 16,
+// the runtime-width kernel (padded FP32 rows) for the others up to 128.
+constexpr uint64_t WARP_MAX_WIDTH = 128;
+inline bool warp_static_width(uint64_t d) { return d == 1 || d == 2 || d == 3 || d == 4 || d == 8 || d == 16; }
+inline bool warp_runtime_width(uint64_t d) { return d >= 1 && d <= WARP_MAX_WIDTH && !warp_static_width(d); }
 
 // Launch arguments of the query kernels (every query translation unit).
 constexpr uint32_t NO_ID = 0xffffffffu;
@@ -64,6 +76,14 @@ struct QArgs {
   uint32_t* status;       // bit 0: non-finite query
   const uint32_t* order;  // optional: thread t runs query order[t] (spatially sorted)
   const uint32_t* leaf_of;  // optional: landing leaf node of each query (by query index)
+  const float* data32w;   // FP32 rows padded to w32 floats (runtime-width warp kernels)
+  uint32_t w32;
+  // Near ties (eps = 0 kernels outside the reference's visiting order): the
+  // query gets (rerun_tag << 32 | query index) appended to rerun_list; NULL
+  // rerun_count: no tracking.
+  uint32_t* rerun_count;
+  uint64_t* rerun_list;
+  uint32_t rerun_tag;
   bool reference_order;   // run the reference-order descent even where eps = 0
   uint64_t nq;
   uint64_t d;
@@ -107,6 +127,7 @@ enum QueryPath : int { PATH_AUTO = 0, PATH_REFERENCE_ORDER = 1, PATH_PACKET = 2,
 
 struct QueryParams {
   int path = PATH_AUTO;
+  bool no_sync = false;  // stream-ordered call (kd_query_async): no host waits, no timing on first use
   int metric;         // MetricKind
   double p;           // exponent (LP only)
   double cutoff;      // reduce(max_distance), -0 normalised to +0
@@ -130,17 +151,27 @@ void noalloc_prepare(int dev);
 // Sets bit 0 of *status when any of the n values is not finite.
 __global__ void k_check_finite(const double* v, uint64_t n, uint32_t* status);
 
+// The launch arguments of a query on tree t: no order, no scratch, no rerun list.
+QArgs query_args(const kd_tree* t, const double* d_queries, uint64_t n_queries, const QueryParams& qp,
+                 double* d_out_d, int64_t* d_out_i, uint32_t* d_status);
+
 // Run the query on device buffers; `d_status` is a device word the kernels set
 // when a query is non-finite.  Work is ordered on `stream`.
 int query_on_device(const kd_tree* t, const double* d_queries, uint64_t n_queries,
                     const QueryParams& qp, double* d_out_d, int64_t* d_out_i,
                     cudaStream_t stream, uint32_t* d_status, unsigned long long* d_survivors = nullptr);
 
-// Same as query_on_device with the dynamic-width CellBound scratch supplied by
-// the caller (n_queries * ndim doubles); allocates nothing.
+// Same as query_on_device with the scratch supplied by the caller; allocates
+// nothing and does not sort the batch.  `d_scratch` serves (one at a time)
+// as the dynamic-width CellBound scratch of the one-thread reference-order
+// kernels (n_queries * ndim doubles) or as the near-tie rerun list of the
+// eps = 0 fast paths (n_queries u64); `d_rerun_count` is one u32.
 int query_on_device_scratch(const kd_tree* t, const double* d_queries, uint64_t n_queries,
                             const QueryParams& qp, double* d_out_d, int64_t* d_out_i,
-                            cudaStream_t stream, uint32_t* d_status, double* d_axes_scratch);
+                            cudaStream_t stream, uint32_t* d_status, void* d_scratch, uint32_t* d_rerun_count);
+
+// Bytes query_on_device_scratch's d_scratch must hold for n_queries of width ndim.
+uint64_t query_scratch_bytes(uint64_t n_queries, uint64_t ndim);
 
 // Whether the query kernels that query_on_device would run for these
 // parameters write each query's result row as whole contiguous segments (so
@@ -158,10 +189,19 @@ void order_by_landing_leaf(const kd_tree* t, const double* d_queries, uint64_t n
 // L-inf, widths 2, 3, 8, 16): whether it covers a query, and its launch.
 bool packet_applicable(uint64_t d, int metric, uint64_t k, uint64_t n_points, bool use_eps);
 int launch_packet_query(const QArgs& a, int metric, cudaStream_t stream);
-// One warp per query (the same envelope, k <= 64): for trees whose queries
-// scan many leaf rows.
+// One warp per query, best-first (eps = 0, L1 / L2 / L-inf, widths up to
+// 128, k <= 64): for queries that scan many leaf rows, and every width the
+// packet traversal lacks.  Flags near ties when a.rerun_count is set.
 bool warp_applicable(uint64_t d, int metric, uint64_t k, uint64_t n_points, bool use_eps);
 int launch_warp_query(const QArgs& a, int metric, cudaStream_t stream);
+
+// The reference's own descent with one warp per query (any eps, every
+// metric, widths up to 128, k <= 64): a.nq queries (a.order when set), or the
+// `count` queries of `list` (a near-tie rerun; low 32 bits of each entry: the
+// query index).
+bool ref_warp_applicable(uint64_t d, uint64_t k, uint64_t n_points);
+int launch_ref_query(const QArgs& a, int metric, cudaStream_t stream);
+int launch_rerun(const QArgs& a, int metric, cudaStream_t stream, const uint32_t* count, const uint64_t* list);
 
 // Exact k-NN through the tensor-core filter (L2, eps = 0, 16 <= d <= 128,
 // k <= 32).  Returns KD_OK, or KD_ERR_INVALID_ARGUMENT without doing anything

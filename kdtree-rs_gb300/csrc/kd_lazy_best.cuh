@@ -222,6 +222,7 @@ struct LazySet {
   float second_hi;   // largest hi among the other slots
   float b_lo, b_hi;  // enclosure of the pruning bound min(k-th best, cutoff)
   float cut_lo, cut_hi;
+  float runner;      // FP32 lower bound of every point dropped within max_distance (near-tie test)
   uint64_t cut_bits;
   QMem<D> q;
   const double* data;
@@ -237,6 +238,7 @@ struct LazySet {
       row[j] = ROW_NONE;
     }
     chunk = 0;
+    runner = __int_as_float(0x7f800000);
     n_empty = static_cast<uint32_t>(k);
     cut_bits = dbits(cutoff);
     cut_lo = mag_dn32(cut_bits);
@@ -338,8 +340,11 @@ struct LazySet {
     if (n_empty == 0) {
       const float wlo = slot_lo(worst), whi = slot_hi(worst);
       const bool definite = second_hi < wlo;  // no other enclosure reaches the worst's
-      if (definite && clo > whi) return;      // after the worst: not kept
-      if (chi < max_lo) {                     // before the worst, whichever slot it is
+      if (definite && clo > whi) {            // after the worst: not kept
+        note(clo);
+        return;
+      }
+      if (chi < max_lo) {  // before the worst, whichever slot it is
         if (!definite) {
           double wx;
           uint32_t wid;
@@ -351,10 +356,14 @@ struct LazySet {
         resolve_worst(&wx, &wid);
         if (!have_x) cx = exact_of(r, in_chunk);
         const uint32_t cid = indices[r];
-        if (!(dbits(cx) < dbits(wx) || (dbits(cx) == dbits(wx) && cid < wid))) return;
+        if (!(dbits(cx) < dbits(wx) || (dbits(cx) == dbits(wx) && cid < wid))) {
+          note(mag_dn32(dbits(cx)));
+          return;
+        }
         clo = mag_dn32(dbits(cx));
         chi = mag_up32(dbits(cx));
       }
+      note(slot_lo(worst));  // the worst drops out
     } else {
       --n_empty;
     }
@@ -366,15 +375,20 @@ struct LazySet {
       hi[j] = m ? chi : hi[j];
       row[j] = m ? r : row[j];
     }
-    if (D == 8) chunk = (chunk & ~(1u << w)) | (static_cast<uint32_t>(in_chunk) << w);
+    if (D == 4 || D == 8) chunk = (chunk & ~(1u << w)) | (static_cast<uint32_t>(in_chunk) << w);
     rescan();
   }
+  __device__ __forceinline__ void note(float x) { runner = fminf(runner, x); }
 
   // write_results (query.rs:421-429, 483-493): the exact values sorted by
-  // (distance, index); empty slots after every real one.
-  __device__ __forceinline__ void write(double* od, int64_t* oi, uint64_t k, uint64_t n_points) const {
+  // (distance, index); empty slots after every real one.  Returns whether
+  // the query is a near tie (kd_warp.cuh: the reference's descent may leave
+  // out a point of this set; the caller reruns it in the reference's order).
+  __device__ __forceinline__ bool write(double* od, int64_t* oi, uint64_t k, uint64_t n_points) const {
     uint64_t xb[K];
     uint32_t id[K];
+    uint64_t dmax = 0;
+    bool any = false;
 #pragma unroll
     for (int j = 0; j < K; ++j) {
       if (static_cast<uint64_t>(j) < K - k) {  // placeholder: sorts first
@@ -384,7 +398,10 @@ struct LazySet {
         xb[j] = ~0ull;
         id[j] = NO_ID;
       } else {
-        xb[j] = dbits(exact_of(row[j], (chunk >> j) & 1u)) + 1;
+        const uint64_t x = dbits(exact_of(row[j], (chunk >> j) & 1u));
+        dmax = x > dmax ? x : dmax;
+        any = true;
+        xb[j] = x + 1;
         id[j] = indices[row[j]];
       }
     }
@@ -414,6 +431,9 @@ struct LazySet {
         }
       }
     }
+    if (!any) return false;
+    const float g = fmaxf(__fmul_ru(mag_up32(dmax), UB_GROW), 1.17549435e-38f);
+    return runner <= g || cut_lo <= g;
   }
 };
 
@@ -445,6 +465,7 @@ struct LazyHeap {
   uint32_t n, k;
   float b_hi;  // upper bound of the pruning bound min(k-th best, cutoff)
   float cut_lo, cut_hi;
+  float runner;  // FP32 lower bound of every point dropped within max_distance (near-tie test)
   uint64_t cut_bits;
   QMem<D> q;
   const double* data;
@@ -464,7 +485,9 @@ struct LazyHeap {
     data = data_;
     indices = indices_;
     b_hi = cut_hi;
+    runner = __int_as_float(0x7f800000);
   }
+  __device__ __forceinline__ void note(float x) { runner = fminf(runner, x); }
   static __device__ __forceinline__ float tag(float l, bool in_chunk) {
     return __uint_as_float(__float_as_uint(l) | (static_cast<uint32_t>(in_chunk) << 31));
   }
@@ -524,12 +547,16 @@ struct LazyHeap {
       return;
     }
     const float rh = hi[0];
-    if (clo > rh) return;
+    if (clo > rh) {
+      note(clo);
+      return;
+    }
     const float rl = fabsf(lo[0]);
     float sec = __int_as_float(0xff800000);
     if (n > 1) sec = hi[S];
     if (n > 2) sec = fmaxf(sec, hi[2 * S]);
     if (chi < rl && sec < rl) {
+      note(rl);  // the root drops out
       sift_down(0, tag(clo, in_chunk), chi, r);
       refresh();
       return;
@@ -569,7 +596,12 @@ struct LazyHeap {
       }
     }
     const uint64_t cb = dbits(cx);
-    if (cb < wb || (cb == wb && cid < wid)) put(wj, tag(mag_dn32(cb), in_chunk), mag_up32(cb), r);
+    if (cb < wb || (cb == wb && cid < wid)) {
+      note(mag_dn32(wb));  // the worst drops out
+      put(wj, tag(mag_dn32(cb), in_chunk), mag_up32(cb), r);
+    } else {
+      note(mag_dn32(cb));
+    }
     for (uint32_t j = n / 2; j-- > 0;) sift_down(j, lo[j * S], hi[j * S], row[j * S]);
     refresh();
   }
@@ -619,6 +651,13 @@ struct LazyHeap {
       swap_slots(0, m - 1);
       sift_exact(0, m - 1);
     }
+  }
+  // After sort_exact: whether the query is a near tie (kd_warp.cuh: the
+  // reference's descent may leave out a point of this set).
+  __device__ __forceinline__ bool near_tie() const {
+    if (n == 0) return false;
+    const float g = fmaxf(__fmul_ru(mag_up32(key_at(n - 1)), UB_GROW), 1.17549435e-38f);
+    return runner <= g || cut_lo <= g;
   }
   // The whole warp writes its lanes' results, one query row at a time, lane j
   // storing element j: every row of distances (and of indices) goes out as
@@ -678,11 +717,14 @@ struct LazySetDyn {
   float max_lo, second_hi;
   float b_lo, b_hi;
   float cut_lo, cut_hi;
+  float runner;  // FP32 lower bound of every point dropped within max_distance (near-tie test)
   uint64_t cut_bits;
   DynPoint pt;
   const uint32_t* indices;
 
+  __device__ __forceinline__ void note(float x) { runner = fminf(runner, x); }
   __device__ __forceinline__ void init(uint64_t k, double cutoff, DynPoint p, const uint32_t* indices_) {
+    runner = __int_as_float(0x7f800000);
 #pragma unroll
     for (int j = 0; j < K; ++j) {
       const bool pad = static_cast<uint64_t>(j) < K - k;
@@ -769,7 +811,10 @@ struct LazySetDyn {
     if (n_empty == 0) {
       const float wlo = slot_lo(worst), whi = slot_hi(worst);
       const bool definite = second_hi < wlo;
-      if (definite && clo > whi) return;
+      if (definite && clo > whi) {
+        note(clo);
+        return;
+      }
       if (chi < max_lo) {
         if (!definite) {
           double wx;
@@ -782,10 +827,14 @@ struct LazySetDyn {
         resolve_worst(&wx, &wid);
         if (!have_x) cx = pt.exact(r);
         const uint32_t cid = indices[r];
-        if (!(dbits(cx) < dbits(wx) || (dbits(cx) == dbits(wx) && cid < wid))) return;
+        if (!(dbits(cx) < dbits(wx) || (dbits(cx) == dbits(wx) && cid < wid))) {
+          note(mag_dn32(dbits(cx)));
+          return;
+        }
         clo = mag_dn32(dbits(cx));
         chi = mag_up32(dbits(cx));
       }
+      note(slot_lo(worst));  // the worst drops out
     } else {
       --n_empty;
     }
@@ -799,10 +848,13 @@ struct LazySetDyn {
     }
     rescan();
   }
-  // exact values of the k best, sorted by (distance, index), written out
-  __device__ void write(double* od, int64_t* oi, uint64_t k, uint64_t n_points) const {
+  // exact values of the k best, sorted by (distance, index), written out;
+  // returns whether the query is a near tie (kd_warp.cuh).
+  __device__ bool write(double* od, int64_t* oi, uint64_t k, uint64_t n_points) const {
     uint64_t xb[K];
     uint32_t id[K];
+    uint64_t dmax = 0;
+    bool any = false;
 #pragma unroll
     for (int j = 0; j < K; ++j) {
       if (static_cast<uint64_t>(j) < K - k) {
@@ -812,7 +864,10 @@ struct LazySetDyn {
         xb[j] = ~0ull;
         id[j] = NO_ID;
       } else {
-        xb[j] = dbits(pt.exact(row[j])) + 1;
+        const uint64_t x = dbits(pt.exact(row[j]));
+        dmax = x > dmax ? x : dmax;
+        any = true;
+        xb[j] = x + 1;
         id[j] = indices[row[j]];
       }
     }
@@ -840,5 +895,8 @@ struct LazySetDyn {
         }
       }
     }
+    if (!any) return false;
+    const float g = fmaxf(__fmul_ru(mag_up32(dmax), UB_GROW), 1.17549435e-38f);
+    return runner <= g || cut_lo <= g;
   }
 };

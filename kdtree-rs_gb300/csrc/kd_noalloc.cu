@@ -12,9 +12,11 @@
 //
 // The array (KD_NOALLOC_SCRATCH_BYTES = 4 MiB) is part of the loaded module:
 // every GPU that loads the library holds it until the process exits.  Its
-// layout: bytes [0, 256) the status word, then up to KD_NOALLOC_MAX_VALUES
-// doubles of CellBound scratch -- which is why a call takes at most
-// KD_NOALLOC_MAX_VALUES = n_queries * ndim query values.
+// layout: bytes [0, 4) the status word, [128, 132) the count of near-tie
+// reruns, then KD_NOALLOC_MAX_VALUES doubles used either as the one-thread
+// kernels' CellBound scratch (n_queries * ndim doubles) or as the near-tie
+// rerun list (n_queries entries) -- never both in one call -- which is why a
+// call takes at most KD_NOALLOC_MAX_VALUES = n_queries * ndim query values.
 #include <cmath>
 #include <mutex>
 #include <string>
@@ -104,7 +106,8 @@ extern "C" int kd_query_device_noalloc(const kd_tree* tree, const double* d_quer
   int rc = scratch_address(tree->device, &base);
   if (rc) return rc;
   uint32_t* d_status = static_cast<uint32_t*>(base);
-  double* d_axes = reinterpret_cast<double*>(static_cast<unsigned char*>(base) + NOALLOC_STATUS_BYTES);
+  uint32_t* d_rerun_count = d_status + 32;
+  void* d_scratch = static_cast<unsigned char*>(base) + NOALLOC_STATUS_BYTES;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
 
   // The status word still holds the previous call's value: clear it first.
@@ -120,7 +123,8 @@ extern "C" int kd_query_device_noalloc(const kd_tree* tree, const double* d_quer
     return fail(scalar, msg);
   }
   const uint64_t nq = n_values / tree->ndim;
-  if ((rc = query_on_device_scratch(tree, d_queries, nq, qp, d_out_distances, d_out_indices, st, d_status, d_axes)))
+  if ((rc = query_on_device_scratch(tree, d_queries, nq, qp, d_out_distances, d_out_indices, st, d_status, d_scratch,
+                                    d_rerun_count)))
     return rc;
   KD_TRY_CUDA(cudaMemcpyAsync(&h_status, d_status, sizeof h_status, cudaMemcpyDeviceToHost, st));
   KD_TRY_CUDA(cudaStreamSynchronize(st));

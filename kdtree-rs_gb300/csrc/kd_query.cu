@@ -510,14 +510,13 @@ int dispatch_d(const QArgs& a, cudaStream_t st) {
   return dispatch_k<M, 0>(a, st);
 }
 
-// The packet traversal where it applies (eps = 0, not forced to the reference
-// order), else the reference-order kernels.
 // The automatic choice between the two eps = 0 traversals, from measurements on
 // GB300 (uniform and clustered data, N = 1M): one warp per query wins at
 // d >= 8, for k > 16, for k >= 8 below a few hundred thousand queries, and for
 // any k on small batches (the packet traversal's 32-query warps have long
 // serial chains, which only a large batch hides); the packet traversal wins for
-// small k on big batches.
+// small k on big batches.  Widths the packet traversal lacks always take the
+// warp.
 bool warp_preferred(const QArgs& a) {
   return a.d >= 8 || a.k > 16 || (a.k >= 8 && a.nq < 400000) || a.nq < 32768;
 }
@@ -564,14 +563,30 @@ struct KernelTimer {
   }
 };
 
+// Launch the query kernels for `a`.  eps = 0 (and not forced to the reference
+// order): the packet or warp traversal, then -- when a.rerun_count is set --
+// the reference-order rerun of the near ties they flag (that count is zeroed
+// here first).  Otherwise the reference-order warp kernel, or for k > 64 or
+// widths above 128 the one-thread reference-order kernels.
 int run_kernels(const QArgs& a, int metric, cudaStream_t st, int path) {
   KernelTimer timer(st);
-  if (!a.reference_order && !force_reference_order()) {
-    if ((path == PATH_WARP || (path == PATH_AUTO && warp_preferred(a))) &&
-        warp_applicable(a.d, metric, a.k, a.n_points, a.use_eps != 0))
-      return launch_warp_query(a, metric, st);
-    if (packet_applicable(a.d, metric, a.k, a.n_points, a.use_eps != 0)) return launch_packet_query(a, metric, st);
+  if (!a.reference_order && !force_reference_order() && path != PATH_REFERENCE_ORDER) {
+    const bool eps0 = !a.use_eps;
+    const bool warp = warp_applicable(a.d, metric, a.k, a.n_points, !eps0);
+    const bool packet = packet_applicable(a.d, metric, a.k, a.n_points, !eps0);
+    int use = 0;  // 1 warp, 2 packet
+    if (path == PATH_WARP) use = warp ? 1 : 0;
+    else if (path == PATH_PACKET) use = packet ? 2 : 0;
+    else if (warp && (warp_preferred(a) || !packet)) use = 1;
+    else if (packet) use = 2;
+    if (use) {
+      if (a.rerun_count) KD_TRY_CUDA(cudaMemsetAsync(a.rerun_count, 0, sizeof(uint32_t), st));
+      const int rc = use == 1 ? launch_warp_query(a, metric, st) : launch_packet_query(a, metric, st);
+      if (rc || !a.rerun_count) return rc;
+      return launch_rerun(a, metric, st, a.rerun_count, a.rerun_list);
+    }
   }
+  if (ref_warp_applicable(a.d, a.k, a.n_points)) return launch_ref_query(a, metric, st);
   switch (metric) {
     case M_L1: return dispatch_d<M_L1>(a, st);
     case M_L2: return dispatch_d<M_L2>(a, st);
@@ -585,8 +600,13 @@ int run_kernels(const QArgs& a, int metric, cudaStream_t st, int path) {
 bool writes_whole_rows(const kd_tree* t, const QueryParams& qp) {
   if (qp.path == PATH_REFERENCE_ORDER || qp.path == PATH_TENSOR_CORE || force_reference_order()) return false;
   if (qp.path == PATH_AUTO && tc_applicable(t, qp)) return false;  // may run the tensor-core filter
-  if (!packet_applicable(t->ndim, qp.metric, qp.k, t->n_points, qp.eps_factor != 1.0)) return false;
-  return qp.k >= 5;  // the packet traversal's heaps (k >= 5) and the warp path write rows whole
+  const bool use_eps = qp.eps_factor != 1.0;
+  if (!warp_applicable(t->ndim, qp.metric, qp.k, t->n_points, use_eps)) return false;
+  // The warp kernels (and the near-tie reruns, which rewrite a few rows after
+  // the first kernel, in stream order) write rows whole; so do the packet
+  // traversal's heaps (k >= 5).
+  if (!packet_applicable(t->ndim, qp.metric, qp.k, t->n_points, use_eps)) return true;
+  return qp.k >= 5;
 }
 
 uint64_t order_scratch_words(const kd_tree* t) {
@@ -625,6 +645,10 @@ int auto_prefers_tc(kd_tree* t, const double* d_queries, uint64_t nq, const Quer
     *tc = choice == 1;
     return KD_OK;
   }
+  if (qp.no_sync) {  // a stream-ordered call times nothing: the warp traversal until a timed call chose
+    *tc = false;
+    return KD_OK;
+  }
   const uint64_t ns = std::min<uint64_t>(nq, 16384);
   QueryParams pq = qp;
   pq.path = PATH_WARP;
@@ -650,6 +674,45 @@ int auto_prefers_tc(kd_tree* t, const double* d_queries, uint64_t nq, const Quer
   return KD_OK;
 }
 
+QArgs query_args(const kd_tree* t, const double* d_queries, uint64_t nq, const QueryParams& qp, double* d_out_d,
+                 int64_t* d_out_i, uint32_t* d_status) {
+  QArgs a{};
+  a.reference_order = qp.path == PATH_REFERENCE_ORDER;
+  a.data = t->data;
+  a.data32 = t->data32;
+  a.data32w = t->data32w;
+  a.w32 = t->w32;
+  a.indices = t->indices;
+  a.nodes = t->nodes;
+  a.boxes = t->boxes;
+  a.boxes32 = t->boxes32;
+  a.coord_max = t->coord_max32;
+  a.queries = d_queries;
+  a.out_d = d_out_d;
+  a.out_i = d_out_i;
+  a.status = d_status;
+  a.nq = nq;
+  a.d = t->ndim;
+  a.k = qp.k;
+  a.n_points = t->n_points;
+  a.p = qp.p;
+  a.cutoff = qp.cutoff;
+  a.eps_factor = qp.eps_factor;
+  a.use_eps = qp.eps_factor != 1.0;
+  return a;
+}
+
+namespace {
+
+// Whether the call can reach the one-thread reference-order kernels with a
+// runtime width, which keep each query's CellBound axes in global scratch.
+bool uses_axes_scratch(const kd_tree* t, const QueryParams& qp) {
+  if (ref_warp_applicable(t->ndim, qp.k, t->n_points)) return false;
+  return !(qp.metric != M_LP && (t->ndim == 2 || t->ndim == 3 || t->ndim == 8));
+}
+
+}  // namespace
+
 int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, const QueryParams& qp,
                     double* d_out_d, int64_t* d_out_i, cudaStream_t st, uint32_t* d_status,
                     unsigned long long* d_survivors) {
@@ -668,30 +731,9 @@ int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, cons
                                 d_survivors);
     }
   }
-  QArgs a{};
-  a.reference_order = qp.path == PATH_REFERENCE_ORDER;
-  a.data = t->data;
-  a.data32 = t->data32;
-  a.indices = t->indices;
-  a.nodes = t->nodes;
-  a.boxes = t->boxes;
-  a.boxes32 = t->boxes32;
-  a.coord_max = t->coord_max32;
-  a.queries = d_queries;
-  a.out_d = d_out_d;
-  a.out_i = d_out_i;
-  a.status = d_status;
-  a.nq = nq;
-  a.d = t->ndim;
-  a.k = qp.k;
-  a.n_points = t->n_points;
-  a.p = qp.p;
-  a.cutoff = qp.cutoff;
-  a.eps_factor = qp.eps_factor;
-  a.use_eps = qp.eps_factor != 1.0;
+  QArgs a = query_args(t, d_queries, nq, qp, d_out_d, d_out_i, d_status);
   void* axes = nullptr;
-  const bool dyn = !(qp.metric != M_LP && (t->ndim == 2 || t->ndim == 3 || t->ndim == 8));
-  if (dyn) {
+  if (uses_axes_scratch(t, qp)) {
     cudaError_t e = dev_alloc(&axes, std::max<uint64_t>(1, nq * t->ndim) * sizeof(double), st);
     if (e != cudaSuccess) {
       cudaGetLastError();
@@ -699,6 +741,15 @@ int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, cons
     }
     a.axes_scratch = static_cast<double*>(axes);
   }
+  // near-tie reruns of the eps = 0 fast paths: a counter and a list
+  void* rerun = nullptr;
+  if (dev_alloc(&rerun, 16 + nq * sizeof(uint64_t), st) != cudaSuccess) {
+    cudaGetLastError();
+    if (axes) cudaFreeAsync(axes, st);
+    return fail(KD_ERR_OUT_OF_MEMORY, "device allocation failed");
+  }
+  a.rerun_count = static_cast<uint32_t*>(rerun);
+  a.rerun_list = reinterpret_cast<uint64_t*>(static_cast<unsigned char*>(rerun) + 16);
   void* sort_mem = nullptr;
   if (nq >= ORDER_MIN_QUERIES && nq < 0xffffffffull) {
     const uint64_t words = 2 * nq + order_scratch_words(t);
@@ -716,34 +767,25 @@ int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, cons
   }
   const int rc = run_kernels(a, qp.metric, st, qp.path);
   if (axes) cudaFreeAsync(axes, st);
+  cudaFreeAsync(rerun, st);
   if (sort_mem) cudaFreeAsync(sort_mem, st);
   return rc;
 }
 
+uint64_t query_scratch_bytes(uint64_t nq, uint64_t ndim) {
+  // the larger use: CellBound axes (nq * ndim doubles) or the rerun list (nq u64)
+  return std::max<uint64_t>(1, nq * std::max<uint64_t>(ndim, 1)) * sizeof(double);
+}
+
 int query_on_device_scratch(const kd_tree* t, const double* d_queries, uint64_t nq, const QueryParams& qp,
                             double* d_out_d, int64_t* d_out_i, cudaStream_t st, uint32_t* d_status,
-                            double* d_axes_scratch) {
-  QArgs a{};
-  a.data = t->data;
-  a.data32 = t->data32;
-  a.indices = t->indices;
-  a.nodes = t->nodes;
-  a.boxes = t->boxes;
-  a.boxes32 = t->boxes32;
-  a.coord_max = t->coord_max32;
-  a.queries = d_queries;
-  a.out_d = d_out_d;
-  a.out_i = d_out_i;
-  a.status = d_status;
-  a.nq = nq;
-  a.d = t->ndim;
-  a.k = qp.k;
-  a.n_points = t->n_points;
-  a.p = qp.p;
-  a.cutoff = qp.cutoff;
-  a.eps_factor = qp.eps_factor;
-  a.use_eps = qp.eps_factor != 1.0;
-  a.axes_scratch = d_axes_scratch;
+                            void* d_scratch, uint32_t* d_rerun_count) {
+  QArgs a = query_args(t, d_queries, nq, qp, d_out_d, d_out_i, d_status);
+  // The one-thread kernels (the only users of the axes) never flag near ties,
+  // and the kernels that flag them never use the axes: one region serves both.
+  a.axes_scratch = static_cast<double*>(d_scratch);
+  a.rerun_count = d_rerun_count;
+  a.rerun_list = static_cast<uint64_t*>(d_scratch);
   return run_kernels(a, qp.metric, st, qp.path);
 }
 

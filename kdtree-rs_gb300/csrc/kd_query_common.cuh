@@ -266,3 +266,11 @@ __device__ __forceinline__ uint64_t ieee_key(uint64_t b) {
   return k == 0x7fffffffffffffffull ? 0x8000000000000000ull : k;
 }
 
+// Append query qi (with the launch's tag) to the list of queries whose eps = 0
+// fast-path result is a near tie and must be run again in the reference's
+// order (kd_warp.cuh, kd_query_ref.cuh).
+__device__ __forceinline__ void flag_rerun(const QArgs& a, uint64_t qi) {
+  if (!a.rerun_count) return;
+  const uint32_t pos = atomicAdd(a.rerun_count, 1u);
+  a.rerun_list[pos] = (static_cast<uint64_t>(a.rerun_tag) << 32) | static_cast<uint32_t>(qi);
+}

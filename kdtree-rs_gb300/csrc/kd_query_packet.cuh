@@ -14,11 +14,11 @@
 // reference's summation order, original index) among the points within
 // max_distance: every pruned subtree's points exceed that lane's bound, and the
 // list keeps exactly those k in order whatever the order of the offers.  That is
-// the reference's result for eps = 0 (its answer does not depend on the visiting
-// order) except where the reference's own FP64 plane bound rounds above a point's
-// exact distance that also sits within rounding error of the k-th distance.  With
-// eps > 0 the result depends on the visiting order and the reference-order
-// descent (k_query_fast) is used instead.
+// the reference's result for eps = 0 except where one of the reference's own
+// FP64 gates rounds above the distance of a point that ties the k-th distance
+// or the cutoff; such near ties are detected (kd_warp.cuh) and those queries
+// run again in the reference's order.  With eps > 0 the result depends on the
+// visiting order and the reference-order kernels are used instead.
 #pragma once
 
 constexpr int PACKET_STACK = 2 * KD_MAX_DEPTH;
@@ -27,10 +27,11 @@ constexpr int PACKET_STACK = 2 * KD_MAX_DEPTH;
 // coordinate within E = 2^-24 (|coordinate bound| + |q|) + 2^-148 of its FP32
 // copy, the triangle inequality gives |p - q| >= |a| - sqrt(d) E (L2; d E for L1,
 // E for L-inf), and the round-to-nearest FP32 sum s over-estimates |a| (squared
-// for L2) by at most (d + 3) 2^-24 relative.  So s > T(b) with
-//   T(b) = (1 + 2^-20) (sqrt(b) + sqrt(d) E)^2 + d 2^-148   (L2),
-//   T(b) = (1 + 2^-20) (b + d E) + d 2^-148                (L1),
-//   T(b) = (1 + 2^-20) (b + E) + 2^-148                    (L-inf),
+// for L2) by at most (d + 3) 2^-24 relative.  So s > T(b) with g the larger of
+// 1 + 2^-20 and 1 + (d + 4) 2^-24 (GROW),
+//   T(b) = g (sqrt(b) + sqrt(d) E)^2 + d 2^-148   (L2),
+//   T(b) = g (b + d E) + d 2^-148                (L1),
+//   T(b) = g (b + E) + 2^-148                    (L-inf),
 // all rounded up, proves the exact distance exceeds b.  NaN never rejects.
 // An FP32 upper bound of sqrt(b) from the hardware reciprocal square root:
 // b * rsqrtf(b) is within 3 units in the last place of sqrt(b) (rsqrtf: 2,
@@ -44,6 +45,7 @@ __device__ __forceinline__ float sqrt_up(float b) {
 
 template <int M, int D>
 struct PointFilter {
+  static constexpr float GROW = D + 3 <= 16 ? UB_GROW : 1.0f + (D + 4) * TWO_M24;
   float q32[D];
   float spread;
   __device__ __forceinline__ void init(const QVec<D>& q, float coord_max) {
@@ -61,9 +63,9 @@ struct PointFilter {
     constexpr float abs_slack = D * 2.9e-45f;
     if (M == M_L2) {
       const float r = __fadd_ru(sqrt_up(b), spread);
-      return __fadd_ru(__fmul_ru(__fmul_ru(r, r), UB_GROW), abs_slack);
+      return __fadd_ru(__fmul_ru(__fmul_ru(r, r), GROW), abs_slack);
     }
-    return __fadd_ru(__fmul_ru(__fadd_ru(b, spread), UB_GROW), abs_slack);
+    return __fadd_ru(__fmul_ru(__fadd_ru(b, spread), GROW), abs_slack);
   }
   // Enclosure [clo, chi] of the exact FP64 distance from the same sum s: |a|
   // within 2^-19 of s * rsqrt(s) (rsqrtf: 2 ulp; s: (d + 3) 2^-24), then the
@@ -127,6 +129,11 @@ struct PointFilter {
   }
 };
 
+// The band above a bound b inside which a point the filter drops still counts
+// for the near-tie test: points with s > threshold(band_of(b)) are farther
+// than (1 + 2^-19) b.
+__device__ __forceinline__ float band_of(float b) { return __fmul_ru(b, 1.0000020f /* 1 + 2^-19 */); }
+
 // Shared memory of one block: the warps' node stacks and the k-best heaps
 // (K >= 8; a dummy word below).
 template <int K>
@@ -180,7 +187,7 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
     best.init(a.k, a.cutoff, q.g, a.data, a.indices, s_lo, s_hi, s_row);
   else
     best.init(a.k, a.cutoff, q.g, a.data, a.indices);
-  float thr = filt.threshold(best.b_hi);
+  float thr = filt.threshold(best.b_hi), thr2 = filt.threshold(band_of(best.b_hi));
 
   // Seed: each lane first offers the points of its own landing leaf (the
   // leaf the reference's descent reaches; any leaf would be correct), so
@@ -210,12 +217,15 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
     const uint32_t chunk_end = (D == 8 && M != M_LINF) ? start + (end - start) / 8 * 8 : end;
     for (uint32_t r = start; r < end; ++r) {
       const float sr = row_sum(r);
-      if (!(sr > thr)) {
+      if (!(sr > thr2)) {
         float clo, chi;
         filt.enclose(sr, &clo, &chi);
-        if (!(clo > best.b_hi)) {
+        if (!(sr > thr) && !(clo > best.b_hi)) {
           best.offer(clo, chi, r, r < chunk_end);
           thr = filt.threshold(best.b_hi);
+          thr2 = filt.threshold(band_of(best.b_hi));
+        } else {
+          best.note(clo);
         }
       }
     }
@@ -230,6 +240,7 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
     const uint32_t node = stack[--sp];
     const float lb = box_lb<M, D>(a.boxes32 + static_cast<uint64_t>(node) * 2 * D, qlo, qhi);
     const bool need = live && !(lb > best.b_hi);
+    if (live && !need) best.note(lb);
     const uint32_t need_mask = __ballot_sync(0xffffffffu, need);
     if (!need_mask) continue;  // every lane's points there exceed its bound
     const DNode nd = a.nodes[node];
@@ -241,11 +252,12 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
       const uint32_t chunk_end = (D == 8 && M != M_LINF) ? start + (end - start) / 8 * 8 : end;
       for (uint32_t c0 = start; c0 < end; c0 += 32) {
         const uint32_t c1 = min(end, c0 + 32);
-        // 1. which of these points can this lane's bound admit?
+        // 1. which of these points can this lane's bound admit (or lie in
+        //    the near-tie band just above it)?
         uint32_t pending = 0;
         for (uint32_t r = c0; r < c1; ++r) {
           const float s = row_sum(r);
-          if (take && !(s > thr)) pending |= 1u << (r - c0);
+          if (take && !(s > thr2)) pending |= 1u << (r - c0);
         }
         // 2. offer them, all lanes with a pending point together
         while (__any_sync(0xffffffffu, pending != 0)) {
@@ -253,12 +265,15 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
             const uint32_t r = c0 + __ffs(pending) - 1;
             pending &= pending - 1;
             const float sr = row_sum(r);
-            if (!(sr > thr)) {  // the bound may have tightened meanwhile
+            if (!(sr > thr2)) {  // the bound may have tightened meanwhile
               float clo, chi;
               filt.enclose(sr, &clo, &chi);
-              if (!(clo > best.b_hi)) {
+              if (!(sr > thr) && !(clo > best.b_hi)) {
                 best.offer(clo, chi, r, r < chunk_end);
                 thr = filt.threshold(best.b_hi);
+                thr2 = filt.threshold(band_of(best.b_hi));
+              } else {
+                best.note(clo);
               }
             }
           }
@@ -280,8 +295,9 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
   if constexpr (K >= 8) {
     if (live) best.sort_exact();
     best.write_warp(live, a.out_d + qi * a.k, a.out_i + qi * a.k, a.k, a.n_points);
+    if (live && best.near_tie()) flag_rerun(a, qi);
   } else {
-    if (live) best.write(a.out_d + qi * a.k, a.out_i + qi * a.k, a.k, a.n_points);
+    if (live && best.write(a.out_d + qi * a.k, a.out_i + qi * a.k, a.k, a.n_points)) flag_rerun(a, qi);
   }
 }
 

@@ -1,0 +1,314 @@
+// kd_query_ref.cuh -- the reference's own descent with one warp per query
+// (any eps, every metric, widths 1..128, k <= 64).  Included after
+// kd_warp.cuh.
+//
+// The warp walks the tree in exactly the reference's order (src/query.rs:
+// 223-341): the root only if its seed admits (CellBound::start, query.rs:
+// 169-194); at an inner node the near child first with the unchanged cell
+// bound, then the far child if the split-plane bound replace_axis(cell,
+// axes[dim], reduce(|diff|)) (metric.rs:93-98) and then the far child's box
+// distance (kernel.rs:565-616) admit -- `dist * eps_factor <= bound` with the
+// bound read after the near child (query.rs:242-244, 275-285); at an
+// `order_by_box` node both children's box distances, the smaller first, each
+// admitted with the bound of its moment (query.rs:298-327).  Every gate value
+// is the reference's FP64 value, computed with its operations in its order, and
+// each comparison decides exactly as the reference's does: against FP32
+// enclosures of the bound first, against the exact bound when those cannot
+// tell.  So the set of scanned leaves -- and the result -- is the reference's,
+// eps > 0 included.
+//
+// The leaf scan is the part spread across the lanes.  Within one leaf the
+// reference offers the points in row order, refreshing the bound after each
+// accepted offer (kernel.rs:366-385); the list it ends with is the k smallest
+// (distance, index) of the list before and the leaf's points within
+// max_distance, whatever the order of the offers (a point above the bound of
+// its moment has k better ones kept, or lies beyond the cutoff).  Here the
+// lanes filter their rows in FP32 and offer the survivors to the warp's list
+// (WarpList), which keeps exactly that set, so the list after the leaf -- and
+// every later gate -- matches.  For L^p (pow) the lanes compute every row's
+// exact FP64 distance.
+//
+// The kernel serves three callers: queries with eps > 0 or general p (whose
+// answers depend on this order), the reference-order path asked for
+// explicitly, and the near-tie reruns of the eps = 0 fast paths (count /
+// list: the flagged queries, kd_warp.cuh).
+#pragma once
+
+struct RefFrame {
+  uint32_t node;  // parent node id (F_FAR / F_BOX_*) or split dim (F_RESTORE)
+  uint32_t kind;
+  double x;       // parent cell_dist, or the saved axis value
+  double y;       // the pending child's box distance (F_BOX_*)
+};
+enum RefFrameKind : uint32_t { RF_FAR = 0, RF_RESTORE = 1, RF_BOX_FAR = 2, RF_BOX_NEAR = 3 };
+constexpr int REF_FRAMES = 2 * KD_MAX_DEPTH;
+
+// Bytes of shared memory one warp of the reference-order kernel uses: its
+// frames, the CellBound axes (d doubles) and the FP32 query (w32 floats).
+__host__ __device__ constexpr uint64_t ref_warp_smem(uint64_t d, uint64_t w32) {
+  return (REF_FRAMES * sizeof(RefFrame) + 8 * d + 4 * w32 + 15) / 16 * 16;
+}
+
+// Lower and upper bounds of one box's exact FP64 distance, compile-time widths
+// <= 16 (both half-warps take the same box; lane i of a half dimension i).
+template <int M, int D>
+__device__ __forceinline__ void warp_box_enc1(const float* b32, float my_qlo, float my_qhi, uint32_t lane,
+                                              float* lb_out, float* ub_out) {
+  static_assert(D > 0 && D <= 16, "one 16-lane half per box");
+  const uint32_t i = lane & 15;
+  float lb = 0.f, ub = 0.f;
+  if (i < static_cast<uint32_t>(D)) {
+    const float lo32 = b32[i], hi32 = b32[D + i];
+    const float lo_up = __fadd_ru(lo32, __fmaf_ru(fabsf(lo32), TWO_M23, TINY32));
+    const float hi_dn = __fsub_rd(hi32, __fmaf_ru(fabsf(hi32), TWO_M23, TINY32));
+    float o_lb = fmaxf(__fsub_rd(lo32, my_qhi), __fsub_rd(my_qlo, hi32));
+    o_lb = o_lb > 0.f ? o_lb : 0.f;
+    const float o_ub = fmaxf(fmaxf(__fsub_ru(lo_up, my_qlo), __fsub_ru(my_qhi, hi_dn)), 0.f);
+    lb = red_lb<M>(o_lb);
+    ub = red_ub<M>(o_ub);
+  }
+#pragma unroll
+  for (int s = Log2Ceil<D>::value - 1; s >= 0; --s) {
+    lb = fold_lb<M>(lb, __shfl_xor_sync(FULL_MASK, lb, 1 << s));
+    ub = fold_ub<M>(ub, __shfl_xor_sync(FULL_MASK, ub, 1 << s));
+  }
+  *lb_out = __fmul_rd(lb, LB_SHRINK);
+  *ub_out = __fmul_ru(ub, UB_GROW);
+}
+
+template <int M, int D, int KS>
+__device__ __forceinline__ void ref_query(const QArgs& a, uint64_t qi, RefFrame* fr, double* axes, float* sq_w) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t d = D > 0 ? static_cast<uint32_t>(D) : static_cast<uint32_t>(a.d);
+  const double pexp = a.p;
+  const double* qg = a.queries + qi * d;
+  bool fin = true;
+  for (uint32_t i = lane; i < d; i += 32) fin &= isfinite(qg[i]);
+  if (!__all_sync(FULL_MASK, fin)) {
+    if (lane == 0) atomicOr(a.status, 1u);
+    return;
+  }
+  QVec<D> q;  // FP64 query: registers for compile-time widths (uniform loops only), memory otherwise
+  q.g = qg;
+  if constexpr (D > 0) {
+#pragma unroll
+    for (int i = 0; i < D; ++i) q.v[i] = qg[i];
+  }
+  constexpr bool FILTER = M != M_LP;
+  using Filt = std::conditional_t<FILTER, typename RowFilterOf<(FILTER ? M : M_L2), D>::type, int>;
+  Filt filt{};
+  float my_qlo = 0.f, my_qhi = 0.f;
+  LaneQ lq;
+  if constexpr (FILTER) {
+    if constexpr (D > 0) {
+      filt.init(q, a.coord_max);
+#pragma unroll
+      for (int i = 0; i < D; ++i) filt.q32[i] = __shfl_sync(FULL_MASK, filt.q32[i], 0);
+#pragma unroll
+      for (int i = 0; i < D; ++i)
+        if ((lane & 15) == static_cast<uint32_t>(i)) rn_enclose(filt.q32[i], &my_qlo, &my_qhi);
+    } else {
+      filt.init(qg, d, a.w32, a.coord_max, sq_w, lane);
+      lane_query_enclosure(qg, d, lane, &lq);
+    }
+  }
+  const float* rows32 = D > 0 ? a.data32 : a.data32w;
+  const uint64_t rstride = D > 0 ? static_cast<uint64_t>(D) : a.w32;
+  const uint64_t bstride = 2ull * d;
+  const uint32_t chunk_w = (M != M_LINF && M != M_LP && (d == 4 || d == 8)) ? (d == 4 ? 2u : 8u) : 0u;
+  // FP32 enclosure of eps_factor (1 when eps = 0)
+  const float ef_lo = mag_dn32(dbits(a.eps_factor)), ef_hi = mag_up32(dbits(a.eps_factor));
+
+  WarpList<M, D, KS> best;
+  best.init(static_cast<uint32_t>(a.k), a.cutoff, lane, qg, a.data, d, pexp);
+  float thr = 0.f;
+  if constexpr (FILTER) thr = filt.threshold(best.bound32);
+
+  // admits_at(dist, bound): dist * eps_factor <= min(k-th best, cutoff)
+  // (query.rs:242-244), decided on the bound's enclosure where it can be.
+  auto admits = [&](double x) -> bool {
+    const double g = a.use_eps ? dmul(x, a.eps_factor) : x;
+    const double blo = static_cast<double>(best.bound_lo), bhi = static_cast<double>(best.bound32);
+    if (g < blo) return true;
+    if (g > bhi) return false;
+    return leq_bound(g, best.bound_exact());
+  };
+  // The far child's box gate: FP32 enclosure first, the exact FP64 box
+  // distance when it cannot decide.
+  auto box_admits = [&](uint32_t id) -> bool {
+    if constexpr (FILTER) {
+      float lb, ub;
+      if constexpr (D > 0 && D <= 16)
+        warp_box_enc1<M, D>(a.boxes32 + id * bstride, my_qlo, my_qhi, lane, &lb, &ub);
+      else
+        warp_box_enc_dyn<M>(a.boxes32 + id * bstride, d, lane, lq, &lb, &ub);
+      const float glb = __fmul_rd(__fmul_rd(lb, ef_lo), LB_SHRINK);
+      const float gub = __fmul_ru(__fmul_ru(ub, ef_hi), UB_GROW);
+      if (glb > best.bound32) return false;
+      if (gub < best.bound_lo) return true;
+    }
+    return admits(exact_box_dist<M, D>(q, a.boxes + id * bstride, d, pexp));
+  };
+  auto box_exact = [&](uint32_t id) -> double { return exact_box_dist<M, D>(q, a.boxes + id * bstride, d, pexp); };
+
+  // scan_leaf (query.rs:343-375) with the rows split across the lanes
+  auto scan_leaf = [&](uint32_t start, uint32_t end) {
+    const uint32_t chunk_end = chunk_w ? start + (end - start) / chunk_w * chunk_w : end;
+    for (uint32_t c0 = start; c0 < end; c0 += 32) {
+      const uint32_t r = c0 + lane;
+      float clo = 0.f, chi = 0.f;
+      bool cand;
+      if constexpr (FILTER) {
+        const float s = filt.sum(rows32 + static_cast<uint64_t>(min(r, end - 1)) * rstride);
+        filt.enclose(s, &clo, &chi);
+        cand = r < end && !(s > thr) && !(clo > best.bound32);
+      } else {
+        // L^p: the exact value (pow) of every row
+        const uint32_t rr = min(r, end - 1);
+        const uint64_t xb = dbits(best.exact_of(rr, false));
+        clo = mag_dn32(xb);
+        chi = mag_up32(xb);
+        cand = r < end && !(clo > best.bound32);
+      }
+      uint32_t mask = __ballot_sync(FULL_MASK, cand);
+      if (!mask) continue;
+      const uint32_t my_id = cand ? a.indices[r] : NO_ID;
+      while (mask) {
+        const int c = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const float cl = __shfl_sync(FULL_MASK, clo, c), ch = __shfl_sync(FULL_MASK, chi, c);
+        const uint32_t cid = __shfl_sync(FULL_MASK, my_id, c);
+        const uint32_t cr = c0 + static_cast<uint32_t>(c);
+        best.offer(cl, ch, cr, cid, cr < chunk_end);
+      }
+      if constexpr (FILTER) thr = filt.threshold(best.bound32);
+    }
+  };
+
+  // Descent::run (query.rs:223-232): CellBound::start seeds the axes from the
+  // root box when the query lies outside it.
+  double seed = 0.0;
+  const double rb = box_exact(0);
+  if (rb != 0.0) {
+    for (uint32_t i = lane; i < d; i += 32) axes[i] = reduce<M>(axis_offset(qg[i], a.boxes[i], a.boxes[d + i]), pexp);
+    __syncwarp();
+    for (uint32_t i = 0; i < d; ++i) seed = (M == M_LINF) ? max_nn(seed, axes[i]) : dadd(seed, axes[i]);
+  } else {
+    for (uint32_t i = lane; i < d; i += 32) axes[i] = 0.0;
+    __syncwarp();
+  }
+  // Every lane writes the same frames and axis values and reads back its own
+  // writes, so the per-warp shared state needs no further synchronisation.
+  int sp = 0;
+  uint32_t node = 0;
+  double cell = seed;
+  bool descending = admits(seed);
+  for (;;) {
+    while (descending) {
+      // Descent::descend (query.rs:248-289)
+      const DNode nd = a.nodes[node];
+      if (nd.meta & KD_NODE_LEAF) {
+        const uint64_t se = dbits(nd.split);
+        scan_leaf(static_cast<uint32_t>(se), static_cast<uint32_t>(se >> 32));
+        descending = false;
+        break;
+      }
+      const uint32_t dim = nd.meta & KD_NODE_DIM_MASK;
+      const double qd = qg[dim];
+      // diff <= 0  <=>  q[dim] <= split (exact for finite doubles)
+      const bool left_near = ieee_key(dbits(qd)) <= ieee_key(dbits(nd.split));
+      const uint32_t near = left_near ? node + 1 : nd.right;
+      const uint32_t far = left_near ? nd.right : node + 1;
+      if (nd.meta & KD_NODE_BOX_ORDER) {
+        // descend_by_box (query.rs:298-327)
+        const double near_box = box_exact(near), far_box = box_exact(far);
+        if (dbits(near_box) <= dbits(far_box)) {
+          fr[sp++] = RefFrame{node, RF_BOX_FAR, cell, far_box};
+          if (admits(near_box)) {
+            node = near;
+            continue;
+          }
+          descending = false;
+          break;
+        }
+        fr[sp++] = RefFrame{node, RF_BOX_NEAR, cell, near_box};
+        if (admits(far_box)) {
+          const double far_axis = reduce<M>(fabs(dsub(qd, nd.split)), pexp);
+          const double old = axes[dim];
+          const double far_dist = (M == M_LINF) ? max_nn(cell, far_axis) : dadd(dsub(cell, old), far_axis);
+          fr[sp++] = RefFrame{dim, RF_RESTORE, old, 0.0};
+          axes[dim] = far_axis;
+          node = far;
+          cell = far_dist;
+          continue;
+        }
+        descending = false;
+        break;
+      }
+      fr[sp++] = RefFrame{node, RF_FAR, cell, 0.0};
+      node = near;  // the near child keeps the parent's cell bound
+    }
+    // unwind to the next pending far-child decision
+    bool resumed = false;
+    while (sp > 0 && !resumed) {
+      const RefFrame f = fr[--sp];
+      if (f.kind == RF_RESTORE) {
+        axes[f.node] = f.x;
+        continue;
+      }
+      const DNode nd = a.nodes[f.node];
+      const uint32_t dim = nd.meta & KD_NODE_DIM_MASK;
+      const double qd = qg[dim];
+      const bool left_near = ieee_key(dbits(qd)) <= ieee_key(dbits(nd.split));
+      const uint32_t near = left_near ? f.node + 1 : nd.right;
+      const uint32_t far = left_near ? nd.right : f.node + 1;
+      if (f.kind == RF_BOX_NEAR) {
+        if (admits(f.y)) {
+          node = near;
+          cell = f.x;
+          resumed = true;
+        }
+        continue;
+      }
+      if (f.kind == RF_BOX_FAR && !admits(f.y)) continue;
+      // far_dist = replace_axis(cell, axes[dim], reduce(|diff|)) (metric.rs:93-98)
+      const double old = axes[dim];
+      const double far_axis = reduce<M>(fabs(dsub(qd, nd.split)), pexp);
+      const double far_dist = (M == M_LINF) ? max_nn(f.x, far_axis) : dadd(dsub(f.x, old), far_axis);
+      const bool enter = f.kind == RF_BOX_FAR || (admits(far_dist) && box_admits(far));
+      if (enter) {
+        // enter_far (query.rs:329-341)
+        fr[sp++] = RefFrame{dim, RF_RESTORE, old, 0.0};
+        axes[dim] = far_axis;
+        node = far;
+        cell = far_dist;
+        resumed = true;
+      }
+    }
+    if (!resumed) break;
+    descending = true;
+  }
+  best.write(a.out_d + qi * a.k, a.out_i + qi * a.k, a.n_points, false);
+}
+
+// Warps take queries w = global warp, + total warps, ... < n: positions of
+// the batch (a.order when set), or -- with `list` -- the flagged queries of a
+// rerun (count on the device).  Dynamic shared memory: ref_warp_smem(d, w32)
+// bytes per warp.
+template <int M, int D, int KS>
+__global__ void __launch_bounds__(QUERY_THREADS) k_query_ref(QArgs a, const uint32_t* count, const uint64_t* list) {
+  extern __shared__ __align__(16) unsigned char ref_smem[];
+  const uint32_t wid = threadIdx.x >> 5;
+  const uint32_t d = D > 0 ? static_cast<uint32_t>(D) : static_cast<uint32_t>(a.d);
+  const uint64_t per = ref_warp_smem(d, (D == 0 && M != M_LP) ? a.w32 : 0);
+  unsigned char* base = ref_smem + wid * per;
+  RefFrame* fr = reinterpret_cast<RefFrame*>(base);
+  double* axes = reinterpret_cast<double*>(base + REF_FRAMES * sizeof(RefFrame));
+  float* sq = reinterpret_cast<float*>(base + REF_FRAMES * sizeof(RefFrame) + 8 * d);
+  const uint64_t n = count ? *count : a.nq;
+  const uint64_t warps = static_cast<uint64_t>(gridDim.x) * (QUERY_THREADS / 32);
+  for (uint64_t w = blockIdx.x * static_cast<uint64_t>(QUERY_THREADS / 32) + wid; w < n; w += warps) {
+    const uint64_t qi = list ? static_cast<uint32_t>(list[w]) : (a.order ? a.order[w] : w);
+    ref_query<M, D, KS>(a, qi, fr, axes, sq);
+  }
+}

@@ -22,7 +22,10 @@
 // (LazySetDyn), which computes the reference's exact FP64 distance (Folded order
 // for d <= 16, Streamed above, kernel.rs) only when two enclosures overlap and
 // for the final k.  The result is the k smallest (exact FP64 distance, index)
-// within max_distance -- the reference's answer for eps = 0.
+// within max_distance -- the reference's answer for eps = 0 unless a near tie
+// lets the reference's own descent leave one of them out; those queries are
+// flagged (every dropped pair's lower bound is tracked, skipped tiles through
+// their box bound) and run again in the reference's order (kd_query_ref.cuh).
 //
 // Pipeline (one persistent CTA per SM, a 128-query tile at a time):
 //   warp 0  TMA: the query tile once, then 256-point tiles into a ring of
@@ -76,6 +79,8 @@ struct TcArgs {
   int64_t* out_i;
   uint32_t* status;
   unsigned long long* survivors;
+  uint32_t* rerun_count;  // near ties: query indices appended to rerun_list
+  uint64_t* rerun_list;
   uint64_t nq, n_points, d, k;
   double cutoff;
   float coord_max;
@@ -203,11 +208,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   __shared__ int s_zero;  // a flag that never rises: the drain waits ignore aborts
   __shared__ uint32_t s_tile[4];      // per stage: the point tile it holds, or TC_END
   __shared__ uint32_t s_acc_tile[2];  // per accumulator: the point tile it scored, or TC_END
+  __shared__ float s_skip[4];         // per stage holding TC_END: the smallest box bound of the tiles skipped
+  __shared__ float s_acc_skip[2];     // ... passed on with the accumulator's TC_END
   __shared__ float s_wb[4];           // per epilogue warp: the largest bound of its rows ...
   __shared__ uint32_t s_wq[4];        // ... for the CTA's query tile number s_wq
   volatile int* abort_flag = &s_abort;
   volatile uint32_t* v_tile = s_tile;
   volatile uint32_t* v_acc_tile = s_acc_tile;
+  volatile float* v_skip = s_skip;
+  volatile float* v_acc_skip = s_acc_skip;
   volatile float* v_wb = s_wb;
   volatile uint32_t* v_wq = s_wq;
 
@@ -264,6 +273,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (!ok) break;
       const float* qb = a.qbox + static_cast<uint64_t>(qt) * 2 * a.d;
+      float skip_min = __int_as_float(0x7f800000);  // lane 0: the skipped tiles' smallest box bound
       for (uint32_t p0 = 0; p0 < a.n_pt && ok; p0 += 32) {
         const uint32_t pt = p0 + lane;
         uint32_t tile = 0;
@@ -282,7 +292,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             __threadfence_block();
             float bound = __int_as_float(0x7f800000);
             if (cur) bound = fmaxf(fmaxf(v_wb[0], v_wb[1]), fmaxf(v_wb[2], v_wb[3]));
-            if (!(lbj > bound)) {
+            if (lbj > bound) {
+              skip_min = fminf(skip_min, lbj);
+            } else {
               const uint32_t s = ld % nst, u = ld / nst;
               ok = mbar_wait(smem_u32(&empty[s]), (u & 1) ^ 1, abort_flag);
               if (ok) {
@@ -305,6 +317,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         ok = mbar_wait(smem_u32(&empty[s]), (u & 1) ^ 1, abort_flag);
         if (ok) {
           v_tile[s] = TC_END;
+          v_skip[s] = skip_min;
           mbar_arrive(smem_u32(&full[s]));
           last_use[s] = u + 1;
         }
@@ -343,6 +356,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           ++ld;
           ++t;
           if (tile == TC_END) {
+            v_acc_skip[b] = v_skip[s];
             mbar_arrive(smem_u32(&empty[s]));  // the stage carried no data
             v_acc_tile[b] = TC_END;
             mbar_arrive(smem_u32(&accf[b]));
@@ -388,8 +402,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const float e = __fmaf_ru(__fadd_ru(a.coord_max, qmax), TWO_M24, 2.9e-45f);
       const float spread = __fmul_ru(e, __fsqrt_ru(static_cast<float>(a.d)));
       const float qn2 = a.qn2[qrow], qnorm = a.qnorm[qrow];
-      float m2r, thr;
+      float m2r, thr, m2r2, thr2;  // (m2r2, thr2): the near-tie band just above the bound
       tc_threshold(set.b_hi, qn2, qnorm, &m2r, &thr);
+      tc_threshold(__fmul_ru(set.b_hi, 1.0000020f /* 1 + 2^-19 */), qn2, qnorm, &m2r2, &thr2);
       if (lane == 0) {  // this query tile's bound: none yet
         v_wb[warp - 2] = __int_as_float(0x7f800000);
         __threadfence_block();
@@ -405,6 +420,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const uint32_t tile = v_acc_tile[b];
         ++t;
         if (tile == TC_END) {
+          set.note(v_acc_skip[b]);  // every pair of a skipped tile is at least that far
           mbar_arrive(smem_u32(&acce[b]));
           break;
         }
@@ -415,7 +431,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           tmem_ld32(tmem + ((quarter * 32) << 16) + b * TC_N + c, r);
           const float4* w4 = reinterpret_cast<const float4*>(a.pw + base + c);
           const float4* v4 = reinterpret_cast<const float4*>(a.pv + base + c);
-          uint32_t mask = 0;
+          uint32_t mask = 0, band = 0;
 #pragma unroll
           for (int j4 = 0; j4 < 8; ++j4) {
             const float4 w = __ldg(w4 + j4), v = __ldg(v4 + j4);
@@ -423,12 +439,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
               const int j = j4 * 4 + u;
-              float x = __fmaf_rn(-2.f, __uint_as_float(r[j]), ww[u]);
-              x = __fmaf_rn(m2r, vv[u], x);
+              const float x0 = __fmaf_rn(-2.f, __uint_as_float(r[j]), ww[u]);
+              const float x = __fmaf_rn(m2r, vv[u], x0);
               mask |= static_cast<uint32_t>(!(x > thr)) << j;
+              band |= static_cast<uint32_t>(!(__fmaf_rn(m2r2, vv[u], x0) > thr2)) << j;
             }
           }
-          if (!active) mask = 0;
+          if (!active) mask = band = 0;
+          // pairs rejected inside the band: farther than the bound, at least b_lo
+          if (band & ~mask) set.note(set.b_lo);
           while (mask) {
             const uint32_t j = __ffs(mask) - 1;
             mask &= mask - 1;
@@ -451,9 +470,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
               clo = __fmul_rd(__fmul_rd(lo, lo), LB_SHRINK);
               chi = __fmul_ru(__fmul_ru(hi, hi), UB_GROW);
             }
-            if (clo > set.b_hi) continue;
+            if (clo > set.b_hi) {
+              set.note(clo);
+              continue;
+            }
             set.offer(clo, chi, p);
             tc_threshold(set.b_hi, qn2, qnorm, &m2r, &thr);
+            tc_threshold(__fmul_ru(set.b_hi, 1.0000020f), qn2, qnorm, &m2r2, &thr2);
           }
         }
         asm volatile("tcgen05.fence::before_thread_sync;");
@@ -464,7 +487,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int off = 16; off; off >>= 1) mb = fmaxf(mb, __shfl_xor_sync(0xffffffffu, mb, off));
         if (lane == 0) v_wb[warp - 2] = mb;
       }
-      if (ok && active) set.write(a.out_d + qi * a.k, a.out_i + qi * a.k, a.k, a.n_points);
+      if (ok && active && set.write(a.out_d + qi * a.k, a.out_i + qi * a.k, a.k, a.n_points) && a.rerun_count)
+        a.rerun_list[atomicAdd(a.rerun_count, 1u)] = qi;
     }
     if (!ok) atomicExch(&s_abort, 1);
     atomicAdd(&s_surv, surv);
@@ -601,9 +625,14 @@ int make_rows_map(CUtensorMap* m, const void* base, uint64_t rows, uint32_t dpad
 }
 
 // Tree-side inputs, made once per tree.
+// The caller's stream waits (on the device) for the kernels that made them,
+// whichever stream those ran on; no host wait.
 int ensure_tc_points(kd_tree* t, cudaStream_t st) {
   std::lock_guard<std::mutex> lock(t->tc_mutex);
-  if (t->tc_points) return KD_OK;
+  if (t->tc_points) {
+    KD_TRY_CUDA(cudaStreamWaitEvent(st, t->tc_ready, 0));
+    return KD_OK;
+  }
   const uint64_t n = t->n_points, d = t->ndim;
   const uint32_t dpad = static_cast<uint32_t>((d + TC_KC - 1) / TC_KC * TC_KC);
   const uint64_t n_pad = (n + TC_N - 1) / TC_N * TC_N;
@@ -628,8 +657,21 @@ int ensure_tc_points(kd_tree* t, cudaStream_t st) {
                                                                      nullptr, nullptr, w, v);
   if (n_pad > n) k_tc_pad<<<1, 256, 0, st>>>(w, v, n, n_pad);
   k_tile_boxes<<<static_cast<unsigned>(n_pt), 128, 0, st>>>(t->data32, n, d, TC_N, tbox);
-  KD_TRY_CUDA(cudaGetLastError());
-  KD_TRY_CUDA(cudaStreamSynchronize(st));
+  cudaEvent_t ready = nullptr;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventRecord(ready, st);
+  if (e != cudaSuccess) {
+    cudaStreamSynchronize(st);  // nothing may still write them when they are freed
+    if (ready) cudaEventDestroy(ready);
+    cudaFree(pts);
+    cudaFree(w);
+    cudaFree(v);
+    cudaFree(centre);
+    cudaFree(tbox);
+    return cuda_fail(e, "tensor-core inputs");
+  }
+  t->tc_ready = ready;
   t->tc_tbox = tbox;
   t->tc_points = pts;
   t->tc_w = w;
@@ -660,13 +702,18 @@ int query_tc_on_device(kd_tree* t, const double* d_queries, uint64_t nq, const Q
   const uint64_t q32_bytes = nq * d * sizeof(float);
   const uint64_t sort_words = 2 * nq + order_scratch_words(t) + n_qt;
   const uint64_t qbox_bytes = static_cast<uint64_t>(n_qt) * 2 * d * sizeof(float);
-  const uint64_t total = qbytes + 2 * fbytes + q32_bytes + qbox_bytes + sort_words * sizeof(uint32_t) + 256;
+  // rounded to 256 bytes: the BF16 query rows after it are a TMA source (16-byte aligned base)
+  const uint64_t rerun_bytes = (16 + nq * sizeof(uint64_t) + 255) / 256 * 256;
+  const uint64_t total = rerun_bytes + qbytes + 2 * fbytes + q32_bytes + qbox_bytes + sort_words * sizeof(uint32_t) +
+                         256;
   if (dev_alloc(&mem, total, st) != cudaSuccess) {
     cudaGetLastError();
     return fail(KD_ERR_OUT_OF_MEMORY, "device allocation failed");
   }
-  uint16_t* qb = static_cast<uint16_t*>(mem);
-  float* qn2 = reinterpret_cast<float*>(static_cast<unsigned char*>(mem) + qbytes);
+  uint32_t* rerun_count = static_cast<uint32_t*>(mem);
+  uint64_t* rerun_list = reinterpret_cast<uint64_t*>(static_cast<unsigned char*>(mem) + 16);
+  uint16_t* qb = reinterpret_cast<uint16_t*>(static_cast<unsigned char*>(mem) + rerun_bytes);
+  float* qn2 = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(qb) + qbytes);
   float* qnorm = qn2 + nq;
   float* q32 = qnorm + nq;
   float* qbox = q32 + nq * d;
@@ -703,6 +750,8 @@ int query_tc_on_device(kd_tree* t, const double* d_queries, uint64_t nq, const Q
   a.out_i = d_out_i;
   a.status = d_status;
   a.survivors = d_survivors;
+  a.rerun_count = rerun_count;
+  a.rerun_list = rerun_list;
   a.nq = nq;
   a.n_points = t->n_points;
   a.d = d;
@@ -720,12 +769,22 @@ int query_tc_on_device(kd_tree* t, const double* d_queries, uint64_t nq, const Q
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(a.n_qt, static_cast<uint64_t>(sms)));
-  KD_TRY_CUDA(cudaFuncSetAttribute(k_query_tc<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-  k_query_tc<32><<<grid, TC_THREADS, smem, st>>>(mq, mp, a);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = cudaMemsetAsync(rerun_count, 0, sizeof(uint32_t), st);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_query_tc<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (e == cudaSuccess) {
+    k_query_tc<32><<<grid, TC_THREADS, smem, st>>>(mq, mp, a);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) {
+    cudaFreeAsync(mem, st);
+    return cuda_fail(e, "k_query_tc launch");
+  }
+  // the near ties, again in the reference's order
+  const QArgs ra = query_args(t, d_queries, nq, qp, d_out_d, d_out_i, d_status);
+  rc = launch_rerun(ra, M_L2, st, rerun_count, rerun_list);
   cudaFreeAsync(mem, st);
-  if (e != cudaSuccess) return cuda_fail(e, "k_query_tc launch");
-  return KD_OK;
+  return rc;
 }
 
 }  // namespace kd

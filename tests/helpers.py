@@ -34,6 +34,31 @@ def assert_bit_exact(actual, expected):
     np.testing.assert_array_equal(a_i, e_i)
 
 
+def lp_max_ulps(d, p):
+    """Largest difference, in units in the last place, between an L^p distance
+    the GPU returns and the oracle's.  Both follow the reference's operations
+    in its order; only pow() differs: CUDA's pow is within 2 ulp, glibc's
+    within 0.52, so each term |q_i - p_i|^p differs by at most 2.52 ulp
+    (relative).  The sequential sum of d non-negative terms keeps that relative
+    bound and adds at most half an ulp of rounding difference per partial sum:
+    2.52 + d / 2 ulp.  restore() = pow(sum, 1 / p) divides that by p and adds
+    its own 2.52."""
+    return int(np.ceil((2.52 + 0.5 * d) / p + 2.52))
+
+
+def assert_lp_close(actual, expected, d, p):
+    """General L^p: indices exact, finite distances within lp_max_ulps(d, p)
+    ulp, +inf where the oracle has +inf."""
+    a_d, a_i = actual
+    e_d, e_i = expected
+    np.testing.assert_array_equal(a_i, e_i)
+    fin = np.isfinite(e_d)
+    assert np.array_equal(np.isfinite(a_d), fin)
+    ulps = np.abs(a_d[fin].view(np.int64) - e_d[fin].view(np.int64))
+    bound = lp_max_ulps(d, p)
+    assert ulps.max(initial=0) <= bound, f"L^p distance off by {ulps.max()} ulp (bound {bound})"
+
+
 def gmm(n, d, rng, components=64, sigma=0.01):
     """Isotropic Gaussian mixture: centres uniform in [0,1)^d, equal weights."""
     centres = rng.uniform(size=(components, d))

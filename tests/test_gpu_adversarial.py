@@ -1,0 +1,96 @@
+"""Inputs where the reference's FP64 gates round above a kept point's distance
+(tests/golden/adversarial.npz, made by make_adversarial.py): the engine must
+return the reference's answer -- which leaves that point out -- on every query
+path, through the C ABI, the drop-in KDTree.query and a batch plan.
+
+The eps = 0 fast paths (packet, warp, tensor-core) compute the exact top-k and
+flag the near ties where the reference's descent can differ from it; those
+queries are run again in the reference's order.  These cases are exactly such
+near ties, on lattice data where many distances are equal."""
+import ctypes
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+PATHS = {"auto": 0, "reference_order": 1, "packet": 2, "tensor_core": 3, "warp": 4}
+
+
+def _cases():
+    f = np.load(Path(__file__).parent / "golden" / "adversarial.npz")
+    out = []
+    for i in range(int(f["n_cases"])):
+        leaf, k, p, md = f[f"c{i}_params"]
+        out.append((f[f"c{i}_data"], f[f"c{i}_q"], int(leaf), int(k), float(p),
+                    None if np.isnan(md) else float(md), f[f"c{i}_ref_d"], f[f"c{i}_ref_i"]))
+    return out
+
+
+CASES = _cases()
+
+
+def _path_lib():
+    from kdtree import _core
+
+    L = _core._lib
+    P, u64, d = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double
+    L.kd_query_device_path.argtypes = [P, P, u64, u64, d, ctypes.c_int, d, d, P, P, P, ctypes.c_int, P]
+    L.kd_query_device_path.restype = ctypes.c_int
+    return L, _core
+
+
+def _exact(got, ref_d, ref_i, what):
+    np.testing.assert_array_equal(got[1], ref_i, err_msg=what)
+    assert np.array_equal(got[0], ref_d), what
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_every_path_returns_the_reference_answer(case):
+    import torch
+
+    from kdtree import KDTree
+
+    data, q, leaf, k, p, md, ref_d, ref_i = CASES[case]
+    L, core = _path_lib()
+    tree = KDTree(data, leafsize=leaf)
+    dq = torch.from_numpy(q).cuda()
+    P = ctypes.c_void_p
+    for name, path in PATHS.items():
+        od = torch.full((q.shape[0], k), -1.0, dtype=torch.float64, device="cuda")
+        oi = torch.full((q.shape[0], k), -1, dtype=torch.int64, device="cuda")
+        st = L.kd_query_device_path(tree._h, P(dq.data_ptr()), dq.numel(), k, p, int(md is not None),
+                                    float(md or 0.0), 0.0, P(od.data_ptr()), P(oi.data_ptr()), None, path, None)
+        assert st == 0, core._last_error()
+        _exact((od.cpu().numpy(), oi.cpu().numpy()), ref_d, ref_i, f"path {name}")
+    # the drop-in surface (host buffers)
+    _exact(tree.query(q, k=k, p=p, max_distance=md), ref_d, ref_i, "KDTree.query")
+
+
+def test_batch_plan_returns_the_reference_answers():
+    """Every case as one job of a batch plan (jobs grouped by p and
+    max_distance, which a plan shares): the fused kernel's near-tie reruns."""
+    import torch
+
+    from kdtree import BatchQuery, KDTree, _core
+
+    groups = {}
+    for c in CASES:
+        groups.setdefault((c[4], c[5]), []).append(c)
+    for (p, md), cases in groups.items():
+        jobs = []
+        for data, q, leaf, k, _, _, _, _ in cases:
+            dq = torch.from_numpy(q).cuda()
+            jobs.append((KDTree(data, leafsize=leaf), dq, k,
+                         torch.full((q.shape[0], k), -1.0, dtype=torch.float64, device="cuda"),
+                         torch.full((q.shape[0], k), -1, dtype=torch.int64, device="cuda")))
+        plan = BatchQuery(jobs, p=p, max_distance=md)
+        for mode in (_core.BATCH_GRAPH, _core.BATCH_FUSED, _core.BATCH_PER_JOB):
+            for j in jobs:
+                j[3].fill_(-1.0)
+                j[4].fill_(-1)
+            plan.run(None, mode)
+            torch.cuda.synchronize()
+            for (_, _, _, _, _, _, ref_d, ref_i), j in zip(cases, jobs):
+                _exact((j[3].cpu().numpy(), j[4].cpu().numpy()), ref_d, ref_i, f"batch mode {mode}")

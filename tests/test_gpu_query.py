@@ -6,7 +6,7 @@ plain workloads at full size."""
 import numpy as np
 import pytest
 
-from helpers import assert_bit_exact, gmm
+from helpers import assert_bit_exact, assert_lp_close, gmm
 
 pytestmark = pytest.mark.gpu
 
@@ -57,15 +57,15 @@ def test_max_distance(oracle, p):
 
 
 def test_general_p(oracle):
-    """L^p distances go through pow(): CUDA's and libm's may differ in the last
-    ulp, so distances are compared with a tolerance and indices exactly."""
+    """L^p distances go through pow(): CUDA's and libm's differ in the last
+    places, so distances are compared within lp_max_ulps(d, p) ulp (the bound
+    is derived in tests/helpers.py) and indices exactly."""
     rng = np.random.default_rng(13)
     data = rng.normal(size=(5000, 4))
     q = rng.normal(size=(500, 4))
     for p in (1.5, 3.0):
         g, o = _both(oracle, data, q, 8, k=6, p=p)
-        np.testing.assert_allclose(g[0], o[0], rtol=1e-13, atol=0)
-        np.testing.assert_array_equal(g[1], o[1])
+        assert_lp_close(g, o, 4, p)
 
 
 def test_ties(oracle):

@@ -353,9 +353,13 @@ def plain_scale_cases(lib, torch, stream, dev):
 
 def precision_cases(lib, torch, stream, dev, cpu_threads):
     """Config 3: N=1M, d in {16, 64}, standard normal x per-dimension scale
-    log-uniform in [0.1, 10], 100k queries, k=32, L2: the tensor-core filter path
-    against the reference-order FP64 path (on a 4,864-query sample), the
-    filter's survivors per pair, and the BF16 score's error against FP64."""
+    log-uniform in [0.1, 10], 100k queries, k=32, L2.  The tensor-core filter
+    path against the plain CUDA-core path (the best-first warp traversal: FP32
+    filters, exact FP64 values in the reference's summation order), both on all
+    100k queries and compared bit for bit; the reference-order warp kernel (the
+    reference's own visiting order and FP64 gates) on a sample; the filter's
+    survivors per pair and the BF16 score's error against FP64; a sample
+    checked against the oracle."""
     from kdtree import KDTree
 
     out = {}
@@ -371,14 +375,13 @@ def precision_cases(lib, torch, stream, dev, cpu_threads):
         surv = torch.zeros(1, dtype=torch.int64, device=dev)
         ms_tc, (od, oi) = time_path(lib, tree, dq, 32, 2.0, PATH_TENSOR_CORE, 3, torch, stream, surv)
         pairs = 3 * q.shape[0] * data.shape[0]
-        # The FP64 reference-order path runs one thread per query; its sample is
-        # 38 blocks of 128 queries (38 SMs with 4 warps each), enough to measure
-        # throughput rather than one warp's latency, in about half a minute at d=64.
-        n_ref = 38 * 128
+        rerank = int(surv.item()) / pairs
+        ms_pl, (pd_, pi_) = time_path(lib, tree, dq, 32, 2.0, PATH_WARP, 1, torch, stream)
+        same = bool(torch.equal(oi, pi_) and torch.equal(od, pd_))
+        n_ref = 152 * 4 * 8  # eight warps an SM's worth of queries for the reference-order kernel
         sample = dq[:n_ref].contiguous()
-        ms_ref, (rd_, ri_) = time_path(lib, tree, sample, 32, 2.0, PATH_REFERENCE_ORDER, 1, torch, stream,
-                                       warm=False)
-        same = bool(torch.equal(oi[:n_ref], ri_) and torch.equal(od[:n_ref], rd_))
+        ms_ref, (rd_, ri_) = time_path(lib, tree, sample, 32, 2.0, PATH_REFERENCE_ORDER, 1, torch, stream)
+        same_ref = bool(torch.equal(oi[:n_ref], ri_) and torch.equal(od[:n_ref], rd_))
         # BF16 score error against FP64 on the true neighbours of 200 queries
         c = (data.min(0) + data.max(0)) / 2
         qi = np.repeat(np.arange(200), 32)
@@ -388,27 +391,25 @@ def precision_cases(lib, torch, stream, dev, cpu_threads):
         approx = (qb[qi] ** 2).sum(1) + (pb ** 2).sum(1) - 2 * (qb[qi] * pb).sum(1)
         exact = ((q[qi] - data[pi]) ** 2).sum(1)
         rel = np.abs(approx - exact) / exact
-        case = {"build_s": build_s, "tc_qps": q.shape[0] / ms_tc * 1e3, "tc_ms_100k": ms_tc,
-                "reference_order_fp64_qps": n_ref / ms_ref * 1e3, "reference_order_sample": n_ref,
-                "speedup_tc_vs_fp64_path": (q.shape[0] / ms_tc) / (n_ref / ms_ref),
-                "sample_identical": same, "rerank_fraction": int(surv.item()) / pairs,
-                "filter_rel_err_max": float(rel.max()), "filter_rel_err_median": float(np.median(rel))}
-        if d == 16:  # the two traversals on a 10,000-query sample (the tree barely prunes here)
-            ps = dq[:10_000].contiguous()
-            for name, path in (("packet", PATH_PACKET), ("warp", PATH_WARP)):
-                ms_pk, (pd_, pi_) = time_path(lib, tree, ps, 32, 2.0, path, 1, torch, stream)
-                case[name + "_qps"] = 10_000 / ms_pk * 1e3
-                case[name + "_identical"] = bool(torch.equal(pi_, oi[:10_000]) and torch.equal(pd_, od[:10_000]))
+        tc_qps, plain_qps = q.shape[0] / ms_tc * 1e3, q.shape[0] / ms_pl * 1e3
+        case = {"build_s": build_s, "tc_qps": tc_qps, "tc_ms_100k": ms_tc, "plain_qps": plain_qps,
+                "plain_path": "warp best-first (CUDA cores, FP64-exact)", "plain_ms_100k": ms_pl,
+                "tc_over_plain": tc_qps / plain_qps, "identical": same and same_ref,
+                "reference_order_qps": n_ref / ms_ref * 1e3, "reference_order_sample": n_ref,
+                "rerank_fraction": rerank, "filter_rel_err_max": float(rel.max()),
+                "filter_rel_err_median": float(np.median(rel))}
         if cpu_threads:
             sys.path.insert(0, str(ROOT / "oracle"))
             import kdtree_oracle
 
             ot = kdtree_oracle.OracleKDTree(data, leafsize=16, parallel=True)
-            ns = 2000 if d == 16 else 200
+            ns = 2000 if d == 16 else 300
             t0 = time.perf_counter()
-            ot.query(q[:ns], k=32, threads=cpu_threads)
+            o_d, o_i = ot.query(q[:ns], k=32, threads=cpu_threads)
             case["cpu_oracle_qps"] = ns / (time.perf_counter() - t0)
             case["cpu_sample"] = ns
+            case["identical"] = case["identical"] and bool(
+                np.array_equal(o_i, oi[:ns].cpu().numpy()) and np.array_equal(o_d, od[:ns].cpu().numpy()))
         out[f"d{d}"] = case
         del tree
     return out
@@ -864,6 +865,20 @@ def main():
         e2e_times.append(time.perf_counter() - t0)
     e2e_value, e2e_s = whole_job_rate(sum(e2e_times), args.steps, ws, dev)
 
+    # the drop-in surface: KDTree.query with a pageable numpy array in and
+    # fresh numpy arrays out (src/lib.rs:161-182)
+    for _ in range(2):
+        tree.query(q, k=K)
+    np_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = tree.query(q, k=K)
+        np_times.append(time.perf_counter() - t0)
+        del res
+    e2e_numpy_value, _ = whole_job_rate(sum(np_times), args.steps, ws, dev)
+
     if rank != 0:
         if ws > 1:
             dist.destroy_process_group()
@@ -908,7 +923,10 @@ def main():
         "gpu_launches": LAUNCHES_PER_STEP * args.steps,
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),
-                "d2h_bytes_per_step": int(N_QUERIES * K * 16)},
+                "d2h_bytes_per_step": int(N_QUERIES * K * 16), "api": "kd_query, page-locked host buffers"},
+        "e2e_numpy": {"value": e2e_numpy_value, "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),
+                      "d2h_bytes_per_step": int(N_QUERIES * K * 16),
+                      "api": "KDTree.query, pageable numpy in, fresh numpy arrays out"},
         "roofline": roofline,
         "build": build_line(build_s, cpu["build_s"] if cpu else None, peak),
         "cpu_baseline": None if cpu is None else {

@@ -88,19 +88,50 @@ int kd_query_device(const kd_tree* tree, const double* d_queries, uint64_t n_val
                     double p, int has_max_distance, double max_distance, double eps,
                     double* d_out_distances, int64_t* d_out_indices, void* stream);
 
+/* kd_query_device without any host wait, for callers that pipeline uploads,
+ * queries and downloads on their own streams (a framework binding, a serving
+ * loop).  No reference counterpart beyond `Tree::query` (src/query.rs:29-78),
+ * whose pyo3 wrapper releases the GIL around it (src/lib.rs:176-177): this is
+ * that seam made stream-ordered.
+ *
+ * Every device step of the call is ordered on `stream` and the call returns
+ * once they are enqueued.  `d_status` is a device u32 the call first clears
+ * (stream-ordered) and the kernels then set: bit 0 a non-finite query (the
+ * reference's NonFiniteData), bit 1 a tensor-core pipeline wait that ran out
+ * (KD_ERR_CUDA); read it after the stream work, e.g. with the results.
+ * The return value covers what the host can check: shape, k, NULL buffers,
+ * and the scalar arguments (p, max_distance, eps, with the reference's
+ * messages).  For a scalar error the finiteness check still runs into bit 0 of
+ * *d_status, and the reference reports that error first.  Scratch comes from
+ * the library's stream-ordered pool.  Two one-time set-ups stay asynchronous
+ * too: a tree's first tensor-core query enqueues its BF16 copy (other streams
+ * wait for it on the device), and at ndim = 16 a call that finds no timed
+ * choice between the two exact paths takes the warp traversal instead of
+ * timing both. */
+int kd_query_async(const kd_tree* tree, const double* d_queries, uint64_t n_values, uint64_t k, double p,
+                   int has_max_distance, double max_distance, double eps, double* d_out_distances,
+                   int64_t* d_out_indices, uint32_t* d_status, void* stream);
+
 /* Query kernels kd_query_device_path can be asked for.  No reference
  * counterpart: the reference has one CPU descent; these are the engine's
  * implementations of it, for measurement and cross-checking.
  *   KD_PATH_AUTO            what kd_query / kd_query_device run
- *   KD_PATH_REFERENCE_ORDER one thread per query, the reference's depth-first
- *                           order (FP64 decisions; the only order for eps > 0)
+ *   KD_PATH_REFERENCE_ORDER the reference's depth-first order with its FP64
+ *                           gate decisions (the only order for eps > 0 and
+ *                           general p): one warp per query, leaf rows split
+ *                           across the lanes (d <= 128, k <= 64), one thread
+ *                           per query otherwise
  *   KD_PATH_PACKET          warp-shared traversal (d in {2, 3, 8, 16}, eps = 0, k <= 64)
  *   KD_PATH_TENSOR_CORE     tcgen05 BF16 distance filter + FP64 re-rank
  *                           (L2, eps = 0, 16 <= d <= 128, k <= 32)
- *   KD_PATH_WARP            one warp per query, rows and dimensions split
- *                           across the lanes (d in {2, 3, 8, 16}, eps = 0,
- *                           k <= 64): for queries that scan many leaf rows
- * A path that does not apply to a call falls back to the reference order. */
+ *   KD_PATH_WARP            one warp per query, best-first, rows and
+ *                           dimensions split across the lanes (d <= 128,
+ *                           eps = 0, k <= 64): for queries that scan many rows
+ * The eps = 0 paths other than the reference order compute the exact top-k
+ * and run again, in the reference's order, the queries where a near tie lets
+ * the reference's own descent leave a point out, so every path returns the
+ * reference's answer.  A path that does not apply to a call falls back to the
+ * reference order. */
 enum kd_query_path {
   KD_PATH_AUTO = 0,
   KD_PATH_REFERENCE_ORDER = 1,

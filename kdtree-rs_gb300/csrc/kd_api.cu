@@ -438,6 +438,34 @@ int kd_query_device(const kd_tree* tree, const double* d_queries, uint64_t n_val
                       d_out_distances, d_out_indices, static_cast<cudaStream_t>(stream));
 }
 
+int kd_query_async(const kd_tree* t, const double* d_queries, uint64_t n_values, uint64_t k, double p,
+                   int has_max_distance, double max_distance, double eps, double* d_out_distances,
+                   int64_t* d_out_indices, uint32_t* d_status, void* stream) {
+  if (!t) return fail(KD_ERR_INVALID_ARGUMENT, "tree is NULL");
+  if (k == 0) return fail(KD_ERR_INVALID_K, "k must be greater than zero");
+  if (n_values == 0 || n_values % t->ndim)
+    return fail(KD_ERR_INVALID_SHAPE, "queries must be a contiguous row-major matrix");
+  if (!d_queries || !d_out_distances || !d_out_indices || !d_status)
+    return fail(KD_ERR_INVALID_ARGUMENT, "NULL buffer");
+  QueryParams qp{};
+  std::string msg;
+  const int scalar = validate_scalars(k, p, has_max_distance, max_distance, eps, &qp, &msg);
+  const uint64_t nq = n_values / t->ndim;
+  DevicePin pin(t->device);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  KD_TRY_CUDA(cudaMemsetAsync(d_status, 0, sizeof(uint32_t), st));
+  if (scalar != KD_OK) {
+    // The reference reports a non-finite query before these (query.rs:46-48):
+    // its check still runs, into bit 0 of *d_status.
+    k_check_finite<<<static_cast<unsigned>((n_values + 255) / 256), 256, 0, st>>>(d_queries, n_values, d_status);
+    KD_TRY_CUDA(cudaGetLastError());
+    return fail(scalar, msg);
+  }
+  if (k > (~0ull / sizeof(double)) / nq) return fail(KD_ERR_OUT_OF_MEMORY, "output would not fit in memory");
+  qp.no_sync = true;
+  return query_on_device(t, d_queries, nq, qp, d_out_distances, d_out_indices, st, d_status, nullptr);
+}
+
 int kd_query_device_path(const kd_tree* tree, const double* d_queries, uint64_t n_values, uint64_t k, double p,
                          int has_max_distance, double max_distance, double eps, double* d_out_distances,
                          int64_t* d_out_indices, void* stream, int path, unsigned long long* d_survivors) {

@@ -53,6 +53,8 @@ def _load():
     L.kd_query.restype = ctypes.c_int
     L.kd_query_device.argtypes = [P, P, u64, u64, d, ctypes.c_int, d, d, P, P, P]
     L.kd_query_device.restype = ctypes.c_int
+    L.kd_query_async.argtypes = [P, P, u64, u64, d, ctypes.c_int, d, d, P, P, P, P]
+    L.kd_query_async.restype = ctypes.c_int
     for name in ("kd_ndim", "kd_n_points", "kd_leafsize", "kd_n_nodes"):
         getattr(L, name).argtypes = [P]
         getattr(L, name).restype = u64
@@ -233,6 +235,36 @@ class KDTree:
         if single:
             return out_d[0], out_i[0]
         return out_d, out_i
+
+    def query_async(self, queries, out_distances, out_indices, status, *, k: int = 1, p: float = 2.0,
+                    max_distance: float | None = None, eps: float = 0.0, stream=None):
+        """Stream-ordered query on device arrays (kd_query_async): queries
+        [n, ndim] f64, out_distances [n, k] f64, out_indices [n, k] i64 and
+        status (one u32 / i32) are CUDA arrays (e.g. torch tensors); returns once
+        the work is enqueued on `stream` (an int handle, an object with
+        `cuda_stream`, or None for the legacy default stream).  After the stream
+        work, status bit 0 means a non-finite query, bit 1 a tensor-core wait
+        that ran out.  Host-checkable errors raise at once."""
+        iface = getattr(queries, "__cuda_array_interface__", None)
+        n = int(iface["shape"][0]) if iface else 0
+        k = _usize(k, "k")
+        if k == 0:  # the engine's own message (InvalidK)
+            one = ctypes.c_void_p(1)
+            _raise(_lib.kd_query_async(self._h, one, self._ndim, 0, 2.0, 0, 0.0, 0.0, one, one, one, None))
+        qa = _cuda_array(queries, "<f8", (n, self._ndim), "queries")
+        da = _cuda_array(out_distances, "<f8", (n, k), "out_distances")
+        ia = _cuda_array(out_indices, "<i8", (n, k), "out_indices")
+        siface = getattr(status, "__cuda_array_interface__", None)
+        if siface is None or siface["typestr"] not in ("<u4", "<i4"):
+            raise TypeError("status: expected a 4-byte integer CUDA array")
+        has_max = max_distance is not None
+        s = getattr(stream, "cuda_stream", stream)
+        st = _lib.kd_query_async(self._h, ctypes.c_void_p(qa), n * self._ndim, k, _f64(p), int(has_max),
+                                 _f64(max_distance) if has_max else 0.0, _f64(eps), ctypes.c_void_p(da),
+                                 ctypes.c_void_p(ia), ctypes.c_void_p(int(siface["data"][0])),
+                                 ctypes.c_void_p(s) if s else None)
+        if st != KD_OK:
+            _raise(st)
 
     # -- inspection (no reference counterpart in Python; mirrors Tree's fields)
     def _export(self):

@@ -42,7 +42,7 @@ def last_error(L):
 def test_header_declares_the_reference_entry_points():
     syms = declared_symbols()
     for s in ("kd_build", "kd_query", "kd_free", "kd_original_data", "kd_last_error", "kd_query_device",
-              "kd_build_device", "kd_export", "kd_count_nodes"):
+              "kd_build_device", "kd_export", "kd_count_nodes", "kd_query_async"):
         assert s in syms
 
 

@@ -72,8 +72,10 @@ __device__ __forceinline__ void warp_box_enc1(const float* b32, float my_qlo, fl
     lb = fold_lb<M>(lb, __shfl_xor_sync(FULL_MASK, lb, 1 << s));
     ub = fold_ub<M>(ub, __shfl_xor_sync(FULL_MASK, ub, 1 << s));
   }
-  *lb_out = __fmul_rd(lb, LB_SHRINK);
-  *ub_out = __fmul_ru(ub, UB_GROW);
+  // The folds above only span the first 2^ceil(log2 D) lanes of each half;
+  // every lane must take the same gate decision, so all take lane 0's sums.
+  *lb_out = __fmul_rd(__shfl_sync(FULL_MASK, lb, 0), LB_SHRINK);
+  *ub_out = __fmul_ru(__shfl_sync(FULL_MASK, ub, 0), UB_GROW);
 }
 
 template <int M, int D, int KS>

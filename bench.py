@@ -515,7 +515,7 @@ def serving_case(torch, duration_s=2.0, n_templates=256):
         `duration` s have passed; return (latencies, queries done, elapsed)."""
         busy = [False] * n_templates
         cv = threading.Condition()
-        pending, lat, done_q, finished = [], [], [0], [False]
+        pending, lat, lat_nq, done_q, finished = [], [], [], [0], [False]
 
         def waiter():
             while True:
@@ -529,6 +529,7 @@ def serving_case(torch, duration_s=2.0, n_templates=256):
                 with cv:
                     busy[j] = False
                     lat.append(l)
+                    lat_nq.append(templates[j][1].shape[0])
                     done_q[0] += templates[j][1].shape[0]
                     cv.notify_all()
 
@@ -565,10 +566,10 @@ def serving_case(torch, duration_s=2.0, n_templates=256):
             finished[0] = True
             cv.notify_all()
         th.join()
-        return np.array(lat) * 1e3, done_q[0], time.perf_counter() - t_start
+        return np.array(lat) * 1e3, done_q[0], time.perf_counter() - t_start, np.array(lat_nq)
 
     # peak: a closed loop keeping 64 requests in flight for 2 s
-    lat, q_done, el = run_load(None, duration_s, window=64)
+    lat, q_done, el, _ = run_load(None, duration_s, window=64)
     peak_rps = len(lat) / el
     out = {"trees": n_trees, "points": int(ns.sum()), "build_all_s": build_s, "templates": n_templates,
            "mean_queries_per_request": total_q / n_templates, "identical_to_lone_queries": identical,
@@ -576,10 +577,14 @@ def serving_case(torch, duration_s=2.0, n_templates=256):
                     "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))}}
     for frac in (0.5, 0.7, 0.9):
         rate = frac * peak_rps
-        lat, q_done, el = run_load(rate, duration_s)
+        lat, q_done, el, nqs = run_load(rate, duration_s)
+        small = lat[nqs <= 10_000]
         out[f"load_{int(frac * 100)}"] = {"offered_requests_per_s": rate, "requests": len(lat),
                                           "p50_ms": float(np.percentile(lat, 50)),
                                           "p99_ms": float(np.percentile(lat, 99)),
+                                          "p50_ms_le_10k": float(np.percentile(small, 50)) if len(small) else None,
+                                          "p99_ms_le_10k": float(np.percentile(small, 99)) if len(small) else None,
+                                          "requests_le_10k": int(len(small)),
                                           "sustained_queries_per_s": q_done / el}
     srv.close()
     del trees

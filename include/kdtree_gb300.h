@@ -228,11 +228,14 @@ void kd_batch_free(kd_batch* batch);
 
 /* ---- Serving: continuous batching over a fixed set of trees --------------
  * No reference counterpart: a request loop in front of `Tree::query`
- * (src/query.rs:29-78).  A scheduler thread forms a batch whenever one of two
- * batch slots is free: every waiting request that fits the slot, in arrival
- * order, runs as one batch (the kernels of kd_batch_run, plus per-request
- * launches for requests outside the packet traversal).  A request's results
- * are exactly kd_query's for the same tree and queries, whatever it is batched
+ * (src/query.rs:29-78).  A request runs as pieces of at most 16,384 queries
+ * (fewer for large k).  A scheduler thread forms a batch whenever one of two
+ * batch slots is free: every waiting single-piece request that fits the slot,
+ * in arrival order, then pieces of larger requests up to one piece's worth of
+ * queries, so a small request waits for about one piece of a large one, not
+ * its whole scan.  A batch runs the kernels of kd_batch_run (plus per-request
+ * launches for requests outside the fused kernel).  A request's results are
+ * exactly kd_query's for the same tree and queries, whatever it is batched
  * with. */
 typedef struct kd_server kd_server;
 
@@ -247,8 +250,10 @@ int kd_server_create(const kd_tree* const* trees, uint64_t n_trees, double p, in
 /* Queue a request for tree index `tree`: n_queries rows in HOST memory, k
  * results each into host out_distances / out_indices (n_queries * k).  The
  * three buffers must stay valid until kd_server_wait returns for the ticket.
- * Validated as kd_query validates a call (k > 0, n_queries > 0); a request
- * larger than one batch fails with KD_ERR_INVALID_ARGUMENT.  Returns at once. */
+ * Validated as kd_query validates a call (k > 0, n_queries > 0); a k whose
+ * results for even one query do not fit a batch fails with
+ * KD_ERR_INVALID_ARGUMENT.  Returns at once; the latency kd_server_wait
+ * reports runs to the completion of the request's last piece. */
 int kd_server_submit(kd_server* server, uint64_t tree, const double* queries, uint64_t n_queries, uint64_t k,
                      double* out_distances, int64_t* out_indices, uint64_t* ticket);
 

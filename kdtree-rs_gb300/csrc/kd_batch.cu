@@ -646,8 +646,18 @@ struct Request {
   int64_t* oi = nullptr;
   Clock::time_point t_submit;
   double latency = 0.0;
+  uint64_t pieces_left = 0;  // pieces not completed yet
   int status = KD_OK;
   bool done = false;
+};
+
+// A request runs as pieces of at most the server's slice size (queries
+// [q0, q0 + nq) of it), each one job of a batch: a large request's remaining
+// pieces queue behind requests that arrive after it, so those need not wait
+// for its whole scan.
+struct Piece {
+  Request* r;
+  uint64_t q0, nq;
 };
 
 // One batch in flight: device staging, batch buffers, pinned host tables.
@@ -661,7 +671,7 @@ struct Slot {
   uint32_t* status = nullptr;  // one word per job
   void* host = nullptr;        // pinned: tables, q_start, task_start, status words
   SideStreams side;
-  std::vector<Request*> reqs;
+  std::vector<Piece> pieces;
   int error = KD_OK;
   std::string error_msg;
   bool busy = false;
@@ -678,7 +688,10 @@ struct kd_server {
   Slot slots[2];
   std::mutex mu;
   std::condition_variable cv;  // queue, slots, completions
-  std::deque<Request*> queue;
+  uint64_t slice = 0;         // largest piece, in queries
+  uint64_t large_budget = 0;  // queries of large requests' pieces one batch admits
+  std::deque<Piece> small_q;  // requests of one piece, arrival order
+  std::deque<Piece> large_q;  // pieces of larger requests, arrival order
   std::deque<Slot*> inflight;
   std::unordered_map<uint64_t, Request*> reqs;
   uint64_t next_ticket = 1;
@@ -689,6 +702,10 @@ struct kd_server {
 namespace {
 
 constexpr uint64_t SERVER_JOBS = 4096;
+// Largest piece of a request, in queries: a batch holds every waiting small
+// request and at most one slice of the larger ones, so a small request waits
+// for at most about one slice's worth of GPU work ahead of it.
+constexpr uint64_t SERVER_SLICE = 16384;
 
 uint64_t host_bytes(const kd_server* s) {
   return round256(s->cap_jobs * sizeof(BatchJob)) + 2 * round256((s->cap_jobs + 1) * 4) +
@@ -699,16 +716,18 @@ uint64_t host_bytes(const kd_server* s) {
 int stage_batch(kd_server* s, Slot* sl) {
   DeviceScope scope(s->device);
   cudaStream_t st = sl->st;
-  const size_t n = sl->reqs.size();
+  const size_t n = sl->pieces.size();
   std::vector<JobSpec> specs(n);
   uint64_t in_off = 0, out_off = 0;
   for (size_t j = 0; j < n; ++j) {
-    Request* r = sl->reqs[j];
+    const Piece& pc = sl->pieces[j];
+    const Request* r = pc.r;
     const kd_tree* t = s->trees[r->tree];
-    specs[j] = JobSpec{t, sl->in + in_off, r->nq, r->k, sl->out_d + out_off, sl->out_i + out_off, sl->status + j};
-    KD_TRY_CUDA(cudaMemcpyAsync(sl->in + in_off, r->q, r->nq * t->ndim * sizeof(double), cudaMemcpyHostToDevice, st));
-    in_off += r->nq * t->ndim;
-    out_off += r->nq * r->k;
+    specs[j] = JobSpec{t, sl->in + in_off, pc.nq, r->k, sl->out_d + out_off, sl->out_i + out_off, sl->status + j};
+    KD_TRY_CUDA(cudaMemcpyAsync(sl->in + in_off, r->q + pc.q0 * t->ndim, pc.nq * t->ndim * sizeof(double),
+                                cudaMemcpyHostToDevice, st));
+    in_off += pc.nq * t->ndim;
+    out_off += pc.nq * r->k;
   }
   KD_TRY_CUDA(cudaMemsetAsync(sl->status, 0, n * sizeof(uint32_t), st));
   Layout L;
@@ -744,12 +763,16 @@ int stage_batch(kd_server* s, Slot* sl) {
 int deliver_batch(Slot* sl, uint32_t* h_status) {
   cudaStream_t st = sl->st;
   uint64_t out_off = 0;
-  for (Request* r : sl->reqs) {
-    KD_TRY_CUDA(cudaMemcpyAsync(r->od, sl->out_d + out_off, r->nq * r->k * sizeof(double), cudaMemcpyDeviceToHost, st));
-    KD_TRY_CUDA(cudaMemcpyAsync(r->oi, sl->out_i + out_off, r->nq * r->k * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-    out_off += r->nq * r->k;
+  for (const Piece& pc : sl->pieces) {
+    const Request* r = pc.r;
+    const uint64_t n = pc.nq * r->k;
+    KD_TRY_CUDA(cudaMemcpyAsync(r->od + pc.q0 * r->k, sl->out_d + out_off, n * sizeof(double), cudaMemcpyDeviceToHost,
+                                st));
+    KD_TRY_CUDA(cudaMemcpyAsync(r->oi + pc.q0 * r->k, sl->out_i + out_off, n * sizeof(int64_t),
+                                cudaMemcpyDeviceToHost, st));
+    out_off += n;
   }
-  KD_TRY_CUDA(cudaMemcpyAsync(h_status, sl->status, sl->reqs.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  KD_TRY_CUDA(cudaMemcpyAsync(h_status, sl->status, sl->pieces.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   KD_TRY_CUDA(cudaStreamSynchronize(st));
   return KD_OK;
 }
@@ -758,30 +781,38 @@ void scheduler_loop(kd_server* s) {
   std::unique_lock<std::mutex> lk(s->mu);
   for (;;) {
     Slot* free_slot = nullptr;
+    auto empty = [&] { return s->small_q.empty() && s->large_q.empty(); };
     s->cv.wait(lk, [&] {
       free_slot = !s->slots[0].busy ? &s->slots[0] : (!s->slots[1].busy ? &s->slots[1] : nullptr);
-      return (s->stop && s->queue.empty()) || (free_slot && !s->queue.empty());
+      return (s->stop && empty()) || (free_slot && !empty());
     });
-    if (s->queue.empty()) return;  // stopping, nothing left
-    // continuous batching: every waiting request that fits, in arrival order
+    if (empty()) return;  // stopping, nothing left
+    // continuous batching: every waiting single-piece request that fits, in
+    // arrival order, then pieces of larger requests up to large_budget queries
     Slot* sl = free_slot;
     sl->busy = true;
-    sl->reqs.clear();
-    uint64_t q = 0, in = 0, out = 0, bins = 0;
-    while (!s->queue.empty() && sl->reqs.size() < s->cap_jobs) {
-      Request* r = s->queue.front();
-      const kd_tree* t = s->trees[r->tree];
-      const uint64_t nb = r->nq >= SORT_MIN_QUERIES ? t->n_nodes : 1;
-      if (!sl->reqs.empty() && (q + r->nq > s->cap_q || in + r->nq * t->ndim > s->cap_in ||
-                                out + r->nq * r->k > s->cap_out || bins + nb > s->cap_bins))
-        break;
-      q += r->nq;
-      in += r->nq * t->ndim;
-      out += r->nq * r->k;
-      bins += nb;
-      sl->reqs.push_back(r);
-      s->queue.pop_front();
-    }
+    sl->pieces.clear();
+    uint64_t q = 0, in = 0, out = 0, bins = 0, large = 0;
+    auto take = [&](std::deque<Piece>& from, bool budget) {
+      while (!from.empty() && sl->pieces.size() < s->cap_jobs) {
+        const Piece pc = from.front();
+        const kd_tree* t = s->trees[pc.r->tree];
+        const uint64_t nb = pc.nq >= SORT_MIN_QUERIES ? t->n_nodes : 1;
+        if (!sl->pieces.empty() && (q + pc.nq > s->cap_q || in + pc.nq * t->ndim > s->cap_in ||
+                                    out + pc.nq * pc.r->k > s->cap_out || bins + nb > s->cap_bins))
+          return;
+        if (budget && large > 0 && large + pc.nq > s->large_budget) return;
+        q += pc.nq;
+        in += pc.nq * t->ndim;
+        out += pc.nq * pc.r->k;
+        bins += nb;
+        if (budget) large += pc.nq;
+        sl->pieces.push_back(pc);
+        from.pop_front();
+      }
+    };
+    take(s->small_q, false);
+    take(s->large_q, true);
     lk.unlock();
     const int rc = stage_batch(s, sl);
     lk.lock();
@@ -795,8 +826,10 @@ void scheduler_loop(kd_server* s) {
 void completer_loop(kd_server* s) {
   std::unique_lock<std::mutex> lk(s->mu);
   for (;;) {
-    s->cv.wait(lk, [&] { return !s->inflight.empty() || (s->stop && s->queue.empty() && !s->slots[0].busy &&
-                                                            !s->slots[1].busy); });
+    s->cv.wait(lk, [&] {
+      return !s->inflight.empty() ||
+             (s->stop && s->small_q.empty() && s->large_q.empty() && !s->slots[0].busy && !s->slots[1].busy);
+    });
     if (s->inflight.empty()) return;
     Slot* sl = s->inflight.front();
     lk.unlock();
@@ -814,13 +847,16 @@ void completer_loop(kd_server* s) {
     }
     const Clock::time_point now = Clock::now();
     lk.lock();
-    for (size_t j = 0; j < sl->reqs.size(); ++j) {
-      Request* r = sl->reqs[j];
-      r->status = err ? err : (h_status[j] ? KD_ERR_NONFINITE_DATA : KD_OK);
-      r->latency = std::chrono::duration<double>(now - r->t_submit).count();
-      r->done = true;
+    for (size_t j = 0; j < sl->pieces.size(); ++j) {
+      Request* r = sl->pieces[j].r;
+      const int st = err ? err : (h_status[j] ? KD_ERR_NONFINITE_DATA : KD_OK);
+      if (st && (!r->status || st != KD_ERR_NONFINITE_DATA)) r->status = st;  // device failures outrank
+      if (--r->pieces_left == 0) {
+        r->latency = std::chrono::duration<double>(now - r->t_submit).count();
+        r->done = true;
+      }
     }
-    sl->reqs.clear();
+    sl->pieces.clear();
     sl->busy = false;
     s->inflight.pop_front();
     s->cv.notify_all();
@@ -1003,6 +1039,8 @@ int kd_server_create(const kd_tree* const* trees, uint64_t n_trees, double p, in
   s->cap_out = cap * 64;
   s->cap_jobs = SERVER_JOBS;
   s->cap_bins = std::max(2 * nodes, nodes_max + SERVER_JOBS);
+  s->slice = std::min<uint64_t>(SERVER_SLICE, cap);
+  s->large_budget = s->slice;
   for (Slot& sl : s->slots) {
     char* extra = nullptr;
     const uint64_t extra_b = round256(s->cap_in * 8) + round256(s->cap_out * 8) * 2 + round256(SERVER_JOBS * 4);
@@ -1048,10 +1086,10 @@ int kd_server_submit(kd_server* s, uint64_t tree, const double* queries, uint64_
   const kd_tree* t = s->trees[tree];
   int rc = job_error(t, n_queries, k, queries, out_distances, out_indices, s->device, "request");
   if (rc) return rc;
-  const uint64_t nb = n_queries >= SORT_MIN_QUERIES ? t->n_nodes : 1;
-  if (n_queries > s->cap_q || n_queries * t->ndim > s->cap_in || n_queries * k > s->cap_out || nb > s->cap_bins)
-    return fail(KD_ERR_INVALID_ARGUMENT, "request exceeds the server's batch capacity (" +
-                                             std::to_string(s->cap_q) + " queries, " +
+  // a piece must fit one batch: the slice, fewer for wide rows or large k
+  const uint64_t piece = std::min({s->slice, s->cap_in / t->ndim, s->cap_out / k});
+  if (piece == 0)
+    return fail(KD_ERR_INVALID_ARGUMENT, "k = " + std::to_string(k) + " exceeds the server's batch capacity (" +
                                              std::to_string(s->cap_out) + " results)");
   Request* r = new (std::nothrow) Request();
   if (!r) return fail(KD_ERR_OUT_OF_MEMORY, "host allocation failed");
@@ -1062,6 +1100,7 @@ int kd_server_submit(kd_server* s, uint64_t tree, const double* queries, uint64_
   r->od = out_distances;
   r->oi = out_indices;
   r->t_submit = Clock::now();
+  r->pieces_left = (n_queries + piece - 1) / piece;
   {
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->stop) {
@@ -1070,7 +1109,12 @@ int kd_server_submit(kd_server* s, uint64_t tree, const double* queries, uint64_
     }
     r->ticket = s->next_ticket++;
     s->reqs[r->ticket] = r;
-    s->queue.push_back(r);
+    if (r->pieces_left == 1) {
+      s->small_q.push_back(Piece{r, 0, n_queries});
+    } else {
+      for (uint64_t q0 = 0; q0 < n_queries; q0 += piece)
+        s->large_q.push_back(Piece{r, q0, std::min(piece, n_queries - q0)});
+    }
   }
   s->cv.notify_all();
   *ticket = r->ticket;

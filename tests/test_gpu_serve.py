@@ -71,8 +71,38 @@ def test_bad_request_fails_alone():
     srv.wait(t_good2)
     with pytest.raises(ValueError, match="k must be greater than zero"):
         srv.submit(0, good, 0)
-    with pytest.raises(RuntimeError, match="capacity"):
-        srv.submit(0, gmm(5000, 3, rng), 4)
+    big = gmm(5000, 3, rng)  # larger than one batch: runs as two pieces
+    assert_bit_exact(srv.wait(srv.submit(0, big, 4))[:2], trees[0][0].query(big, k=4))
+    with pytest.raises(RuntimeError, match="capacity"):  # one query's results exceed a batch
+        srv.submit(0, good[:1], 300_000)
     with pytest.raises(ValueError, match="dimension mismatch"):
         srv.submit(1, good, 4)
+    srv.close()
+
+
+def test_large_requests_run_in_pieces_beside_small_ones():
+    """Requests above the 16,384-query piece size run as several pieces that
+    small requests overtake; each result still equals a lone query, and a
+    non-finite query in any piece fails the whole request."""
+    from kdtree import Server
+
+    rng = np.random.default_rng(77)
+    trees = _trees(rng)
+    srv = Server([t for t, _ in trees])
+    big = gmm(40_000, 3, rng)
+    bad_big = gmm(35_000, 8, rng)
+    bad_big[30_000, 2] = np.inf  # in its second piece
+    t_big = srv.submit(0, big, 16)
+    t_bad = srv.submit(1, bad_big, 4)
+    small = [(int(rng.integers(len(trees))), int(rng.integers(1, 500)), int(rng.integers(1, 30))) for _ in range(40)]
+    smalls = []
+    for ti, nq, k in small:
+        q = gmm(nq, trees[ti][1], rng)
+        smalls.append((ti, q, k, srv.submit(ti, q, k)))
+    for ti, q, k, tk in smalls:
+        assert_bit_exact(srv.wait(tk)[:2], trees[ti][0].query(q, k=k))
+    d, i, lat = srv.wait(t_big)
+    assert_bit_exact((d, i), trees[0][0].query(big, k=16))
+    with pytest.raises(ValueError, match="finite"):
+        srv.wait(t_bad)
     srv.close()

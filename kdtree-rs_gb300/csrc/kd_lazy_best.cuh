@@ -1,10 +1,12 @@
-// kd_lazy_best.cuh -- the k best candidates of one query, kept as FP32
-// enclosures of their exact FP64 reduced distances (BestK / Best1,
-// src/query.rs:379-494), for compile-time widths and the L1 / L2 / L-inf
-// metrics.  Included by kd_query.cu after its interval helpers.
+// kd_lazy_best.cuh -- the k best candidates of one query held by one thread,
+// kept as FP32 enclosures of their exact FP64 reduced distances (BestK /
+// Best1, src/query.rs:379-494): LazySet (register slots) and LazyHeap
+// (shared-memory max-heap) for the packet traversal's compile-time widths,
+// LazySetDyn for the tensor-core filter's runtime widths; plus the FP32 box
+// lower bound the packet traversal prunes with.  Included by the query
+// translation units after their interval helpers.
 //
-// Slots are sorted by (exact FP64 reduced distance, original index).  The first
-// K - k slots are placeholders ([-inf, -inf]: every candidate sorts after them);
+// Placeholder slots (k < K) are [-inf, -inf]: every candidate sorts after them;
 // empty slots are [+inf, +inf] with row ROW_NONE (exact +inf, index after all).
 // Each real slot keeps the tree row of its point: the exact value is recomputed
 // from the point's coordinates with the reference's operations whenever two
@@ -13,180 +15,6 @@
 #pragma once
 
 constexpr uint32_t ROW_NONE = 0xffffffffu;
-
-template <int M, int D, int K>
-struct LazyBest {
-  float lo[K], hi[K];
-  uint32_t row[K];
-  uint32_t chunk;  // bit j: slot j's point lies in a full Packed d8 chunk (kernel.rs:540-562)
-  float b_lo, b_hi;  // enclosure of the pruning bound min(k-th best, cutoff)
-  float cut_lo, cut_hi;
-  uint64_t cut_bits;
-  QMem<D> q;
-  const double* data;
-  const uint32_t* indices;
-
-  __device__ __forceinline__ void init(uint64_t k, double cutoff, const double* qg, const double* data_,
-                                       const uint32_t* indices_) {
-#pragma unroll
-    for (int j = 0; j < K; ++j) {
-      const bool pad = static_cast<uint64_t>(j) < K - k;
-      lo[j] = pad ? __int_as_float(0xff800000) : __int_as_float(0x7f800000);
-      hi[j] = lo[j];
-      row[j] = ROW_NONE;
-    }
-    chunk = 0;
-    cut_bits = dbits(cutoff);
-    cut_lo = mag_dn32(cut_bits);
-    cut_hi = mag_up32(cut_bits);
-    q.g = qg;
-    data = data_;
-    indices = indices_;
-    refresh();
-  }
-  __device__ __forceinline__ void refresh() {
-    b_lo = fminf(lo[K - 1], cut_lo);
-    b_hi = fminf(hi[K - 1], cut_hi);
-  }
-  __device__ __forceinline__ double exact_of(uint32_t r, bool in_chunk) const {
-    return exact_dist<M, D>(q, data + static_cast<uint64_t>(r) * D, D, S_PACKED, in_chunk, 0.0);
-  }
-  __device__ __forceinline__ void slot_exact(int j, double* x, uint32_t* id) const {
-    if (row[j] == ROW_NONE) {
-      *x = bitsd(INF_BITS);
-      *id = NO_ID;
-    } else {
-      *x = exact_of(row[j], (chunk >> j) & 1u);
-      *id = indices[row[j]];
-    }
-  }
-  // exact bound min(k-th best, cutoff) as bits (query.rs:452-459)
-  __device__ __forceinline__ uint64_t bound_exact() const {
-    double kth;
-    uint32_t id;
-    slot_exact(K - 1, &kth, &id);
-    const uint64_t kb = dbits(kth);
-    return kb < cut_bits ? kb : cut_bits;
-  }
-
-  // Offer the point at tree row `r` whose exact distance lies in [clo, chi]:
-  // it is kept iff exact <= cutoff and (exact, id) sorts before the k-th best
-  // (LeafSink::offer + BestK::consider, query.rs:364-375, 461-481).
-  __device__ __forceinline__ void offer(float clo, float chi, uint32_t r, bool in_chunk) {
-    double cx = 0.0;
-    bool have_x = false;
-    if (!(chi <= cut_lo)) {  // the cutoff test, unless clearly inside
-      if (clo > cut_hi) return;
-      cx = exact_of(r, in_chunk);
-      have_x = true;
-      if (dbits(cx) > cut_bits) return;
-    }
-    bool lt[K];
-    uint32_t amb = 0;
-#pragma unroll
-    for (int j = 0; j < K; ++j) {
-      lt[j] = chi < lo[j];
-      if (!lt[j] && !(clo > hi[j])) amb |= 1u << j;
-    }
-    if (amb) {  // overlapping enclosures: decide on the exact values
-      if (!have_x) cx = exact_of(r, in_chunk);
-      const uint32_t cid = indices[r];
-      clo = mag_dn32(dbits(cx));
-      chi = mag_up32(dbits(cx));
-#pragma unroll
-      for (int j = 0; j < K; ++j) {
-        if ((amb >> j) & 1u) {
-          double ex;
-          uint32_t eid;
-          slot_exact(j, &ex, &eid);
-          lt[j] = dbits(cx) < dbits(ex) || (dbits(cx) == dbits(ex) && cid < eid);
-          if (row[j] != ROW_NONE) {  // keep the tighter enclosure
-            lo[j] = mag_dn32(dbits(ex));
-            hi[j] = mag_up32(dbits(ex));
-          }
-        }
-      }
-    }
-    if (!lt[K - 1]) return;  // not before the k-th best
-#pragma unroll
-    for (int j = K - 1; j > 0; --j) {
-      const bool take_prev = lt[j - 1];
-      const bool take_c = lt[j] && !lt[j - 1];
-      lo[j] = take_prev ? lo[j - 1] : (take_c ? clo : lo[j]);
-      hi[j] = take_prev ? hi[j - 1] : (take_c ? chi : hi[j]);
-      row[j] = take_prev ? row[j - 1] : (take_c ? r : row[j]);
-    }
-    if (lt[0]) {
-      lo[0] = clo;
-      hi[0] = chi;
-      row[0] = r;
-    }
-    if (D == 8) {  // insert the chunk flag at the same position
-      uint32_t pos = 0;
-#pragma unroll
-      for (int j = 0; j < K; ++j) pos += lt[j] ? 0u : 1u;
-      const uint32_t low = chunk & ((1u << pos) - 1u);
-      const uint32_t high = (chunk << 1) & ~((2u << pos) - 1u);
-      chunk = low | (static_cast<uint32_t>(in_chunk) << pos) | high;
-    }
-    refresh();
-  }
-
-  // Enclosure of a leaf point's exact distance from its FP32 copy.
-  __device__ __forceinline__ static void point_enclosure(const float* p32, const float* qlo, const float* qhi,
-                                                         float* clo, float* chi) {
-    float lb = 0.f, ub = 0.f;
-#pragma unroll
-    for (int i = 0; i < D; ++i) {
-      float plo, phi;
-      rn_enclose(p32[i], &plo, &phi);
-      lb = fold_lb<M>(lb, red_lb<M>(absdiff_lb(plo, phi, qlo[i], qhi[i])));
-      ub = fold_ub<M>(ub, red_ub<M>(absdiff_ub(plo, phi, qlo[i], qhi[i])));
-    }
-    // the FP64 distance is within d + 3 roundings of 2^-53 of the real one
-    *clo = __fmul_rd(lb, LB_SHRINK);
-    *chi = __fmul_ru(ub, UB_GROW);
-  }
-
-  // write_results (query.rs:421-429, 483-493): exact values of the k best.
-  __device__ __forceinline__ void write(double* od, int64_t* oi, uint64_t k, uint64_t n_points) const {
-#pragma unroll
-    for (int j = 0; j < K; ++j) {
-      if (static_cast<uint64_t>(j) >= K - k) {
-        const uint64_t o = j - (K - k);
-        if (row[j] != ROW_NONE) {
-          od[o] = restore<M>(exact_of(row[j], (chunk >> j) & 1u), 0.0);
-          oi[o] = static_cast<int64_t>(indices[row[j]]);
-        } else {
-          od[o] = bitsd(INF_BITS);
-          oi[o] = static_cast<int64_t>(n_points);
-        }
-      }
-    }
-  }
-};
-
-// Lower / upper bound of the exact FP64 box distance (kernel.rs:565-616) of a
-// query enclosed by [qlo, qhi] to the box whose outward-rounded FP32 copy is b32.
-template <int M, int D>
-__device__ __forceinline__ void box_enclosure(const float* b32, const float* qlo, const float* qhi, float* lb_out,
-                                              float* ub_out) {
-  float lb = 0.f, ub = 0.f;
-#pragma unroll
-  for (int i = 0; i < D; ++i) {
-    // lo in [lo32, lo32 + ulp], hi in [hi32 - ulp, hi32]
-    const float lo32 = b32[i], hi32 = b32[D + i];
-    const float lo_up = __fadd_ru(lo32, __fmaf_ru(fabsf(lo32), TWO_M23, TINY32));
-    const float hi_dn = __fsub_rd(hi32, __fmaf_ru(fabsf(hi32), TWO_M23, TINY32));
-    float o_lb = fmaxf(__fsub_rd(lo32, qhi[i]), __fsub_rd(qlo[i], hi32));
-    o_lb = o_lb > 0.f ? o_lb : 0.f;
-    const float o_ub = fmaxf(fmaxf(__fsub_ru(lo_up, qlo[i]), __fsub_ru(qhi[i], hi_dn)), 0.f);
-    lb = fold_lb<M>(lb, red_lb<M>(o_lb));
-    ub = fold_ub<M>(ub, red_ub<M>(o_ub));
-  }
-  *lb_out = __fmul_rd(lb, LB_SHRINK);
-  *ub_out = __fmul_ru(ub, UB_GROW);
-}
 
 // Lower bound only (the packet traversal's pruning test).
 template <int M, int D>
@@ -202,7 +30,7 @@ __device__ __forceinline__ float box_lb(const float* b32, const float* qlo, cons
 }
 
 // ---------------------------------------------------------------------------
-// LazySet: the same k best as LazyBest (BestK keeps the k smallest by
+// LazySet: the k best of one query (BestK keeps the k smallest by
 // (distance, index), query.rs:461-481 -- a set under a strict total order),
 // held unsorted: while slots are empty a candidate fills one (the reference
 // inserts unconditionally then); afterwards an accepted candidate replaces the

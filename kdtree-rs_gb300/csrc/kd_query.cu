@@ -459,8 +459,6 @@ __global__ void k_scatter_order(const uint32_t* leaf_of, uint32_t* offsets, uint
 // Below this many queries the ordering costs more than it saves.
 constexpr uint64_t ORDER_MIN_QUERIES = 4096;
 
-#include "kd_lazy_best.cuh"
-#include "kd_query_fast.cuh"
 
 // KD_QUERY_MODE=dfs runs every query through the reference-order descent (the
 // eps > 0 kernel) instead of the packet traversal; a diagnostic switch, same results.
@@ -472,29 +470,15 @@ bool force_reference_order() {
   return force;
 }
 
-template <int M, int D, int K>
-int launch(const QArgs& a, cudaStream_t st) {
-  const unsigned blocks = static_cast<unsigned>((a.nq + QUERY_THREADS - 1) / QUERY_THREADS);
-  if constexpr (D > 0 && M != M_LP && K > 0) {
-    if (a.n_points < ROW_NONE) {
-      k_query_fast<M, D, K><<<blocks, QUERY_THREADS, 0, st>>>(a);
-      KD_TRY_CUDA(cudaGetLastError());
-      return KD_OK;
-    }
-  }
-  k_query<M, D, K><<<blocks, QUERY_THREADS, 0, st>>>(a);
-  KD_TRY_CUDA(cudaGetLastError());
-  return KD_OK;
-}
-
+// The one-thread reference-order kernel, for what the warp kernels do not
+// take (k > 64, widths above 128): its k-best list lives in the query's own
+// output row, so any k fits.
 template <int M, int D>
 int dispatch_k(const QArgs& a, cudaStream_t st) {
-  if (a.k == 1) return launch<M, D, 1>(a, st);
-  if (a.k <= 4) return launch<M, D, 4>(a, st);
-  if (a.k <= 8) return launch<M, D, 8>(a, st);
-  if (a.k <= 16) return launch<M, D, 16>(a, st);
-  if (a.k <= 32) return launch<M, D, 32>(a, st);
-  return launch<M, D, 0>(a, st);
+  const unsigned blocks = static_cast<unsigned>((a.nq + QUERY_THREADS - 1) / QUERY_THREADS);
+  k_query<M, D, 0><<<blocks, QUERY_THREADS, 0, st>>>(a);
+  KD_TRY_CUDA(cudaGetLastError());
+  return KD_OK;
 }
 
 template <int M>

@@ -302,6 +302,16 @@ int kd_export(const kd_tree* tree, double* data, uint32_t* indices, uint32_t* no
  * text through `KDTreeError`'s Display (src/error.rs:18-51). */
 size_t kd_last_error(char* buf, size_t len);
 
+/* Page-locked host memory for result arrays (no reference counterpart: the
+ * reference's pyo3 layer returns fresh numpy arrays, src/lib.rs:86-98).
+ * kd_query writes each result row straight from the kernel into page-locked
+ * outputs (no download phase), while a freshly allocated pageable array first
+ * takes a page fault per page.  Blocks are pooled: kd_host_free keeps up to
+ * 4 GiB of freed blocks for later kd_host_alloc calls of about the same size;
+ * NULL and pointers this pool did not hand out are ignored. */
+int kd_host_alloc(uint64_t bytes, void** out);
+void kd_host_free(void* p);
+
 /* Number of nodes `count_nodes(n_points, leafsize)` (src/build.rs:166-173)
  * a tree of this size has; lets callers size kd_export buffers up front. */
 uint64_t kd_count_nodes(uint64_t n_points, uint64_t leafsize);

@@ -10,9 +10,11 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <new>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "kd_internal.hpp"
@@ -526,6 +528,67 @@ int kd_export(const kd_tree* t, double* data, uint32_t* indices, uint32_t* node_
   }
   KD_TRY_CUDA(cudaStreamSynchronize(st));
   return KD_OK;
+}
+
+// Page-locked host blocks for result arrays.  Kept for reuse up to
+// HOST_POOL_KEEP_BYTES: allocating (pinning) a block costs about 4 ms per
+// 128 MB, which a query loop would otherwise pay on every call.
+namespace {
+constexpr uint64_t HOST_POOL_KEEP_BYTES = 4ull << 30;
+std::mutex g_host_mu;
+std::multimap<uint64_t, void*> g_host_free;       // size -> block
+std::unordered_map<void*, uint64_t> g_host_size;  // every live or pooled block
+uint64_t g_host_free_bytes = 0;
+}  // namespace
+
+int kd_host_alloc(uint64_t bytes, void** out) {
+  if (!out) return fail(KD_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  const uint64_t want = std::max<uint64_t>(bytes, 1);
+  {
+    std::lock_guard<std::mutex> lock(g_host_mu);
+    auto it = g_host_free.lower_bound(want);
+    if (it != g_host_free.end() && it->first <= 2 * want) {  // reuse a block of about this size
+      *out = it->second;
+      g_host_free_bytes -= it->first;
+      g_host_free.erase(it);
+      return KD_OK;
+    }
+  }
+  const uint64_t size = (want + (2ull << 20) - 1) / (2ull << 20) * (2ull << 20);
+  void* p = nullptr;
+  cudaError_t e = cudaHostAlloc(&p, size, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    std::lock_guard<std::mutex> lock(g_host_mu);  // give the cached blocks back and try once more
+    for (auto& kv : g_host_free) {
+      g_host_size.erase(kv.second);
+      cudaFreeHost(kv.second);
+    }
+    g_host_free.clear();
+    g_host_free_bytes = 0;
+    cudaGetLastError();
+    e = cudaHostAlloc(&p, size, cudaHostAllocDefault);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaHostAlloc");
+  }
+  std::lock_guard<std::mutex> lock(g_host_mu);
+  g_host_size[p] = size;
+  *out = p;
+  return KD_OK;
+}
+
+void kd_host_free(void* p) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lock(g_host_mu);
+  auto it = g_host_size.find(p);
+  if (it == g_host_size.end()) return;  // not ours
+  const uint64_t size = it->second;
+  if (g_host_free_bytes + size > HOST_POOL_KEEP_BYTES) {
+    g_host_size.erase(it);
+    cudaFreeHost(p);
+    return;
+  }
+  g_host_free.emplace(size, p);
+  g_host_free_bytes += size;
 }
 
 size_t kd_last_error(char* buf, size_t len) {

@@ -21,6 +21,7 @@ from __future__ import annotations
 
 import ctypes
 import operator
+import weakref
 from pathlib import Path
 
 import numpy as np
@@ -78,6 +79,10 @@ def _load():
     L.kd_server_wait.restype = ctypes.c_int
     L.kd_server_free.argtypes = [P]
     L.kd_server_free.restype = None
+    L.kd_host_alloc.argtypes = [u64, ctypes.POINTER(P)]
+    L.kd_host_alloc.restype = ctypes.c_int
+    L.kd_host_free.argtypes = [P]
+    L.kd_host_free.restype = None
     L.kd_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.kd_last_error.restype = ctypes.c_size_t
     return L
@@ -148,6 +153,20 @@ def _as_points(obj, what: str, allow_single: bool):
 
 def _ptr(a: np.ndarray):
     return ctypes.c_void_p(a.ctypes.data)
+
+
+def _result_array(shape, dtype) -> np.ndarray:
+    """A fresh numpy array for query results, backed by a page-locked block
+    from the engine's pool (kd_host_alloc): the kernel writes result rows
+    straight into it.  The block goes back to the pool when the array (and
+    every view of it) is gone.  Plain numpy memory if pinning fails."""
+    n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+    p = ctypes.c_void_p()
+    if n == 0 or _lib.kd_host_alloc(n, ctypes.byref(p)) != KD_OK or not p.value:
+        return np.empty(shape, dtype)
+    buf = (ctypes.c_char * n).from_address(p.value)
+    weakref.finalize(buf, _lib.kd_host_free, ctypes.c_void_p(p.value))
+    return np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
 
 
 class KDTree:
@@ -226,8 +245,8 @@ class KDTree:
             st = _lib.kd_query(self._h, _ptr(q) if q.size else None, q.size, k, p, int(has_max), md, eps,
                                int(parallel), _ptr(dummy_d), _ptr(dummy_i))
             _raise(st if st != KD_OK else 10)
-        out_d = np.empty((nq, k), np.float64)
-        out_i = np.empty((nq, k), np.int64)
+        out_d = _result_array((nq, k), np.float64)
+        out_i = _result_array((nq, k), np.int64)
         st = _lib.kd_query(self._h, _ptr(q), q.size, k, p, int(has_max), md, eps, int(parallel), _ptr(out_d),
                            _ptr(out_i))
         if st != KD_OK:
@@ -395,7 +414,7 @@ class Server:
         k = _usize(k, "k")
         n = q.shape[0]
         if out is None:
-            out = (np.empty((n, k), np.float64), np.empty((n, k), np.int64))
+            out = (_result_array((n, k), np.float64), _result_array((n, k), np.int64))
         od, oi = out
         if od.shape != (n, k) or oi.shape != (n, k) or od.dtype != np.float64 or oi.dtype != np.int64 \
                 or not od.flags.c_contiguous or not oi.flags.c_contiguous:

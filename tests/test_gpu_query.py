@@ -166,3 +166,32 @@ def test_host_buffers_pinned_and_pageable(oracle, k):
     assert_bit_exact(outs[0], outs[1])
     o = oracle.OracleKDTree(data, leafsize=16).query(q[:3000], k=k, parallel=True)
     assert_bit_exact((outs[0][0][:3000], outs[0][1][:3000]), o)
+
+
+def test_result_arrays_come_from_the_page_locked_pool(oracle):
+    """KDTree.query returns ordinary numpy arrays backed by page-locked blocks
+    (kd_host_alloc), which the kernel writes directly; a block freed with its
+    arrays is handed out again, and results stay valid after the tree is gone."""
+    import ctypes
+
+    from kdtree import KDTree, _core
+
+    rng = np.random.default_rng(21)
+    data = rng.uniform(size=(50_000, 3))
+    q = rng.uniform(size=(20_000, 3))
+    tree = KDTree(data, leafsize=16)
+    want = oracle.OracleKDTree(data, leafsize=16).query(q, k=8, parallel=True)
+    d1, i1 = tree.query(q, k=8)
+    assert_bit_exact((d1, i1), want)
+    assert d1.flags.c_contiguous and d1.dtype == np.float64 and i1.dtype == np.int64
+    addr = d1.ctypes.data
+    del d1, i1
+    d2, i2 = tree.query(q, k=8)  # the freed blocks come back
+    assert d2.ctypes.data in (addr,) or i2.ctypes.data == addr
+    del tree
+    assert_bit_exact((d2, i2), want)
+    L = _core._lib
+    p = ctypes.c_void_p()
+    assert L.kd_host_alloc(1 << 20, ctypes.byref(p)) == 0 and p.value
+    L.kd_host_free(p)
+    L.kd_host_free(None)

@@ -694,6 +694,86 @@ def compact_cases(cases):
     return out
 
 
+PROFILE_CASES = {
+    "build": "kd_build, N=1,000,000 uniform d=3, leafsize 16 (every build kernel)",
+    "packet": "packet traversal, N=1M uniform d=3 leafsize 16, 200,000 queries, k=16 (with the landing-leaf sort)",
+    "warp16": "best-first warp, 64-component mixture d=16 sigma 0.01, N=1M, 20,000 queries, k=16",
+    "warpdyn": "best-first warp at a runtime width, normal d=20, N=200,000, 20,000 queries, k=8",
+    "ref": "reference-order warp kernel, eps=0.5, N=1M uniform d=3, 100,000 queries, k=16",
+    "onethread": "one-thread reference-order kernel (k > 64), N=1M uniform d=3, 20,000 queries, k=100",
+    "tc": "tensor-core filter, scaled normal d=64, N=100,000, 19,456 queries, k=32",
+    "batch": "batch plan: 64 trees N log-uniform [1e3, 2e5], d in {2,3,8}, 100k queries in all, k in {1,4,32}",
+}
+
+
+def run_profile_case(name):
+    """One small scenario per kernel family, the target of the per-kernel ncu
+    captures summarised under profiles/ (one kernel, one launch each)."""
+    import torch
+
+    from kdtree import BatchQuery, KDTree
+
+    lib = path_lib()
+    stream = torch.cuda.Stream()
+    rng = np.random.default_rng(77)
+    out = {"case": name}
+    t0 = time.perf_counter()
+    if name == "build":
+        data = np.random.default_rng(2).uniform(size=(N_POINTS, 3))
+        KDTree(data, leafsize=16)
+    elif name in ("packet", "ref", "onethread"):
+        data = np.random.default_rng(2).uniform(size=(N_POINTS, 3))
+        tree = KDTree(data, leafsize=16)
+        nq = {"packet": 200_000, "ref": 100_000, "onethread": 20_000}[name]
+        dq = torch.from_numpy(np.random.default_rng(3).uniform(size=(nq, 3))).cuda()
+        if name == "packet":
+            out["ms"] = time_path(lib, tree, dq, 16, 2.0, PATH_PACKET, 1, torch, stream)[0]
+        elif name == "onethread":
+            out["ms"] = time_path(lib, tree, dq, 100, 2.0, PATH_AUTO, 1, torch, stream)[0]
+        else:
+            od = torch.empty((nq, 16), dtype=torch.float64, device="cuda")
+            oi = torch.empty((nq, 16), dtype=torch.int64, device="cuda")
+            P = ctypes.c_void_p
+            st = lib.kd_query_device(tree._h, P(dq.data_ptr()), dq.numel(), 16, 2.0, 0, 0.0, 0.5, P(od.data_ptr()),
+                                     P(oi.data_ptr()), P(stream.cuda_stream))
+            torch.cuda.synchronize()
+            assert st == 0
+    elif name == "warp16":
+        c = rng.uniform(size=(64, 16))
+        data = c[rng.integers(0, 64, N_POINTS)] + 0.01 * rng.standard_normal((N_POINTS, 16))
+        q = c[rng.integers(0, 64, 20_000)] + 0.01 * rng.standard_normal((20_000, 16))
+        tree = KDTree(data)
+        out["ms"] = time_path(lib, tree, torch.from_numpy(q).cuda(), 16, 2.0, PATH_WARP, 1, torch, stream)[0]
+    elif name == "warpdyn":
+        data = rng.standard_normal((200_000, 20))
+        q = rng.standard_normal((20_000, 20))
+        tree = KDTree(data, leafsize=16)
+        out["ms"] = time_path(lib, tree, torch.from_numpy(q).cuda(), 8, 2.0, PATH_WARP, 1, torch, stream)[0]
+    elif name == "tc":
+        scale = np.exp(rng.uniform(np.log(0.1), np.log(10), 64))
+        data = rng.standard_normal((100_000, 64)) * scale
+        q = rng.standard_normal((152 * 128, 64)) * scale
+        tree = KDTree(data, leafsize=16)
+        out["ms"] = time_path(lib, tree, torch.from_numpy(q).cuda(), 32, 2.0, PATH_TENSOR_CORE, 1, torch, stream)[0]
+    elif name == "batch":
+        jobs = []
+        for _ in range(64):
+            n = int(np.exp(rng.uniform(np.log(1e3), np.log(2e5))))
+            d = int(rng.choice([2, 3, 8]))
+            nq = int(np.exp(rng.uniform(np.log(100), np.log(5000))))
+            k = int(rng.choice([1, 4, 32]))
+            jobs.append((KDTree(rng.uniform(size=(n, d))), torch.from_numpy(rng.uniform(size=(nq, d))).cuda(), k,
+                         torch.empty((nq, k), dtype=torch.float64, device="cuda"),
+                         torch.empty((nq, k), dtype=torch.int64, device="cuda")))
+        BatchQuery(jobs).run(stream, 1)  # the fused launches, no graph (the graph's first run tunes)
+    else:
+        raise SystemExit(f"unknown profile case {name!r}; cases: {', '.join(PROFILE_CASES)}")
+    torch.cuda.synchronize()
+    out["wall_s"] = time.perf_counter() - t0
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_profile_tc():
     """A tensor-core-path case small enough for an ncu capture: one CTA-filling
     batch (152 x 128 queries) against 100,000 points, d=64, k=32."""
@@ -753,7 +833,11 @@ def main():
     ap.add_argument("--profile-tc", action="store_true",
                     help="only run the tensor-core path on a profiling-sized case (N=100k, d=64, "
                          "19,456 queries, k=32), 3 calls")
+    ap.add_argument("--profile-case", default=None,
+                    help="only run one small scenario for a per-kernel ncu capture: " + ", ".join(PROFILE_CASES))
     args = ap.parse_args()
+    if args.profile_case:
+        return run_profile_case(args.profile_case)
     if args.impl == "reference":
         return run_reference(args)
     if args.profile_tc:

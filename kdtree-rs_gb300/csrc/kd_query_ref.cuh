@@ -43,11 +43,15 @@ struct RefFrame {
 enum RefFrameKind : uint32_t { RF_FAR = 0, RF_RESTORE = 1, RF_BOX_FAR = 2, RF_BOX_NEAR = 3 };
 constexpr int REF_FRAMES = 2 * KD_MAX_DEPTH;
 
-// Bytes of shared memory one warp of the reference-order kernel uses: its
-// frames, the CellBound axes (d doubles) and the FP32 query (w32 floats).
+// Shared memory of one warp of the reference-order kernel: its frames, the
+// CellBound axes (d doubles, padded to 16 bytes) and the FP32 query (w32
+// floats, read as float4: it must start on a 16-byte boundary).
+__host__ __device__ constexpr uint64_t ref_axes_offset() { return REF_FRAMES * sizeof(RefFrame); }
+__host__ __device__ constexpr uint64_t ref_q32_offset(uint64_t d) { return ref_axes_offset() + (8 * d + 15) / 16 * 16; }
 __host__ __device__ constexpr uint64_t ref_warp_smem(uint64_t d, uint64_t w32) {
-  return (REF_FRAMES * sizeof(RefFrame) + 8 * d + 4 * w32 + 15) / 16 * 16;
+  return (ref_q32_offset(d) + 4 * w32 + 15) / 16 * 16;
 }
+static_assert(ref_axes_offset() % 16 == 0, "frames keep the axes 16-byte aligned");
 
 // Lower and upper bounds of one box's exact FP64 distance, compile-time widths
 // <= 16 (both half-warps take the same box; lane i of a half dimension i).
@@ -305,8 +309,8 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query_ref(QArgs a, const uint
   const uint64_t per = ref_warp_smem(d, (D == 0 && M != M_LP) ? a.w32 : 0);
   unsigned char* base = ref_smem + wid * per;
   RefFrame* fr = reinterpret_cast<RefFrame*>(base);
-  double* axes = reinterpret_cast<double*>(base + REF_FRAMES * sizeof(RefFrame));
-  float* sq = reinterpret_cast<float*>(base + REF_FRAMES * sizeof(RefFrame) + 8 * d);
+  double* axes = reinterpret_cast<double*>(base + ref_axes_offset());
+  float* sq = reinterpret_cast<float*>(base + ref_q32_offset(d));
   const uint64_t n = count ? *count : a.nq;
   const uint64_t warps = static_cast<uint64_t>(gridDim.x) * (QUERY_THREADS / 32);
   for (uint64_t w = blockIdx.x * static_cast<uint64_t>(QUERY_THREADS / 32) + wid; w < n; w += warps) {

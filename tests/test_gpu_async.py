@@ -42,8 +42,10 @@ def test_async_equals_device_call(d, k, p, eps):
         od = torch.empty((dq.shape[0], k), dtype=torch.float64, device="cuda")
         oi = torch.empty((dq.shape[0], k), dtype=torch.int64, device="cuda")
         status = torch.full((1,), 7, dtype=torch.int32, device="cuda")
-        tree.query_async(dq, od, oi, status, k=k, p=p, eps=eps, stream=streams[i % 2])
         outs.append((od, oi, status))
+    torch.cuda.synchronize()  # the buffers' own fills (default stream) are done before the calls' streams start
+    for i, (dq, (od, oi, status)) in enumerate(zip(batches, outs)):
+        tree.query_async(dq, od, oi, status, k=k, p=p, eps=eps, stream=streams[i % 2])
     torch.cuda.synchronize()
     for dq, (od, oi, status) in zip(batches, outs):
         assert int(status.item()) == 0
@@ -91,11 +93,13 @@ def test_async_errors():
     od = torch.empty((100, 4), dtype=torch.float64, device="cuda")
     oi = torch.empty((100, 4), dtype=torch.int64, device="cuda")
     status = torch.full((1,), 12345, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
     tree.query_async(dq, od, oi, status, k=4)  # accepted: the non-finite query shows in the status
     torch.cuda.synchronize()
     assert int(status.item()) & 1
     # a scalar error raises at once; the finiteness check still lands in the status
     status.fill_(0)
+    torch.cuda.synchronize()
     with pytest.raises(ValueError, match="p must be finite"):
         tree.query_async(dq, od, oi, status, k=4, p=0.5)
     torch.cuda.synchronize()

@@ -143,13 +143,12 @@ __global__ void k_export_nodes(const DNode* nodes, uint64_t n_nodes, uint32_t* w
 void free_tree(kd_tree* t) {
   if (!t) return;
   DevicePin pin(t->device);
-  cudaFree(t->data);
-  cudaFree(t->indices);
-  cudaFree(t->nodes);
-  cudaFree(t->boxes);
-  if (t->data32w != t->data32) cudaFree(t->data32w);
-  cudaFree(t->data32);
-  cudaFree(t->boxes32);
+  if (t->block) {
+    // calls on other streams may still read the tree: let them finish, then
+    // return the block to the pool
+    cudaDeviceSynchronize();
+    cudaFreeAsync(t->block, thread_stream());
+  }
   cudaFree(t->tc_points);
   cudaFree(t->tc_w);
   cudaFree(t->tc_v);

@@ -821,6 +821,12 @@ __global__ void k_boxes_finalize(uint64_t* boxkeys, uint64_t total) {
   if (i < total) boxkeys[i] = from_total_key_bits(boxkeys[i]);
 }
 
+__global__ void k_root_segment(uint32_t* node, uint32_t* start, uint32_t* len, uint32_t n) {
+  *node = 0;
+  *start = 0;
+  *len = n;
+}
+
 __global__ void k_iota(uint32_t* idx, uint64_t n) {
   uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
   if (i < n) idx[i] = static_cast<uint32_t>(i);
@@ -847,24 +853,38 @@ __global__ void k_pad_rows(const float* src, uint64_t n, uint64_t d, uint64_t w,
   dst[f] = j < d ? src[r * d + j] : 0.f;
 }
 
-struct DevBuf {
-  void* p = nullptr;
-  ~DevBuf() {
-    if (p) cudaFree(p);
+// Arrays carved out of one device block, each starting on a 256-byte boundary:
+// a first pass with base == nullptr sizes the block, a second one sets the
+// pointers.
+struct Carve {
+  unsigned char* base = nullptr;
+  uint64_t off = 0;
+  template <typename T>
+  T* take(uint64_t count) {
+    T* q = base ? reinterpret_cast<T*>(base + off) : nullptr;
+    off += (std::max<uint64_t>(count, 1) * sizeof(T) + 255) / 256 * 256;
+    return q;
   }
 };
 
-template <typename T>
-int dalloc(DevBuf& b, uint64_t count) {
-  if (count == 0) count = 1;
-  cudaError_t e = cudaMalloc(&b.p, count * sizeof(T));
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    b.p = nullptr;
-    return fail(KD_ERR_OUT_OF_MEMORY, "device allocation failed");
+// A block from the library's stream-ordered pool, returned to it on the
+// build's stream unless handed to the tree.
+struct PoolBlock {
+  void* p = nullptr;
+  cudaStream_t st = nullptr;
+  ~PoolBlock() {
+    if (p) cudaFreeAsync(p, st);
   }
-  return KD_OK;
-}
+  int alloc(uint64_t bytes, cudaStream_t s) {
+    st = s;
+    if (dev_alloc(&p, bytes, s) != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      return fail(KD_ERR_OUT_OF_MEMORY, "device allocation failed");
+    }
+    return KD_OK;
+  }
+};
 
 inline unsigned grid1(uint64_t n, unsigned t) { return static_cast<unsigned>((n + t - 1) / t); }
 
@@ -912,70 +932,124 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
     if (s.any_inner && s.max_len > static_cast<uint64_t>(SMALL_MAX)) large_slots = std::max(large_slots, s.slots);
   const uint32_t max_chunks = static_cast<uint32_t>((n + LG_CHUNK - 1) / LG_CHUNK);
 
-  DevBuf data_a, data_b, idx_a, idx_b, nodes, boxes, node_len, seg_a[3], seg_b[3], status;
-  DevBuf keys, keys_out, rankbuf, plist, hist, sel_prefix, sel_rank, seg_dim, seg_pivot, seg_lt, chunk_cnt, seg_mis;
+  // Rows are permuted once per level with an inner node (every level but the
+  // last).  Level 0 reads the input itself; the levels then alternate between
+  // the tree's own row array and a scratch one, arranged so that the last level
+  // writes the tree's.
+  const size_t n_perm = shape.size() - 1;
+  const bool need_pad = warp_runtime_width(d) && (d + 3) / 4 * 4 != d;
+  const uint64_t w32 = (d + 3) / 4 * 4;
+
+  // The tree's arrays: one pool block, owned by the tree.
+  struct TreeArrays {
+    double* data;
+    uint32_t* idx;
+    DNode* nodes;
+    uint64_t* boxes;
+    float *data32, *boxes32, *data32w;
+  } T{};
+  auto carve_tree = [&](Carve& c) {
+    T.data = c.take<double>(n * d);
+    T.idx = c.take<uint32_t>(n);
+    T.nodes = c.take<DNode>(n_nodes);
+    T.boxes = c.take<uint64_t>(n_nodes * 2 * d);
+    T.data32 = c.take<float>(n * d);
+    T.boxes32 = c.take<float>(n_nodes * 2 * d);
+    T.data32w = need_pad ? c.take<float>(n * w32) : nullptr;
+  };
+  // Scratch: one pool block, returned on the build's stream at the end.
+  struct Scratch {
+    double* data;
+    uint32_t* idx;
+    uint32_t* node_len;
+    uint32_t* status;
+    uint32_t* seg[2][3];
+    LargeScratch lg;
+  } X{};
+  auto carve_scratch = [&](Carve& c) {
+    X.data = c.take<double>(n * d);
+    X.idx = c.take<uint32_t>(n);
+    X.node_len = c.take<uint32_t>(n_nodes);
+    X.status = c.take<uint32_t>(1);
+    for (auto& sg : X.seg)
+      for (auto& a : sg) a = c.take<uint32_t>(max_slots);
+    if (large_slots) {
+      X.lg.keys = c.take<uint64_t>(n);
+      X.lg.keys_out = c.take<uint64_t>(n);
+      X.lg.rankbuf = c.take<uint32_t>(n);
+      X.lg.plist = c.take<uint32_t>(n);
+      X.lg.hist = c.take<uint32_t>(large_slots * RADIX_PASSES * 256);
+      X.lg.sel_prefix = c.take<uint64_t>(large_slots * (RADIX_PASSES + 1));
+      X.lg.sel_rank = c.take<uint32_t>(large_slots * (RADIX_PASSES + 1));
+      X.lg.seg_dim = c.take<uint32_t>(large_slots);
+      X.lg.seg_pivot = c.take<uint64_t>(large_slots);
+      X.lg.seg_lt = c.take<uint32_t>(large_slots);
+      X.lg.chunk_cnt = c.take<uint32_t>(large_slots * static_cast<uint64_t>(max_chunks));
+      X.lg.seg_mis = c.take<uint32_t>(large_slots);
+    }
+  };
+  PoolBlock tree_block, scratch_block;
   int rc;
-  if ((rc = dalloc<double>(data_a, n * d)) || (rc = dalloc<double>(data_b, n * d)) ||
-      (rc = dalloc<uint32_t>(idx_a, n)) || (rc = dalloc<uint32_t>(idx_b, n)) ||
-      (rc = dalloc<DNode>(nodes, n_nodes)) || (rc = dalloc<uint64_t>(boxes, n_nodes * 2 * d)) ||
-      (rc = dalloc<uint32_t>(node_len, n_nodes)) || (rc = dalloc<uint32_t>(status, 1)))
-    return rc;
-  for (int i = 0; i < 3; ++i)
-    if ((rc = dalloc<uint32_t>(seg_a[i], max_slots)) || (rc = dalloc<uint32_t>(seg_b[i], max_slots))) return rc;
-  if (large_slots) {
-    if ((rc = dalloc<uint64_t>(keys, n)) || (rc = dalloc<uint64_t>(keys_out, n)) ||
-        (rc = dalloc<uint32_t>(rankbuf, n)) || (rc = dalloc<uint32_t>(plist, n)) ||
-        (rc = dalloc<uint32_t>(hist, large_slots * RADIX_PASSES * 256)) ||
-        (rc = dalloc<uint64_t>(sel_prefix, large_slots * (RADIX_PASSES + 1))) ||
-        (rc = dalloc<uint32_t>(sel_rank, large_slots * (RADIX_PASSES + 1))) ||
-        (rc = dalloc<uint32_t>(seg_dim, large_slots)) || (rc = dalloc<uint64_t>(seg_pivot, large_slots)) ||
-        (rc = dalloc<uint32_t>(seg_lt, large_slots)) ||
-        (rc = dalloc<uint32_t>(chunk_cnt, large_slots * static_cast<uint64_t>(max_chunks))) ||
-        (rc = dalloc<uint32_t>(seg_mis, large_slots)))
-      return rc;
-  }
-
-  KD_TRY_CUDA(cudaMemcpyAsync(data_a.p, d_src, n * d * sizeof(double), cudaMemcpyDeviceToDevice, st));
-  k_iota<<<grid1(n, 256), 256, 0, st>>>(static_cast<uint32_t*>(idx_a.p), n);
-  k_init_boxkeys<<<grid1(2 * d, 256), 256, 0, st>>>(static_cast<uint64_t*>(boxes.p), 1, d);
-  KD_TRY_CUDA(cudaMemsetAsync(status.p, 0, sizeof(uint32_t), st));
   {
-    uint32_t root[3] = {0, 0, static_cast<uint32_t>(n)};
-    for (int i = 0; i < 3; ++i)
-      KD_TRY_CUDA(cudaMemcpyAsync(seg_a[i].p, &root[i], sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    Carve ct, cs;
+    carve_tree(ct);
+    carve_scratch(cs);
+    if ((rc = tree_block.alloc(ct.off, st)) || (rc = scratch_block.alloc(cs.off, st))) return rc;
+    ct = Carve{static_cast<unsigned char*>(tree_block.p), 0};
+    cs = Carve{static_cast<unsigned char*>(scratch_block.p), 0};
+    carve_tree(ct);
+    carve_scratch(cs);
   }
+  // level lv writes the tree's arrays when (n_perm - 1 - lv) is even
+  auto writes_tree = [&](size_t lv) { return ((n_perm - 1 - lv) & 1) == 0; };
 
-  double* din = static_cast<double*>(data_a.p);
-  double* dout = static_cast<double*>(data_b.p);
-  uint32_t* iin = static_cast<uint32_t*>(idx_a.p);
-  uint32_t* iout = static_cast<uint32_t*>(idx_b.p);
-  DevBuf* scur = seg_a;
-  DevBuf* snxt = seg_b;
+  k_init_boxkeys<<<grid1(2 * d, 256), 256, 0, st>>>(T.boxes, 1, d);
+  KD_TRY_CUDA(cudaMemsetAsync(X.status, 0, sizeof(uint32_t), st));
+  const double* din;
+  const uint32_t* iin;
+  if (n_perm == 0) {  // the root is a leaf
+    KD_TRY_CUDA(cudaMemcpyAsync(T.data, d_src, n * d * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    k_iota<<<grid1(n, 256), 256, 0, st>>>(T.idx, n);
+    din = T.data;
+    iin = T.idx;
+  } else {
+    // the identity permutation sits in the index array level 0 does not write
+    uint32_t* iota = writes_tree(0) ? X.idx : T.idx;
+    k_iota<<<grid1(n, 256), 256, 0, st>>>(iota, n);
+    din = d_src;
+    iin = iota;
+  }
+  k_root_segment<<<1, 1, 0, st>>>(X.seg[0][0], X.seg[0][1], X.seg[0][2], static_cast<uint32_t>(n));
+  KD_TRY_CUDA(cudaGetLastError());
+  KD_TRY_CUDA(cudaFuncSetAttribute(k_small_level, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(SMALL_MAX * (sizeof(uint64_t) + 2 * sizeof(uint16_t)))));
+
+  int cur = 0;
   const unsigned bbox_threads = d <= 256 ? static_cast<unsigned>(d * (256 / d)) : 256u;
 
   for (size_t lv = 0; lv < shape.size(); ++lv) {
     const LevelShape& s = shape[lv];
+    double* dout = nullptr;
+    uint32_t* iout = nullptr;
+    if (lv < n_perm) {
+      dout = writes_tree(lv) ? T.data : X.data;
+      iout = writes_tree(lv) ? T.idx : X.idx;
+    }
     Level L{din, dout, iin, iout, d, leafsize,
-            static_cast<uint32_t*>(scur[0].p), static_cast<uint32_t*>(scur[1].p), static_cast<uint32_t*>(scur[2].p),
-            static_cast<uint32_t*>(snxt[0].p), static_cast<uint32_t*>(snxt[1].p), static_cast<uint32_t*>(snxt[2].p),
-            static_cast<DNode*>(nodes.p), static_cast<uint64_t*>(boxes.p), static_cast<uint32_t*>(node_len.p),
-            s.slots};
+            X.seg[cur][0], X.seg[cur][1], X.seg[cur][2],
+            X.seg[cur ^ 1][0], X.seg[cur ^ 1][1], X.seg[cur ^ 1][2],
+            T.nodes, T.boxes, X.node_len, s.slots};
     // Boxes: the root and every level below the large path's levels come from
     // the bbox kernel (the small path initialises its children's box keys).
+    // Level 0 also checks that every coordinate is finite; the status is read
+    // once the build has finished (non-finite keys still order consistently).
     {
       const uint64_t chunk_rows = std::max<uint64_t>(1, (bbox_threads * 8) / d);
       const uint64_t nchunk = (s.max_len + chunk_rows - 1) / chunk_rows;
       dim3 g(static_cast<unsigned>(s.slots), static_cast<unsigned>(std::min<uint64_t>(nchunk, 65535)));
       k_bbox<<<g, bbox_threads, 2 * d * sizeof(uint64_t), st>>>(L, static_cast<uint32_t>(chunk_rows),
-                                                                static_cast<uint32_t>(nchunk), lv == 0,
-                                                                static_cast<uint32_t*>(status.p));
+                                                                static_cast<uint32_t>(nchunk), lv == 0, X.status);
       KD_TRY_CUDA(cudaGetLastError());
-    }
-    if (lv == 0) {
-      uint32_t h_status = 0;
-      KD_TRY_CUDA(cudaMemcpyAsync(&h_status, status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-      KD_TRY_CUDA(cudaStreamSynchronize(st));
-      if (h_status) return fail(KD_ERR_NONFINITE_DATA, "all coordinates must be finite");
     }
     if (!s.any_inner) {
       k_leaf_records<<<grid1(s.slots, 256), 256, 0, st>>>(L);
@@ -984,20 +1058,13 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
     }
     if (s.max_len <= static_cast<uint64_t>(SMALL_MAX)) {
       const size_t smem = SMALL_MAX * (sizeof(uint64_t) + 2 * sizeof(uint16_t));
-      KD_TRY_CUDA(cudaFuncSetAttribute(k_small_level, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(smem)));
       k_small_level<<<static_cast<unsigned>(s.slots), SMALL_THREADS, smem, st>>>(L);
       KD_TRY_CUDA(cudaGetLastError());
     } else {
-      LargeScratch S{static_cast<uint64_t*>(keys.p),     static_cast<uint64_t*>(keys_out.p),
-                     static_cast<uint32_t*>(rankbuf.p),  static_cast<uint32_t*>(plist.p),
-                     static_cast<uint32_t*>(hist.p),     static_cast<uint64_t*>(sel_prefix.p),
-                     static_cast<uint32_t*>(sel_rank.p), static_cast<uint32_t*>(seg_dim.p),
-                     static_cast<uint64_t*>(seg_pivot.p), static_cast<uint32_t*>(seg_lt.p),
-                     static_cast<uint32_t*>(chunk_cnt.p), static_cast<uint32_t*>(seg_mis.p)};
+      const LargeScratch& S = X.lg;
       const uint32_t nch = static_cast<uint32_t>((s.max_len + LG_CHUNK - 1) / LG_CHUNK);
       dim3 g(static_cast<unsigned>(s.slots), std::min<uint32_t>(nch, 65535u));
-      KD_TRY_CUDA(cudaMemsetAsync(hist.p, 0, s.slots * RADIX_PASSES * 256 * sizeof(uint32_t), st));
+      KD_TRY_CUDA(cudaMemsetAsync(S.hist, 0, s.slots * RADIX_PASSES * 256 * sizeof(uint32_t), st));
       k_lg_prepare<<<grid1(s.slots, 256), 256, 0, st>>>(L, S);
       k_lg_keys<<<g, LG_THREADS, 0, st>>>(L, S);
       for (int pass = 0; pass < RADIX_PASSES; ++pass) k_lg_hist<<<g, LG_THREADS, 0, st>>>(L, S, pass);
@@ -1010,27 +1077,32 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
       k_lg_expand<<<grid1(s.slots, 256), 256, 0, st>>>(L, S);
       KD_TRY_CUDA(cudaGetLastError());
     }
-    std::swap(din, dout);
-    std::swap(iin, iout);
-    std::swap(scur, snxt);
+    din = dout;
+    iin = iout;
+    cur ^= 1;
   }
 
-  k_order_by_box<<<grid1(n_nodes, 256), 256, 0, st>>>(static_cast<DNode*>(nodes.p), static_cast<uint64_t*>(boxes.p),
-                                                      static_cast<uint32_t*>(node_len.p), n_nodes, d);
-  k_boxes_finalize<<<grid1(n_nodes * 2 * d, 256), 256, 0, st>>>(static_cast<uint64_t*>(boxes.p), n_nodes * 2 * d);
+  k_order_by_box<<<grid1(n_nodes, 256), 256, 0, st>>>(T.nodes, T.boxes, X.node_len, n_nodes, d);
+  k_boxes_finalize<<<grid1(n_nodes * 2 * d, 256), 256, 0, st>>>(T.boxes, n_nodes * 2 * d);
   KD_TRY_CUDA(cudaGetLastError());
 
-  // The final row order sits in `din` (the last level's destination, or the
-  // copy of the input when the root is a leaf).
-  DevBuf data32, boxes32;
-  if ((rc = dalloc<float>(data32, n * d)) || (rc = dalloc<float>(boxes32, n_nodes * 2 * d))) return rc;
+  // The final row order sits in the tree's row array (din).
   k_make_f32<<<grid1(std::max(n * d, n_nodes * 2 * d), 256), 256, 0, st>>>(
-      din, static_cast<float*>(data32.p), n * d, reinterpret_cast<const double*>(boxes.p),
-      static_cast<float*>(boxes32.p), n_nodes, d);
+      T.data, T.data32, n * d, reinterpret_cast<const double*>(T.boxes), T.boxes32, n_nodes, d);
   KD_TRY_CUDA(cudaGetLastError());
+  // FP32 rows padded for the runtime-width warp kernels (widths other than 1,
+  // 2, 3, 4, 8, 16, up to 128): the FP32 copy itself when d is a multiple of 4
+  if (need_pad) {
+    k_pad_rows<<<grid1(n * w32, 256), 256, 0, st>>>(T.data32, n, d, w32, T.data32w);
+    KD_TRY_CUDA(cudaGetLastError());
+  }
+  // The one host synchronisation: the finiteness status and the root box.
   std::vector<double> root_box(2 * d);
-  KD_TRY_CUDA(cudaMemcpyAsync(root_box.data(), boxes.p, 2 * d * sizeof(double), cudaMemcpyDeviceToHost, st));
+  uint32_t h_status = 0;
+  KD_TRY_CUDA(cudaMemcpyAsync(&h_status, X.status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  KD_TRY_CUDA(cudaMemcpyAsync(root_box.data(), T.boxes, 2 * d * sizeof(double), cudaMemcpyDeviceToHost, st));
   KD_TRY_CUDA(cudaStreamSynchronize(st));
+  if (h_status) return fail(KD_ERR_NONFINITE_DATA, "all coordinates must be finite");
   double cmax = 0.0;  // the root box holds every coordinate
   for (double v : root_box) cmax = std::max(cmax, std::fabs(v));
   float cmax32 = static_cast<float>(cmax);
@@ -1041,35 +1113,16 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
   t->ndim = d;
   t->leafsize = leafsize;
   t->n_nodes = n_nodes;
-  // hand the final buffers to the tree; the DevBuf destructors free the rest
-  DevBuf* final_data = (din == data_a.p) ? &data_a : &data_b;
-  DevBuf* final_idx = (iin == idx_a.p) ? &idx_a : &idx_b;
-  t->data = static_cast<double*>(final_data->p);
-  final_data->p = nullptr;
-  t->indices = static_cast<uint32_t*>(final_idx->p);
-  final_idx->p = nullptr;
-  t->nodes = static_cast<DNode*>(nodes.p);
-  nodes.p = nullptr;
-  t->boxes = reinterpret_cast<double*>(boxes.p);
-  boxes.p = nullptr;
-  // FP32 rows padded for the runtime-width warp kernels (widths other than 1,
-  // 2, 3, 4, 8, 16, up to 128): the FP32 copy itself when d is a multiple of 4
-  t->w32 = static_cast<uint32_t>((d + 3) / 4 * 4);
-  if (warp_runtime_width(d) && t->w32 != d) {
-    DevBuf padded;
-    if ((rc = dalloc<float>(padded, n * t->w32))) return rc;
-    k_pad_rows<<<grid1(n * t->w32, 256), 256, 0, st>>>(static_cast<const float*>(data32.p), n, d, t->w32,
-                                                       static_cast<float*>(padded.p));
-    KD_TRY_CUDA(cudaGetLastError());
-    t->data32w = static_cast<float*>(padded.p);
-    padded.p = nullptr;
-  } else {
-    t->data32w = static_cast<float*>(data32.p);
-  }
-  t->data32 = static_cast<float*>(data32.p);
-  data32.p = nullptr;
-  t->boxes32 = static_cast<float*>(boxes32.p);
-  boxes32.p = nullptr;
+  t->block = tree_block.p;
+  tree_block.p = nullptr;
+  t->data = T.data;
+  t->indices = T.idx;
+  t->nodes = T.nodes;
+  t->boxes = reinterpret_cast<double*>(T.boxes);
+  t->data32 = T.data32;
+  t->boxes32 = T.boxes32;
+  t->w32 = static_cast<uint32_t>(w32);
+  t->data32w = need_pad ? T.data32w : T.data32;
   return KD_OK;
 }
 

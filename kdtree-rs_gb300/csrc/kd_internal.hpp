@@ -18,6 +18,9 @@ struct kd_tree {
   uint64_t leafsize = 0;
   uint64_t n_nodes = 0;
   int device = 0;
+  // One block from the library's device pool holds the arrays below up to
+  // data32w; the tensor-core arrays are separate allocations.
+  void* block = nullptr;
   double* data = nullptr;       // n_points * ndim, tree (leaf-contiguous) order
   uint32_t* indices = nullptr;  // tree position -> original row
   kd::DNode* nodes = nullptr;   // n_nodes, preorder

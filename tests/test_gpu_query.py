@@ -173,6 +173,7 @@ def test_result_arrays_come_from_the_page_locked_pool(oracle):
     (kd_host_alloc), which the kernel writes directly; a block freed with its
     arrays is handed out again, and results stay valid after the tree is gone."""
     import ctypes
+    import gc
 
     from kdtree import KDTree, _core
 
@@ -184,14 +185,20 @@ def test_result_arrays_come_from_the_page_locked_pool(oracle):
     d1, i1 = tree.query(q, k=8)
     assert_bit_exact((d1, i1), want)
     assert d1.flags.c_contiguous and d1.dtype == np.float64 and i1.dtype == np.int64
-    addr = d1.ctypes.data
+    addrs = {d1.ctypes.data, i1.ctypes.data}
     del d1, i1
-    d2, i2 = tree.query(q, k=8)  # the freed blocks come back
-    assert d2.ctypes.data in (addr,) or i2.ctypes.data == addr
-    del tree
-    assert_bit_exact((d2, i2), want)
+    gc.collect()  # numpy's comparison helpers can leave the arrays in a reference cycle
     L = _core._lib
     p = ctypes.c_void_p()
+    assert L.kd_host_alloc(20_000 * 8 * 8, ctypes.byref(p)) == 0 and p.value in addrs  # a freed block comes back
+    L.kd_host_free(p)
+    d2, i2 = tree.query(q, k=8)
+    assert {d2.ctypes.data, i2.ctypes.data} == addrs
+    del tree
+    assert_bit_exact((d2, i2), want)
     assert L.kd_host_alloc(1 << 20, ctypes.byref(p)) == 0 and p.value
+    q_ = ctypes.c_void_p(p.value)
+    L.kd_host_free(p)
+    assert L.kd_host_alloc(1 << 20, ctypes.byref(p)) == 0 and p.value == q_.value
     L.kd_host_free(p)
     L.kd_host_free(None)

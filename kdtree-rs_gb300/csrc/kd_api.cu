@@ -530,7 +530,8 @@ int kd_export(const kd_tree* t, double* data, uint32_t* indices, uint32_t* node_
 }
 
 // Page-locked host blocks for result arrays.  Kept for reuse up to
-// HOST_POOL_KEEP_BYTES: allocating (pinning) a block costs about 4 ms per
+// HOST_POOL_KEEP_BYTES (the largest cached blocks are unpinned first to make
+// room for a freed one): allocating (pinning) a block costs about 4 ms per
 // 128 MB, which a query loop would otherwise pay on every call.
 namespace {
 constexpr uint64_t HOST_POOL_KEEP_BYTES = 4ull << 30;
@@ -581,10 +582,19 @@ void kd_host_free(void* p) {
   auto it = g_host_size.find(p);
   if (it == g_host_size.end()) return;  // not ours
   const uint64_t size = it->second;
-  if (g_host_free_bytes + size > HOST_POOL_KEEP_BYTES) {
+  if (size > HOST_POOL_KEEP_BYTES) {
     g_host_size.erase(it);
     cudaFreeHost(p);
     return;
+  }
+  // the block just freed is the likeliest to be asked for again: make room
+  // for it by unpinning the largest cached blocks
+  while (g_host_free_bytes + size > HOST_POOL_KEEP_BYTES) {
+    auto big = std::prev(g_host_free.end());
+    g_host_free_bytes -= big->first;
+    g_host_size.erase(big->second);
+    cudaFreeHost(big->second);
+    g_host_free.erase(big);
   }
   g_host_free.emplace(size, p);
   g_host_free_bytes += size;

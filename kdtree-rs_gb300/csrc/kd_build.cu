@@ -937,7 +937,7 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
   // the tree's own row array and a scratch one, arranged so that the last level
   // writes the tree's.
   const size_t n_perm = shape.size() - 1;
-  const bool need_pad = warp_runtime_width(d) && (d + 3) / 4 * 4 != d;
+  const bool need_pad = padded_rows(d) && (d + 3) / 4 * 4 != d;
   const uint64_t w32 = (d + 3) / 4 * 4;
 
   // The tree's arrays: one pool block, owned by the tree.
@@ -1090,8 +1090,9 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
   k_make_f32<<<grid1(std::max(n * d, n_nodes * 2 * d), 256), 256, 0, st>>>(
       T.data, T.data32, n * d, reinterpret_cast<const double*>(T.boxes), T.boxes32, n_nodes, d);
   KD_TRY_CUDA(cudaGetLastError());
-  // FP32 rows padded for the runtime-width warp kernels (widths other than 1,
-  // 2, 3, 4, 8, 16, up to 128): the FP32 copy itself when d is a multiple of 4
+  // FP32 rows padded to a multiple of 4 floats for width 3 and the
+  // runtime-width warp kernels (widths other than 1, 2, 3, 4, 8, 16, up to
+  // 128): the FP32 copy itself when d is a multiple of 4
   if (need_pad) {
     k_pad_rows<<<grid1(n * w32, 256), 256, 0, st>>>(T.data32, n, d, w32, T.data32w);
     KD_TRY_CUDA(cudaGetLastError());

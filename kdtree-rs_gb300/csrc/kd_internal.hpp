@@ -29,8 +29,8 @@ struct kd_tree {
   float* boxes32 = nullptr;     // n_nodes * 2 * ndim, [lo rounded down | hi rounded up]
   float coord_max32 = 0.f;      // FP32 upper bound of every |coordinate| (the root box)
   // FP32 rows padded to w32 = ndim rounded up to a multiple of 4 floats, for
-  // the runtime-width warp kernels (made by the build; data32 itself when
-  // ndim is a multiple of 4 or the width has compile-time kernels).
+  // width 3 and the runtime-width warp kernels (made by the build; data32
+  // itself when ndim is a multiple of 4 or another compile-time width).
   float* data32w = nullptr;
   uint32_t w32 = 0;
   // Tensor-core filter inputs, made on first use (guarded by tc_mutex):
@@ -58,6 +58,9 @@ namespace kd {
 constexpr uint64_t WARP_MAX_WIDTH = 128;
 inline bool warp_static_width(uint64_t d) { return d == 1 || d == 2 || d == 3 || d == 4 || d == 8 || d == 16; }
 inline bool warp_runtime_width(uint64_t d) { return d >= 1 && d <= WARP_MAX_WIDTH && !warp_static_width(d); }
+// Widths whose filters read the FP32 rows padded to w32 floats: the runtime
+// widths, and 3 (one 16-byte load a row instead of three 4-byte ones).
+inline bool padded_rows(uint64_t d) { return d == 3 || warp_runtime_width(d); }
 
 // Launch arguments of the query kernels (every query translation unit).
 constexpr uint32_t NO_ID = 0xffffffffu;
@@ -79,7 +82,7 @@ struct QArgs {
   uint32_t* status;       // bit 0: non-finite query
   const uint32_t* order;  // optional: thread t runs query order[t] (spatially sorted)
   const uint32_t* leaf_of;  // optional: landing leaf node of each query (by query index)
-  const float* data32w;   // FP32 rows padded to w32 floats (runtime-width warp kernels)
+  const float* data32w;   // FP32 rows padded to w32 floats (width 3 and the runtime widths)
   uint32_t w32;
   // Near ties (eps = 0 kernels outside the reference's visiting order): the
   // query gets (rerun_tag << 32 | query index) appended to rerun_list; NULL

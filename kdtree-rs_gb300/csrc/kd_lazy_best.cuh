@@ -19,10 +19,30 @@ constexpr uint32_t ROW_NONE = 0xffffffffu;
 // Lower bound only (the packet traversal's pruning test).
 template <int M, int D>
 __device__ __forceinline__ float box_lb(const float* b32, const float* qlo, const float* qhi) {
+  // A node's box is 2D floats at node * 2D: 16-byte aligned for even D
+  // (float4 loads), 8-byte aligned otherwise (float2 loads).
+  float v[2 * D];
+  if constexpr (D % 2 == 0) {
+#pragma unroll
+    for (int c = 0; c < D / 2; ++c) {
+      const float4 w = reinterpret_cast<const float4*>(b32)[c];
+      v[4 * c] = w.x;
+      v[4 * c + 1] = w.y;
+      v[4 * c + 2] = w.z;
+      v[4 * c + 3] = w.w;
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      const float2 w = reinterpret_cast<const float2*>(b32)[c];
+      v[2 * c] = w.x;
+      v[2 * c + 1] = w.y;
+    }
+  }
   float lb = 0.f;
 #pragma unroll
   for (int i = 0; i < D; ++i) {
-    float o = fmaxf(__fsub_rd(b32[i], qhi[i]), __fsub_rd(qlo[i], b32[D + i]));
+    float o = fmaxf(__fsub_rd(v[i], qhi[i]), __fsub_rd(qlo[i], v[D + i]));
     o = o > 0.f ? o : 0.f;
     lb = fold_lb<M>(lb, red_lb<M>(o));
   }
@@ -491,29 +511,33 @@ struct LazyHeap {
   // storing element j: every row of distances (and of indices) goes out as
   // whole contiguous segments.  Every lane of the warp calls it; `live` says
   // whether this lane has a query whose results to write (sorted already).
+  // The warp's (query, slot) pairs are written 32 at a time, pair f = lane +
+  // 32 t being slot f % k of lane f / k's query: every lane takes part in each
+  // pass (the FP64 square root of L2 is a long instruction sequence on the
+  // FP64 pipe) and one store covers 32 / k queries' rows.
   __device__ __forceinline__ void write_warp(bool live, double* od, int64_t* oi, uint64_t k_, uint64_t n_points) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t live_mask = __ballot_sync(0xffffffffu, live);
     __syncwarp();
     const uint32_t col0 = threadIdx.x - lane;  // this warp's first heap column
-    for (uint32_t m = live_mask; m; m &= m - 1) {
-      const uint32_t r = __ffs(m) - 1;
+    const uint32_t kk = static_cast<uint32_t>(k_);
+    const uint32_t total = 32 * kk;
+    for (uint32_t f0 = 0; f0 < total; f0 += 32) {
+      const uint32_t f = f0 + lane;
+      const uint32_t r = min(f / kk, 31u), j = f - r * kk;
       double* od_r = reinterpret_cast<double*>(__shfl_sync(0xffffffffu, reinterpret_cast<uintptr_t>(od), r));
       int64_t* oi_r = reinterpret_cast<int64_t*>(__shfl_sync(0xffffffffu, reinterpret_cast<uintptr_t>(oi), r));
       const uint32_t n_r = __shfl_sync(0xffffffffu, n, r);
-      const float* lo_r = lo - threadIdx.x + col0 + r;
-      const float* hi_r = hi - threadIdx.x + col0 + r;
-      const uint32_t* row_r = row - threadIdx.x + col0 + r;
-      for (uint32_t j = lane; j < k_; j += 32) {
-        if (j < n_r) {
-          const uint64_t key =
-              (static_cast<uint64_t>(__float_as_uint(hi_r[j * S])) << 32) | __float_as_uint(lo_r[j * S]);
-          od_r[j] = restore<M>(bitsd(key), 0.0);
-          oi_r[j] = static_cast<int64_t>(row_r[j * S]);
-        } else {
-          od_r[j] = bitsd(INF_BITS);
-          oi_r[j] = static_cast<int64_t>(n_points);
-        }
+      if (f >= total || !((live_mask >> r) & 1u)) continue;
+      if (j < n_r) {
+        const uint32_t c = (col0 + r) + j * S;
+        const uint64_t key = (static_cast<uint64_t>(__float_as_uint(hi[c - threadIdx.x])) << 32) |
+                             __float_as_uint(lo[c - threadIdx.x]);
+        od_r[j] = restore<M>(bitsd(key), 0.0);
+        oi_r[j] = static_cast<int64_t>(row[c - threadIdx.x]);
+      } else {
+        od_r[j] = bitsd(INF_BITS);
+        oi_r[j] = static_cast<int64_t>(n_points);
       }
     }
   }

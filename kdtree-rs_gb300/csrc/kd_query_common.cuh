@@ -266,6 +266,18 @@ __device__ __forceinline__ uint64_t ieee_key(uint64_t b) {
   return k == 0x7fffffffffffffffull ? 0x8000000000000000ull : k;
 }
 
+// FP32 rows the filters read: the copy padded to w32 floats for width 3 (4
+// floats: one 16-byte load a row) and the runtime widths (D = 0), the plain
+// copy for the other compile-time widths.
+template <int D>
+__device__ __forceinline__ const float* filter_rows(const QArgs& a) {
+  return (D == 0 || D == 3) ? a.data32w : a.data32;
+}
+template <int D>
+__device__ __forceinline__ uint64_t filter_stride(const QArgs& a) {
+  return D == 3 ? 4 : (D > 0 ? static_cast<uint64_t>(D) : a.w32);
+}
+
 // Append query qi (with the launch's tag) to the list of queries whose eps = 0
 // fast-path result is a near tie and must be run again in the reference's
 // order (kd_warp.cuh, kd_query_ref.cuh).

@@ -94,10 +94,16 @@ struct PointFilter {
   // FP32 reduced distance of the row at p32, summed in dimension order.  The
   // FP32 copy starts on an allocation boundary, so rows of a width divisible
   // by 4 (2) are 16 (8) byte aligned and load as vectors: a quarter (half)
-  // of the load instructions.
+  // of the load instructions.  Width 3 reads the copy padded to 4 floats
+  // (filter_rows): one 16-byte load.
   __device__ __forceinline__ float sum(const float* p32) const {
     float p[D];
-    if constexpr (D % 4 == 0) {
+    if constexpr (D == 3) {
+      const float4 v = *reinterpret_cast<const float4*>(p32);
+      p[0] = v.x;
+      p[1] = v.y;
+      p[2] = v.z;
+    } else if constexpr (D % 4 == 0) {
 #pragma unroll
       for (int c = 0; c < D / 4; ++c) {
         const float4 v = reinterpret_cast<const float4*>(p32)[c];
@@ -179,7 +185,8 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
   }
   PointFilter<M, D> filt;
   filt.init(q, a.coord_max);
-  auto row_sum = [&](uint32_t r) { return filt.sum(a.data32 + static_cast<uint64_t>(r) * D); };
+  const float* rows32 = filter_rows<D>(a);
+  auto row_sum = [&](uint32_t r) { return filt.sum(rows32 + static_cast<uint64_t>(r) * filter_stride<D>(a)); };
 
   // k-best set: a shared-memory heap from K = 8 up, register slots below
   std::conditional_t<(K >= 8), LazyHeap<M, D, K>, LazySet<M, D, K>> best;

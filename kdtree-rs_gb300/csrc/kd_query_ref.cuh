@@ -118,8 +118,8 @@ __device__ __forceinline__ void ref_query(const QArgs& a, uint64_t qi, RefFrame*
       lane_query_enclosure(qg, d, lane, &lq);
     }
   }
-  const float* rows32 = D > 0 ? a.data32 : a.data32w;
-  const uint64_t rstride = D > 0 ? static_cast<uint64_t>(D) : a.w32;
+  const float* rows32 = filter_rows<D>(a);
+  const uint64_t rstride = filter_stride<D>(a);
   const uint64_t bstride = 2ull * d;
   const uint32_t chunk_w = (M != M_LINF && M != M_LP && (d == 4 || d == 8)) ? (d == 4 ? 2u : 8u) : 0u;
   // FP32 enclosure of eps_factor (1 when eps = 0)

@@ -69,8 +69,8 @@ __device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, WarpStack
     filt.init(qg, d, a.w32, a.coord_max, sq_w, lane);
     lane_query_enclosure(qg, d, lane, &lq);
   }
-  const float* rows32 = D > 0 ? a.data32 : a.data32w;
-  const uint64_t rstride = D > 0 ? static_cast<uint64_t>(D) : a.w32;
+  const float* rows32 = filter_rows<D>(a);
+  const uint64_t rstride = filter_stride<D>(a);
   const uint64_t bstride = 2ull * d;
   // Packed d4 / d8 chunk flags (kernel.rs:517-562): L1 / L2 only
   const uint32_t chunk_w = (M != M_LINF && (d == 4 || d == 8)) ? (d == 4 ? 2u : 8u) : 0u;

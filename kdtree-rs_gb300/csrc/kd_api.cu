@@ -548,7 +548,8 @@ int kd_host_alloc(uint64_t bytes, void** out) {
   {
     std::lock_guard<std::mutex> lock(g_host_mu);
     auto it = g_host_free.lower_bound(want);
-    if (it != g_host_free.end() && it->first <= 2 * want) {  // reuse a block of about this size
+    if (it != g_host_free.end() && it->first <= 2 * want) {  // reuse a block of about this size:
+      it = std::prev(g_host_free.upper_bound(it->first));     // the one freed last (warmest)
       *out = it->second;
       g_host_free_bytes -= it->first;
       g_host_free.erase(it);

@@ -189,7 +189,7 @@ struct LazySet {
       const float wlo = slot_lo(worst), whi = slot_hi(worst);
       const bool definite = second_hi < wlo;  // no other enclosure reaches the worst's
       if (definite && clo > whi) {            // after the worst: not kept
-        note(clo);
+        note_point(clo, r, in_chunk);
         return;
       }
       if (chi < max_lo) {  // before the worst, whichever slot it is
@@ -211,7 +211,7 @@ struct LazySet {
         clo = mag_dn32(dbits(cx));
         chi = mag_up32(dbits(cx));
       }
-      note(slot_lo(worst));  // the worst drops out
+      note_slot(worst);  // the worst drops out
     } else {
       --n_empty;
     }
@@ -227,6 +227,20 @@ struct LazySet {
     rescan();
   }
   __device__ __forceinline__ void note(float x) { runner = fminf(runner, x); }
+  // A dropped point (tree row r) whose exact distance is at least lb, and the
+  // slot about to be replaced: noted as near_window (kd_query_common.cuh)
+  // describes.
+  __device__ __forceinline__ void note_point(float lb, uint32_t r, bool in_chunk) {
+    if (lb > near_window(b_hi)) return;
+    note(mag_dn32(dbits(exact_of(r, in_chunk))));
+  }
+  __device__ __forceinline__ void note_slot(int w) {
+    if (slot_lo(w) > near_window(b_hi)) return;
+    uint32_t r = row[0];
+#pragma unroll
+    for (int j = 1; j < K; ++j) r = (j == w) ? row[j] : r;
+    note(mag_dn32(dbits(exact_of(r, (chunk >> w) & 1u))));
+  }
 
   // write_results (query.rs:421-429, 483-493): the exact values sorted by
   // (distance, index); empty slots after every real one.  Returns whether
@@ -336,6 +350,12 @@ struct LazyHeap {
     runner = __int_as_float(0x7f800000);
   }
   __device__ __forceinline__ void note(float x) { runner = fminf(runner, x); }
+  // A dropped point (tree row r) whose exact distance is at least lb: noted
+  // as near_window (kd_query_common.cuh) describes.
+  __device__ __forceinline__ void note_point(float lb, uint32_t r, bool in_chunk) {
+    if (lb > near_window(b_hi)) return;
+    note(mag_dn32(dbits(exact_of(r, in_chunk))));
+  }
   static __device__ __forceinline__ float tag(float l, bool in_chunk) {
     return __uint_as_float(__float_as_uint(l) | (static_cast<uint32_t>(in_chunk) << 31));
   }
@@ -396,7 +416,7 @@ struct LazyHeap {
     }
     const float rh = hi[0];
     if (clo > rh) {
-      note(clo);
+      note_point(clo, r, in_chunk);
       return;
     }
     const float rl = fabsf(lo[0]);
@@ -404,7 +424,8 @@ struct LazyHeap {
     if (n > 1) sec = hi[S];
     if (n > 2) sec = fmaxf(sec, hi[2 * S]);
     if (chi < rl && sec < rl) {
-      note(rl);  // the root drops out
+      if (!(rl > near_window(b_hi)))  // the root drops out
+        note(mag_dn32(dbits(exact_of(row[0], chunk_of(lo[0])))));
       sift_down(0, tag(clo, in_chunk), chi, r);
       refresh();
       return;
@@ -575,6 +596,20 @@ struct LazySetDyn {
   const uint32_t* indices;
 
   __device__ __forceinline__ void note(float x) { runner = fminf(runner, x); }
+  // A dropped point (tree row r) whose exact distance is at least lb, and the
+  // slot about to be replaced: noted as near_window (kd_query_common.cuh)
+  // describes.
+  __device__ __forceinline__ void note_point(float lb, uint32_t r) {
+    if (lb > near_window(b_hi)) return;
+    note(mag_dn32(dbits(pt.exact(r))));
+  }
+  __device__ __forceinline__ void note_slot(int w) {
+    if (slot_lo(w) > near_window(b_hi)) return;
+    uint32_t r = row[0];
+#pragma unroll
+    for (int j = 1; j < K; ++j) r = (j == w) ? row[j] : r;
+    note(mag_dn32(dbits(pt.exact(r))));
+  }
   __device__ __forceinline__ void init(uint64_t k, double cutoff, DynPoint p, const uint32_t* indices_) {
     runner = __int_as_float(0x7f800000);
 #pragma unroll
@@ -664,7 +699,7 @@ struct LazySetDyn {
       const float wlo = slot_lo(worst), whi = slot_hi(worst);
       const bool definite = second_hi < wlo;
       if (definite && clo > whi) {
-        note(clo);
+        note_point(clo, r);
         return;
       }
       if (chi < max_lo) {
@@ -686,7 +721,7 @@ struct LazySetDyn {
         clo = mag_dn32(dbits(cx));
         chi = mag_up32(dbits(cx));
       }
-      note(slot_lo(worst));  // the worst drops out
+      note_slot(worst);  // the worst drops out
     } else {
       --n_empty;
     }

@@ -266,6 +266,15 @@ __device__ __forceinline__ uint64_t ieee_key(uint64_t b) {
   return k == 0x7fffffffffffffffull ? 0x8000000000000000ull : k;
 }
 
+// x (1 + 2^-20) rounded up, never below the smallest normal FP32: the near-tie
+// window above a distance's upper enclosure.  A query is a near tie when a
+// point it dropped (within max_distance) may lie inside the window above its
+// k-th distance.  The window only shrinks as the bound does, so a dropped
+// point whose lower bound exceeds the window of the present bound never
+// counts; one whose bound is inside is noted by its exact distance (a loose
+// FP32 enclosure there would flag queries whose dropped points are not ties).
+__device__ __forceinline__ float near_window(float x) { return fmaxf(__fmul_ru(x, UB_GROW), 1.17549435e-38f); }
+
 // FP32 rows the filters read: the copy padded to w32 floats for width 3 (4
 // floats: one 16-byte load a row) and the runtime widths (D = 0), the plain
 // copy for the other compile-time widths.

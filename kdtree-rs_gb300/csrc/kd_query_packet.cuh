@@ -232,7 +232,7 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
           thr = filt.threshold(best.b_hi);
           thr2 = filt.threshold(band_of(best.b_hi));
         } else {
-          best.note(clo);
+          best.note_point(clo, r, r < chunk_end);
         }
       }
     }
@@ -280,7 +280,7 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
                 thr = filt.threshold(best.b_hi);
                 thr2 = filt.threshold(band_of(best.b_hi));
               } else {
-                best.note(clo);
+                best.note_point(clo, r, r < chunk_end);
               }
             }
           }

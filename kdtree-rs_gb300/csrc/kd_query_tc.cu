@@ -446,14 +446,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
           }
           if (!active) mask = band = 0;
-          // pairs rejected inside the band: farther than the bound, at least b_lo
-          if (band & ~mask) set.note(set.b_lo);
-          while (mask) {
-            const uint32_t j = __ffs(mask) - 1;
-            mask &= mask - 1;
+          // survivors, and the pairs the filter rejected inside the near-tie
+          // band (farther than the bound): those are noted by their FP32
+          // enclosure, and by their exact value when it lies in the window
+          uint32_t todo = mask | band;
+          while (todo) {
+            const uint32_t j = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const bool survivor = (mask >> j) & 1u;
             const uint32_t p = base + c + j;
             if (p >= a.n_points) continue;
-            ++surv;
+            surv += survivor;
             // FP32 sum of squares and its enclosure (triangle inequality, as the
             // packet filter; the sqrt margin 2^-16 covers d <= 128)
             const float* p32 = a.data32 + static_cast<uint64_t>(p) * a.d;
@@ -470,8 +473,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
               clo = __fmul_rd(__fmul_rd(lo, lo), LB_SHRINK);
               chi = __fmul_ru(__fmul_ru(hi, hi), UB_GROW);
             }
-            if (clo > set.b_hi) {
-              set.note(clo);
+            if (!survivor || clo > set.b_hi) {
+              set.note_point(clo, p);
               continue;
             }
             set.offer(clo, chi, p);

@@ -128,7 +128,9 @@ __device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, WarpStack
         float clo, chi;
         filt.enclose(s, &clo, &chi);
         const bool cand = r < end && !(s > thr) && !(clo > best.bound32);
-        if (r < end && !cand && !(s > thr2)) best.note(clo);  // dropped inside the near-tie band
+        // dropped inside the near-tie band: noted by its exact value (rare)
+        if (r < end && !cand && !(s > thr2) && !(clo > near_window(best.bound32)))
+          best.note(mag_dn32(dbits(best.exact_of(r, r < chunk_end))));
         uint32_t mask = __ballot_sync(FULL_MASK, cand);
         if (!mask) continue;
         const uint32_t my_id = cand ? a.indices[r] : NO_ID;

@@ -47,10 +47,6 @@ struct Log2Ceil<1> {
   static constexpr int value = 0;
 };
 
-// x (1 + 2^-20) rounded up, never below the smallest normal FP32: the near-tie
-// window above a distance's upper enclosure.
-__device__ __forceinline__ float near_window(float x) { return fmaxf(__fmul_ru(x, UB_GROW), 1.17549435e-38f); }
-
 // ---------------------------------------------------------------------------
 // FP32 row filter for runtime widths (the packet traversal's PointFilter with
 // the width and the margins taken at run time).  The FP32 sum of d terms
@@ -362,11 +358,18 @@ struct WarpList {
     refresh();
     return kb < cut_bits ? kb : cut_bits;
   }
+  // A dropped point (tree row r; warp-uniform arguments) whose exact distance
+  // is at least lb: noted, by lane 0, as near_window (kd_query_common.cuh)
+  // describes.
+  __device__ __forceinline__ void note_point(float lb, uint32_t r, bool in_chunk) {
+    if (lb > near_window(bound32)) return;
+    if (lane == 0) note(mag_dn32(dbits(exact_of(r, in_chunk))));
+  }
   // Offer the candidate at tree row cr (original index cid) whose exact
   // distance lies in [cl, ch]; warp-uniform arguments.
   __device__ __forceinline__ void offer(float cl, float ch, uint32_t cr, uint32_t cid, bool cchunk) {
     if (cl > bound32) {
-      note(cl);
+      note_point(cl, cr, cchunk);
       return;
     }
     uint64_t cx_bits = 0;
@@ -405,21 +408,18 @@ struct WarpList {
 #pragma unroll
     for (int s = 0; s < KS; ++s) pos += __popc(__ballot_sync(FULL_MASK, before[s]));
     if (pos >= k) {
-      note(cl);
+      note_point(cl, cr, cchunk);
       refresh();  // enclosures may have tightened
       return;
     }
-    // the k-th entry, if real, drops out
+    // the k-th entry, if real, drops out (its owner lane notes it)
     {
       const uint32_t r = k - 1;
-      float el = __int_as_float(0x7f800000);
+      const float win = near_window(bound32);
 #pragma unroll
-      for (int s = 0; s < KS; ++s) {
-        const float l = __shfl_sync(FULL_MASK, row[s] != ROW_NONE ? lo[s] : __int_as_float(0x7f800000),
-                                    static_cast<int>(r & 31));
-        if (r / 32 == static_cast<uint32_t>(s)) el = l;
-      }
-      note(el);
+      for (int s = 0; s < KS; ++s)
+        if (lane == (r & 31) && r / 32 == static_cast<uint32_t>(s) && row[s] != ROW_NONE && !(lo[s] > win))
+          note(mag_dn32(dbits(exact_of(row[s], chunk[s]))));
     }
     float up_lo[KS], up_hi[KS];
     uint32_t up_row[KS], up_id[KS];

@@ -372,11 +372,14 @@ def precision_cases(lib, torch, stream, dev, cpu_threads):
         tree = KDTree(data, leafsize=16)
         build_s = time.perf_counter() - t0
         dq = torch.from_numpy(q).to(dev)
-        surv = torch.zeros(1, dtype=torch.int64, device=dev)
+        surv = torch.zeros(2, dtype=torch.int64, device=dev)  # TC survivors, near-tie reruns
         ms_tc, (od, oi) = time_path(lib, tree, dq, 32, 2.0, PATH_TENSOR_CORE, 3, torch, stream, surv)
         pairs = 3 * q.shape[0] * data.shape[0]
-        rerank = int(surv.item()) / pairs
-        ms_pl, (pd_, pi_) = time_path(lib, tree, dq, 32, 2.0, PATH_WARP, 1, torch, stream)
+        rerank = int(surv[0].item()) / pairs
+        tc_ties = int(surv[1].item()) / (3 * q.shape[0])
+        cnt = torch.zeros(2, dtype=torch.int64, device=dev)
+        ms_pl, (pd_, pi_) = time_path(lib, tree, dq, 32, 2.0, PATH_WARP, 1, torch, stream, cnt)
+        warp_ties = int(cnt[1].item()) / q.shape[0]
         same = bool(torch.equal(oi, pi_) and torch.equal(od, pd_))
         n_ref = 152 * 4 * 8  # eight warps an SM's worth of queries for the reference-order kernel
         sample = dq[:n_ref].contiguous()
@@ -396,7 +399,8 @@ def precision_cases(lib, torch, stream, dev, cpu_threads):
                 "plain_path": "warp best-first (CUDA cores, FP64-exact)", "plain_ms_100k": ms_pl,
                 "tc_over_plain": tc_qps / plain_qps, "identical": same and same_ref,
                 "reference_order_qps": n_ref / ms_ref * 1e3, "reference_order_sample": n_ref,
-                "rerank_fraction": rerank, "filter_rel_err_max": float(rel.max()),
+                "rerank_fraction": rerank, "near_tie_rerun_fraction": {"tc": tc_ties, "warp": warp_ties},
+                "filter_rel_err_max": float(rel.max()),
                 "filter_rel_err_median": float(np.median(rel))}
         if cpu_threads:
             sys.path.insert(0, str(ROOT / "oracle"))
@@ -717,6 +721,7 @@ def run_profile_case(name):
     stream = torch.cuda.Stream()
     rng = np.random.default_rng(77)
     out = {"case": name}
+    cnt = torch.zeros(2, dtype=torch.int64, device="cuda")  # TC survivors, near-tie reruns of the timed call
     t0 = time.perf_counter()
     if name == "build":
         data = np.random.default_rng(2).uniform(size=(N_POINTS, 3))
@@ -727,9 +732,9 @@ def run_profile_case(name):
         nq = {"packet": 200_000, "ref": 100_000, "onethread": 20_000}[name]
         dq = torch.from_numpy(np.random.default_rng(3).uniform(size=(nq, 3))).cuda()
         if name == "packet":
-            out["ms"] = time_path(lib, tree, dq, 16, 2.0, PATH_PACKET, 1, torch, stream)[0]
+            out["ms"] = time_path(lib, tree, dq, 16, 2.0, PATH_PACKET, 1, torch, stream, cnt)[0]
         elif name == "onethread":
-            out["ms"] = time_path(lib, tree, dq, 100, 2.0, PATH_AUTO, 1, torch, stream)[0]
+            out["ms"] = time_path(lib, tree, dq, 100, 2.0, PATH_AUTO, 1, torch, stream, cnt)[0]
         else:
             od = torch.empty((nq, 16), dtype=torch.float64, device="cuda")
             oi = torch.empty((nq, 16), dtype=torch.int64, device="cuda")
@@ -743,18 +748,18 @@ def run_profile_case(name):
         data = c[rng.integers(0, 64, N_POINTS)] + 0.01 * rng.standard_normal((N_POINTS, 16))
         q = c[rng.integers(0, 64, 20_000)] + 0.01 * rng.standard_normal((20_000, 16))
         tree = KDTree(data)
-        out["ms"] = time_path(lib, tree, torch.from_numpy(q).cuda(), 16, 2.0, PATH_WARP, 1, torch, stream)[0]
+        out["ms"] = time_path(lib, tree, torch.from_numpy(q).cuda(), 16, 2.0, PATH_WARP, 1, torch, stream, cnt)[0]
     elif name == "warpdyn":
         data = rng.standard_normal((200_000, 20))
         q = rng.standard_normal((20_000, 20))
         tree = KDTree(data, leafsize=16)
-        out["ms"] = time_path(lib, tree, torch.from_numpy(q).cuda(), 8, 2.0, PATH_WARP, 1, torch, stream)[0]
+        out["ms"] = time_path(lib, tree, torch.from_numpy(q).cuda(), 8, 2.0, PATH_WARP, 1, torch, stream, cnt)[0]
     elif name == "tc":
         scale = np.exp(rng.uniform(np.log(0.1), np.log(10), 64))
         data = rng.standard_normal((100_000, 64)) * scale
         q = rng.standard_normal((152 * 128, 64)) * scale
         tree = KDTree(data, leafsize=16)
-        out["ms"] = time_path(lib, tree, torch.from_numpy(q).cuda(), 32, 2.0, PATH_TENSOR_CORE, 1, torch, stream)[0]
+        out["ms"] = time_path(lib, tree, torch.from_numpy(q).cuda(), 32, 2.0, PATH_TENSOR_CORE, 1, torch, stream, cnt)[0]
     elif name == "batch":
         jobs = []
         for _ in range(64):
@@ -770,6 +775,7 @@ def run_profile_case(name):
         raise SystemExit(f"unknown profile case {name!r}; cases: {', '.join(PROFILE_CASES)}")
     torch.cuda.synchronize()
     out["wall_s"] = time.perf_counter() - t0
+    out["near_tie_reruns"] = int(cnt[1].item())
     print(json.dumps(out), flush=True)
     return 0
 
@@ -930,6 +936,11 @@ def main():
     step_ms = [e0.elapsed_time(e1) for e0, e1 in events]
     value, total_s = whole_job_rate(sum(step_ms) / 1e3, args.steps, ws, dev)
     clocks = sampler.summary()
+    # the queries the traversal flagged as near ties and ran again in the
+    # reference's order: one more (untimed) call of the same step
+    cnt = torch.zeros(2, dtype=torch.int64, device=dev)
+    time_path(lib, tree, dq, K, 2.0, PATH_AUTO, 1, torch, stream, cnt, warm=False)
+    near_ties = int(cnt[1].item())
 
     # end to end through the C ABI with pinned host buffers
     hq = torch.from_numpy(q).pin_memory()
@@ -997,6 +1008,7 @@ def main():
                     "algorithmic_bytes_per_launch": per_launch,
                     "per_query": {"nodes_visited": counts[0] / N_QUERIES, "rows_scanned": counts[1] / N_QUERIES,
                                   "boxes_evaluated": counts[2] / N_QUERIES},
+                    "near_tie_reruns": near_ties,
                     "compulsory_bytes_per_launch": compulsory_bytes(),
                     "traffic_over_compulsory": (traffic / compulsory_bytes()) if traffic else None,
                     "kernel": "k_query_packet<L2, d=3, K=16>", "kernel_ms": mean_s * 1e3,

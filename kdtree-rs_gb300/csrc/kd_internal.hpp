@@ -90,6 +90,7 @@ struct QArgs {
   uint32_t* rerun_count;
   uint64_t* rerun_list;
   uint32_t rerun_tag;
+  unsigned long long* rerun_total;  // optional: the rerun count is added to it (measurement)
   bool reference_order;   // run the reference-order descent even where eps = 0
   uint64_t nq;
   uint64_t d;

@@ -211,11 +211,16 @@ struct LazySet {
         clo = mag_dn32(dbits(cx));
         chi = mag_up32(dbits(cx));
       }
-      note_slot(worst);  // the worst drops out
     } else {
       --n_empty;
     }
     const int w = worst;
+    // the worst drops out (when the set was full): its row and lower
+    // enclosure, noted against the bound after the replacement
+    const bool evict = row_of(w) != ROW_NONE;
+    const float ev_lo = slot_lo(w);
+    const uint32_t ev_row = row_of(w);
+    const bool ev_chunk = (chunk >> w) & 1u;
 #pragma unroll
     for (int j = 0; j < K; ++j) {
       const bool m = j == w;
@@ -225,21 +230,20 @@ struct LazySet {
     }
     if (D == 4 || D == 8) chunk = (chunk & ~(1u << w)) | (static_cast<uint32_t>(in_chunk) << w);
     rescan();
+    if (evict) note_point(ev_lo, ev_row, ev_chunk);
   }
   __device__ __forceinline__ void note(float x) { runner = fminf(runner, x); }
-  // A dropped point (tree row r) whose exact distance is at least lb, and the
-  // slot about to be replaced: noted as near_window (kd_query_common.cuh)
-  // describes.
+  // A dropped point (tree row r) whose exact distance is at least lb: noted as
+  // near_window (kd_query_common.cuh) describes.
   __device__ __forceinline__ void note_point(float lb, uint32_t r, bool in_chunk) {
     if (lb > near_window(b_hi)) return;
     note(mag_dn32(dbits(exact_of(r, in_chunk))));
   }
-  __device__ __forceinline__ void note_slot(int w) {
-    if (slot_lo(w) > near_window(b_hi)) return;
+  __device__ __forceinline__ uint32_t row_of(int w) const {
     uint32_t r = row[0];
 #pragma unroll
     for (int j = 1; j < K; ++j) r = (j == w) ? row[j] : r;
-    note(mag_dn32(dbits(exact_of(r, (chunk >> w) & 1u))));
+    return r;
   }
 
   // write_results (query.rs:421-429, 483-493): the exact values sorted by
@@ -423,11 +427,12 @@ struct LazyHeap {
     float sec = __int_as_float(0xff800000);
     if (n > 1) sec = hi[S];
     if (n > 2) sec = fmaxf(sec, hi[2 * S]);
-    if (chi < rl && sec < rl) {
-      if (!(rl > near_window(b_hi)))  // the root drops out
-        note(mag_dn32(dbits(exact_of(row[0], chunk_of(lo[0])))));
+    if (chi < rl && sec < rl) {  // the root drops out
+      const uint32_t ev_row = row[0];
+      const bool ev_chunk = chunk_of(lo[0]);
       sift_down(0, tag(clo, in_chunk), chi, r);
       refresh();
+      note_point(rl, ev_row, ev_chunk);  // against the bound after the eviction
       return;
     }
     offer_exact(r, in_chunk, have_x, cx);
@@ -596,19 +601,17 @@ struct LazySetDyn {
   const uint32_t* indices;
 
   __device__ __forceinline__ void note(float x) { runner = fminf(runner, x); }
-  // A dropped point (tree row r) whose exact distance is at least lb, and the
-  // slot about to be replaced: noted as near_window (kd_query_common.cuh)
-  // describes.
+  // A dropped point (tree row r) whose exact distance is at least lb: noted as
+  // near_window (kd_query_common.cuh) describes.
   __device__ __forceinline__ void note_point(float lb, uint32_t r) {
     if (lb > near_window(b_hi)) return;
     note(mag_dn32(dbits(pt.exact(r))));
   }
-  __device__ __forceinline__ void note_slot(int w) {
-    if (slot_lo(w) > near_window(b_hi)) return;
+  __device__ __forceinline__ uint32_t row_of(int w) const {
     uint32_t r = row[0];
 #pragma unroll
     for (int j = 1; j < K; ++j) r = (j == w) ? row[j] : r;
-    note(mag_dn32(dbits(pt.exact(r))));
+    return r;
   }
   __device__ __forceinline__ void init(uint64_t k, double cutoff, DynPoint p, const uint32_t* indices_) {
     runner = __int_as_float(0x7f800000);
@@ -721,11 +724,15 @@ struct LazySetDyn {
         clo = mag_dn32(dbits(cx));
         chi = mag_up32(dbits(cx));
       }
-      note_slot(worst);  // the worst drops out
     } else {
       --n_empty;
     }
     const int w = worst;
+    // the worst drops out (when the set was full): noted against the bound
+    // after the replacement
+    const bool evict = row_of(w) != ROW_NONE;
+    const float ev_lo = slot_lo(w);
+    const uint32_t ev_row = row_of(w);
 #pragma unroll
     for (int j = 0; j < K; ++j) {
       const bool m = j == w;
@@ -734,6 +741,7 @@ struct LazySetDyn {
       row[j] = m ? r : row[j];
     }
     rescan();
+    if (evict) note_point(ev_lo, ev_row);
   }
   // exact values of the k best, sorted by (distance, index), written out;
   // returns whether the query is a near tie (kd_warp.cuh).

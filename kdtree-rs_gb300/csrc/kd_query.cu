@@ -734,6 +734,7 @@ int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, cons
   }
   a.rerun_count = static_cast<uint32_t*>(rerun);
   a.rerun_list = reinterpret_cast<uint64_t*>(static_cast<unsigned char*>(rerun) + 16);
+  a.rerun_total = d_survivors ? d_survivors + 1 : nullptr;
   void* sort_mem = nullptr;
   if (nq >= ORDER_MIN_QUERIES && nq < 0xffffffffull) {
     const uint64_t words = 2 * nq + order_scratch_words(t);

@@ -77,9 +77,15 @@ int launch_ref_query(const QArgs& a, int metric, cudaStream_t st) {
   return launch_any(b, metric, st, nullptr, nullptr, blocks);
 }
 
+__global__ void k_add_count(unsigned long long* total, const uint32_t* count) { *total += *count; }
+
 int launch_rerun(const QArgs& a, int metric, cudaStream_t st, const uint32_t* count, const uint64_t* list) {
   if (!ref_warp_applicable(a.d, a.k, a.n_points))
     return fail(KD_ERR_INVALID_ARGUMENT, "the reference-order warp kernel does not cover this query");
+  if (a.rerun_total) {
+    k_add_count<<<1, 1, 0, st>>>(a.rerun_total, count);
+    KD_TRY_CUDA(cudaGetLastError());
+  }
   QArgs b = a;
   b.rerun_count = nullptr;
   b.order = nullptr;

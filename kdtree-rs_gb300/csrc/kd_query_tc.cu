@@ -784,7 +784,8 @@ int query_tc_on_device(kd_tree* t, const double* d_queries, uint64_t nq, const Q
     return cuda_fail(e, "k_query_tc launch");
   }
   // the near ties, again in the reference's order
-  const QArgs ra = query_args(t, d_queries, nq, qp, d_out_d, d_out_i, d_status);
+  QArgs ra = query_args(t, d_queries, nq, qp, d_out_d, d_out_i, d_status);
+  ra.rerun_total = d_survivors ? d_survivors + 1 : nullptr;
   rc = launch_rerun(ra, M_L2, st, rerun_count, rerun_list);
   cudaFreeAsync(mem, st);
   return rc;

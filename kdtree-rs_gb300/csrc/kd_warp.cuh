@@ -412,14 +412,20 @@ struct WarpList {
       refresh();  // enclosures may have tightened
       return;
     }
-    // the k-th entry, if real, drops out (its owner lane notes it)
+    // the k-th entry, if real, drops out: its owner lane keeps its row and
+    // lower enclosure, noted against the bound after the insert
+    float ev_lo = __int_as_float(0x7f800000);
+    uint32_t ev_row = ROW_NONE;
+    bool ev_chunk = false;
     {
       const uint32_t r = k - 1;
-      const float win = near_window(bound32);
 #pragma unroll
       for (int s = 0; s < KS; ++s)
-        if (lane == (r & 31) && r / 32 == static_cast<uint32_t>(s) && row[s] != ROW_NONE && !(lo[s] > win))
-          note(mag_dn32(dbits(exact_of(row[s], chunk[s]))));
+        if (lane == (r & 31) && r / 32 == static_cast<uint32_t>(s) && row[s] != ROW_NONE) {
+          ev_lo = lo[s];
+          ev_row = row[s];
+          ev_chunk = chunk[s];
+        }
     }
     float up_lo[KS], up_hi[KS];
     uint32_t up_row[KS], up_id[KS];
@@ -463,6 +469,7 @@ struct WarpList {
       }
     }
     refresh();
+    if (ev_row != ROW_NONE && !(ev_lo > near_window(bound32))) note(mag_dn32(dbits(exact_of(ev_row, ev_chunk))));
   }
   // write_results (query.rs:421-429, 483-493): lane j writes rank j (and
   // 32 + j, ...); the entries are in exact order already, their exact values

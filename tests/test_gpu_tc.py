@@ -33,12 +33,12 @@ def _path_query(tree, q, k, path, max_distance=None):
     dq = torch.from_numpy(np.ascontiguousarray(q)).cuda()
     od = torch.empty((q.shape[0], k), dtype=torch.float64, device="cuda")
     oi = torch.empty((q.shape[0], k), dtype=torch.int64, device="cuda")
-    surv = torch.zeros(1, dtype=torch.int64, device="cuda")
+    surv = torch.zeros(2, dtype=torch.int64, device="cuda")  # filter survivors, near-tie reruns
     st = L.kd_query_device_path(tree._h, P(dq.data_ptr()), dq.numel(), k, 2.0, int(max_distance is not None),
                                 float(max_distance or 0.0), 0.0, P(od.data_ptr()), P(oi.data_ptr()), None, path,
                                 P(surv.data_ptr()))
     assert st == 0, _core._last_error()
-    return od.cpu().numpy(), oi.cpu().numpy(), int(surv.item())
+    return od.cpu().numpy(), oi.cpu().numpy(), int(surv[0].item())
 
 
 @pytest.mark.parametrize("d", [16, 17, 31, 64, 100, 128])

@@ -372,14 +372,14 @@ def precision_cases(lib, torch, stream, dev, cpu_threads):
         tree = KDTree(data, leafsize=16)
         build_s = time.perf_counter() - t0
         dq = torch.from_numpy(q).to(dev)
-        surv = torch.zeros(2, dtype=torch.int64, device=dev)  # TC survivors, near-tie reruns
+        surv = torch.zeros(3, dtype=torch.int64, device=dev)  # TC survivors, near ties, full reruns
         ms_tc, (od, oi) = time_path(lib, tree, dq, 32, 2.0, PATH_TENSOR_CORE, 3, torch, stream, surv)
         pairs = 3 * q.shape[0] * data.shape[0]
         rerank = int(surv[0].item()) / pairs
-        tc_ties = int(surv[1].item()) / (3 * q.shape[0])
-        cnt = torch.zeros(2, dtype=torch.int64, device=dev)
+        tc_ties = [int(surv[1].item()) / (3 * q.shape[0]), int(surv[2].item()) / (3 * q.shape[0])]
+        cnt = torch.zeros(3, dtype=torch.int64, device=dev)
         ms_pl, (pd_, pi_) = time_path(lib, tree, dq, 32, 2.0, PATH_WARP, 1, torch, stream, cnt)
-        warp_ties = int(cnt[1].item()) / q.shape[0]
+        warp_ties = [int(cnt[1].item()) / q.shape[0], int(cnt[2].item()) / q.shape[0]]
         same = bool(torch.equal(oi, pi_) and torch.equal(od, pd_))
         n_ref = 152 * 4 * 8  # eight warps an SM's worth of queries for the reference-order kernel
         sample = dq[:n_ref].contiguous()
@@ -399,7 +399,8 @@ def precision_cases(lib, torch, stream, dev, cpu_threads):
                 "plain_path": "warp best-first (CUDA cores, FP64-exact)", "plain_ms_100k": ms_pl,
                 "tc_over_plain": tc_qps / plain_qps, "identical": same and same_ref,
                 "reference_order_qps": n_ref / ms_ref * 1e3, "reference_order_sample": n_ref,
-                "rerank_fraction": rerank, "near_tie_rerun_fraction": {"tc": tc_ties, "warp": warp_ties},
+                "rerank_fraction": rerank, "near_tie_fraction": {"tc": tc_ties, "warp": warp_ties,
+                                                            "note": "[flagged, run again in the reference's order]"},
                 "filter_rel_err_max": float(rel.max()),
                 "filter_rel_err_median": float(np.median(rel))}
         if cpu_threads:
@@ -721,7 +722,7 @@ def run_profile_case(name):
     stream = torch.cuda.Stream()
     rng = np.random.default_rng(77)
     out = {"case": name}
-    cnt = torch.zeros(2, dtype=torch.int64, device="cuda")  # TC survivors, near-tie reruns of the timed call
+    cnt = torch.zeros(3, dtype=torch.int64, device="cuda")  # TC survivors, near ties, full reruns (timed call)
     t0 = time.perf_counter()
     if name == "build":
         data = np.random.default_rng(2).uniform(size=(N_POINTS, 3))
@@ -775,7 +776,7 @@ def run_profile_case(name):
         raise SystemExit(f"unknown profile case {name!r}; cases: {', '.join(PROFILE_CASES)}")
     torch.cuda.synchronize()
     out["wall_s"] = time.perf_counter() - t0
-    out["near_tie_reruns"] = int(cnt[1].item())
+    out["near_ties"] = [int(cnt[1].item()), int(cnt[2].item())]
     print(json.dumps(out), flush=True)
     return 0
 
@@ -938,9 +939,9 @@ def main():
     clocks = sampler.summary()
     # the queries the traversal flagged as near ties and ran again in the
     # reference's order: one more (untimed) call of the same step
-    cnt = torch.zeros(2, dtype=torch.int64, device=dev)
+    cnt = torch.zeros(3, dtype=torch.int64, device=dev)
     time_path(lib, tree, dq, K, 2.0, PATH_AUTO, 1, torch, stream, cnt, warm=False)
-    near_ties = int(cnt[1].item())
+    near_ties = {"flagged": int(cnt[1].item()), "rerun_in_reference_order": int(cnt[2].item())}
 
     # end to end through the C ABI with pinned host buffers
     hq = torch.from_numpy(q).pin_memory()
@@ -1008,7 +1009,7 @@ def main():
                     "algorithmic_bytes_per_launch": per_launch,
                     "per_query": {"nodes_visited": counts[0] / N_QUERIES, "rows_scanned": counts[1] / N_QUERIES,
                                   "boxes_evaluated": counts[2] / N_QUERIES},
-                    "near_tie_reruns": near_ties,
+                    "near_ties": near_ties,
                     "compulsory_bytes_per_launch": compulsory_bytes(),
                     "traffic_over_compulsory": (traffic / compulsory_bytes()) if traffic else None,
                     "kernel": "k_query_packet<L2, d=3, K=16>", "kernel_ms": mean_s * 1e3,

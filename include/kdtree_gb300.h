@@ -141,10 +141,11 @@ enum kd_query_path {
 };
 
 /* kd_query_device with the kernel chosen by `path` (see kd_query_path).
- * `d_counters`, when not NULL, points to two device counters the call adds
+ * `d_counters`, when not NULL, points to three device counters the call adds
  * to: [0] the (query, point) pairs the tensor-core filter could not reject,
- * [1] the queries an eps = 0 path flagged as near ties and ran again in the
- * reference's order. */
+ * [1] the queries an eps = 0 path flagged as near ties, [2] those of them
+ * whose results a test of the reference's gates along the paths to the
+ * result points could not confirm, run again in the reference's order. */
 int kd_query_device_path(const kd_tree* tree, const double* d_queries, uint64_t n_values, uint64_t k,
                          double p, int has_max_distance, double max_distance, double eps,
                          double* d_out_distances, int64_t* d_out_indices, void* stream, int path,

@@ -197,6 +197,14 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_batch_rerun(const BatchJob* j
     const uint64_t e = list[w];
     const BatchJob* J = jobs + (e >> 32);
     const uint64_t qi = static_cast<uint32_t>(e);
+    bool stands;
+    switch (J->cls & 3) {  // widths 2, 3, 8, 16 (the class's low bits)
+      case 0: stands = ref_results_stand<M, 2>(J->a, qi); break;
+      case 1: stands = ref_results_stand<M, 3>(J->a, qi); break;
+      case 2: stands = ref_results_stand<M, 8>(J->a, qi); break;
+      default: stands = ref_results_stand<M, 16>(J->a, qi); break;
+    }
+    if (stands) continue;
     switch (J->cls) {
       case 0: ref_query<M, 2, 1>(J->a, qi, s_fr[wid], s_axes[wid], nullptr); break;
       case 1: ref_query<M, 3, 1>(J->a, qi, s_fr[wid], s_axes[wid], nullptr); break;
@@ -265,6 +273,7 @@ void fill_args(QArgs* a, const JobSpec& J, const QueryParams& qp) {
   a->data32w = t->data32w;
   a->w32 = t->w32;
   a->indices = t->indices;
+  a->rows_of = t->rows_of;
   a->nodes = t->nodes;
   a->boxes = t->boxes;
   a->boxes32 = t->boxes32;

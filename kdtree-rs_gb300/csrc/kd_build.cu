@@ -827,6 +827,11 @@ __global__ void k_root_segment(uint32_t* node, uint32_t* start, uint32_t* len, u
   *len = n;
 }
 
+__global__ void k_invert_rows(const uint32_t* idx, uint32_t* rows_of, uint64_t n) {
+  const uint64_t r = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  if (r < n) rows_of[idx[r]] = static_cast<uint32_t>(r);
+}
+
 __global__ void k_iota(uint32_t* idx, uint64_t n) {
   uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
   if (i < n) idx[i] = static_cast<uint32_t>(i);
@@ -944,6 +949,7 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
   struct TreeArrays {
     double* data;
     uint32_t* idx;
+    uint32_t* rows_of;
     DNode* nodes;
     uint64_t* boxes;
     float *data32, *boxes32, *data32w;
@@ -951,6 +957,7 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
   auto carve_tree = [&](Carve& c) {
     T.data = c.take<double>(n * d);
     T.idx = c.take<uint32_t>(n);
+    T.rows_of = c.take<uint32_t>(n);
     T.nodes = c.take<DNode>(n_nodes);
     T.boxes = c.take<uint64_t>(n_nodes * 2 * d);
     T.data32 = c.take<float>(n * d);
@@ -1087,6 +1094,7 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
   KD_TRY_CUDA(cudaGetLastError());
 
   // The final row order sits in the tree's row array (din).
+  k_invert_rows<<<grid1(n, 256), 256, 0, st>>>(T.idx, T.rows_of, n);
   k_make_f32<<<grid1(std::max(n * d, n_nodes * 2 * d), 256), 256, 0, st>>>(
       T.data, T.data32, n * d, reinterpret_cast<const double*>(T.boxes), T.boxes32, n_nodes, d);
   KD_TRY_CUDA(cudaGetLastError());
@@ -1118,6 +1126,7 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
   tree_block.p = nullptr;
   t->data = T.data;
   t->indices = T.idx;
+  t->rows_of = T.rows_of;
   t->nodes = T.nodes;
   t->boxes = reinterpret_cast<double*>(T.boxes);
   t->data32 = T.data32;

@@ -23,6 +23,7 @@ struct kd_tree {
   void* block = nullptr;
   double* data = nullptr;       // n_points * ndim, tree (leaf-contiguous) order
   uint32_t* indices = nullptr;  // tree position -> original row
+  uint32_t* rows_of = nullptr;  // original row -> tree position
   kd::DNode* nodes = nullptr;   // n_nodes, preorder
   double* boxes = nullptr;      // n_nodes * 2 * ndim, [lo | hi] per node
   float* data32 = nullptr;      // n_points * ndim, round-to-nearest FP32 copy (filters)
@@ -90,7 +91,10 @@ struct QArgs {
   uint32_t* rerun_count;
   uint64_t* rerun_list;
   uint32_t rerun_tag;
-  unsigned long long* rerun_total;  // optional: the rerun count is added to it (measurement)
+  // optional (measurement): rerun_total[0] gets the flagged queries,
+  // rerun_total[1] those the path test could not confirm (run again)
+  unsigned long long* rerun_total;
+  const uint32_t* rows_of;  // original index -> tree row (inverse of indices)
   bool reference_order;   // run the reference-order descent even where eps = 0
   uint64_t nq;
   uint64_t d;

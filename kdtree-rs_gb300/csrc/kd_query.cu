@@ -667,6 +667,7 @@ QArgs query_args(const kd_tree* t, const double* d_queries, uint64_t nq, const Q
   a.data32w = t->data32w;
   a.w32 = t->w32;
   a.indices = t->indices;
+  a.rows_of = t->rows_of;
   a.nodes = t->nodes;
   a.boxes = t->boxes;
   a.boxes32 = t->boxes32;

@@ -297,9 +297,161 @@ __device__ __forceinline__ void ref_query(const QArgs& a, uint64_t qi, RefFrame*
   best.write(a.out_d + qi * a.k, a.out_i + qi * a.k, a.n_points, false);
 }
 
+// Whether the eps = 0 result already written for query qi is the reference's
+// own, decided without its descent.  The reference's bound min(k-th best,
+// cutoff) never falls below T = min(k-th exact distance, cutoff) of the exact
+// top-k (the k-th best among the points it has seen is at least the k-th
+// among all points), and it enters a subtree when every gate on the way admits
+// (x <= bound): the root's seed (query.rs:223-232); at an inner node, the far
+// child's plane bound replace_axis(cell, axes[dim], reduce(|diff|)) and then
+// its box distance (query.rs:270-289); at an order_by_box node, the child's box
+// distance (query.rs:298-327); the near child of an inner node has none.  Those
+// gate values depend on the path alone.  So when every gate on the path to
+// each of the k result points admits at T, the reference reaches all of them,
+// and the k smallest of what it sees are they: the same rows in the same
+// order.  Only a gate that rounds within an ulp or so of T fails the test.
+// Lane j walks the path of result slot j (and j + 32); the CellBound axes its
+// path replaces are kept as a per-lane log.
+template <int M, int D>
+__device__ bool ref_results_stand(const QArgs& a, uint64_t qi) {
+  if constexpr (M == M_LP) {
+    return false;
+  } else {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t d = D > 0 ? static_cast<uint32_t>(D) : static_cast<uint32_t>(a.d);
+    const double* qg = a.queries + qi * d;
+    QVec<D> q;
+    q.g = qg;
+    if constexpr (D > 0) {
+#pragma unroll
+      for (int i = 0; i < D; ++i) q.v[i] = qg[i];
+    }
+    const uint32_t k = static_cast<uint32_t>(a.k);
+    const int64_t* oi = a.out_i + qi * a.k;
+    uint32_t row[2] = {0, 0};
+    bool real[2];
+    uint32_t n_real = 0;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const uint32_t j = lane + 32u * s;
+      const int64_t id = j < k ? oi[j] : -1;
+      real[s] = id >= 0 && static_cast<uint64_t>(id) < a.n_points;
+      if (real[s]) row[s] = a.rows_of[id];
+      n_real += __popc(__ballot_sync(FULL_MASK, real[s]));
+    }
+    // T: the cutoff, or the k-th point's exact distance (its Packed chunk flag
+    // needs its leaf: the left child of a node holds the first len / 2 rows)
+    uint64_t T = dbits(a.cutoff);
+    if (n_real == k && k > 0) {
+      const uint32_t j = k - 1;
+      uint64_t xb = 0;
+      if (lane == (j & 31)) {
+        const uint32_t r = row[j >> 5];
+        uint32_t node = 0, start = 0, len = static_cast<uint32_t>(a.n_points);
+        DNode nd = a.nodes[0];
+        while (!(nd.meta & KD_NODE_LEAF)) {
+          const uint32_t mid = len / 2;
+          if (r < start + mid) {
+            node = node + 1;
+            len = mid;
+          } else {
+            node = nd.right;
+            start += mid;
+            len -= mid;
+          }
+          nd = a.nodes[node];
+        }
+        const uint32_t cw = (M != M_LINF && (d == 4 || d == 8)) ? (d == 4 ? 2u : 8u) : 0u;
+        const bool in_chunk = cw && r < start + len / cw * cw;
+        const int strat = (d <= 8) ? S_PACKED : ((M == M_L1 || M == M_L2) && d <= 16 ? S_FOLDED : S_STREAMED);
+        if constexpr (D > 0) {
+          QMem<D> qm;
+          qm.g = qg;
+          xb = dbits(exact_dist<M, D>(qm, a.data + static_cast<uint64_t>(r) * D, D, S_PACKED, in_chunk, 0.0));
+        } else {
+          xb = dbits(exact_dist<M, 0>(q, a.data + static_cast<uint64_t>(r) * d, d, strat, in_chunk, 0.0));
+        }
+      }
+      xb = __shfl_sync(FULL_MASK, xb, static_cast<int>(j & 31));
+      T = xb < T ? xb : T;
+    }
+    // the root's seed (CellBound::start)
+    const double rb = exact_box_dist<M, D>(q, a.boxes, d, 0.0);
+    auto seed_axis = [&](uint32_t i) -> double {
+      return rb != 0.0 ? reduce<M>(axis_offset(qg[i], a.boxes[i], a.boxes[d + i]), 0.0) : 0.0;
+    };
+    double seed = 0.0;
+    if (rb != 0.0)
+      for (uint32_t i = 0; i < d; ++i) seed = (M == M_LINF) ? max_nn(seed, seed_axis(i)) : dadd(seed, seed_axis(i));
+    bool ok = leq_bound(seed, T);
+    uint32_t log_dim[KD_MAX_DEPTH];
+    double log_val[KD_MAX_DEPTH];
+#pragma unroll 1
+    for (int s = 0; s < 2; ++s) {
+      if (!ok || !real[s]) continue;
+      const uint32_t r = row[s];
+      uint32_t node = 0, start = 0, len = static_cast<uint32_t>(a.n_points);
+      double cell = seed;
+      int n_log = 0;
+      for (;;) {
+        const DNode nd = a.nodes[node];
+        if (nd.meta & KD_NODE_LEAF) break;
+        const uint32_t dim = nd.meta & KD_NODE_DIM_MASK;
+        const double qd = qg[dim];
+        const bool left_near = ieee_key(dbits(qd)) <= ieee_key(dbits(nd.split));
+        const uint32_t mid = len / 2;
+        const bool go_left = r < start + mid;
+        const uint32_t child = go_left ? node + 1 : nd.right;
+        const bool far = go_left != left_near;
+        const double* cbox = a.boxes + static_cast<uint64_t>(child) * 2 * d;
+        if (nd.meta & KD_NODE_BOX_ORDER) {
+          if (!leq_bound(exact_box_dist<M, D>(q, cbox, d, 0.0), T)) {
+            ok = false;
+            break;
+          }
+        }
+        if (far) {
+          double old = seed_axis(dim);
+          for (int t = n_log - 1; t >= 0; --t)
+            if (log_dim[t] == dim) {
+              old = log_val[t];
+              break;
+            }
+          const double far_axis = reduce<M>(fabs(dsub(qd, nd.split)), 0.0);
+          const double far_dist = (M == M_LINF) ? max_nn(cell, far_axis) : dadd(dsub(cell, old), far_axis);
+          if (!(nd.meta & KD_NODE_BOX_ORDER) &&
+              !(leq_bound(far_dist, T) && leq_bound(exact_box_dist<M, D>(q, cbox, d, 0.0), T))) {
+            ok = false;
+            break;
+          }
+          if (n_log < KD_MAX_DEPTH) {
+            log_dim[n_log] = dim;
+            log_val[n_log] = far_axis;
+            ++n_log;
+          } else {
+            ok = false;  // deeper than any tree the build makes
+            break;
+          }
+          cell = far_dist;
+        }
+        if (go_left) {
+          node = node + 1;
+          len = mid;
+        } else {
+          node = nd.right;
+          start += mid;
+          len -= mid;
+        }
+      }
+    }
+    return __all_sync(FULL_MASK, ok);
+  }
+}
+
 // Warps take queries w = global warp, + total warps, ... < n: positions of
 // the batch (a.order when set), or -- with `list` -- the flagged queries of a
-// rerun (count on the device).  Dynamic shared memory: ref_warp_smem(d, w32)
+// rerun (count on the device): those whose results the path test above
+// confirms are left as they are, the rest run in the reference's order.  Dynamic shared memory: ref_warp_smem(d, w32)
 // bytes per warp.
 template <int M, int D, int KS>
 __global__ void __launch_bounds__(QUERY_THREADS) k_query_ref(QArgs a, const uint32_t* count, const uint64_t* list) {
@@ -315,6 +467,10 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query_ref(QArgs a, const uint
   const uint64_t warps = static_cast<uint64_t>(gridDim.x) * (QUERY_THREADS / 32);
   for (uint64_t w = blockIdx.x * static_cast<uint64_t>(QUERY_THREADS / 32) + wid; w < n; w += warps) {
     const uint64_t qi = list ? static_cast<uint32_t>(list[w]) : (a.order ? a.order[w] : w);
+    if (list) {
+      if (ref_results_stand<M, D>(a, qi)) continue;
+      if (a.rerun_total && (threadIdx.x & 31) == 0) atomicAdd(a.rerun_total + 1, 1ull);
+    }
     ref_query<M, D, KS>(a, qi, fr, axes, sq);
   }
 }

@@ -4,9 +4,11 @@ return the reference's answer -- which leaves that point out -- on every query
 path, through the C ABI, the drop-in KDTree.query and a batch plan.
 
 The eps = 0 fast paths (packet, warp, tensor-core) compute the exact top-k and
-flag the near ties where the reference's descent can differ from it; those
-queries are run again in the reference's order.  These cases are exactly such
-near ties, on lattice data where many distances are equal."""
+flag the near ties where the reference's descent can differ from it; a test of
+the reference's gates along the paths to the result points confirms most of
+them, and the rest are run again in the reference's order.  These cases are
+exactly such near ties, on lattice data where many distances are equal, so
+the gate test must send some queries to the rerun."""
 import ctypes
 from pathlib import Path
 
@@ -60,12 +62,29 @@ def test_every_path_returns_the_reference_answer(case):
     for name, path in PATHS.items():
         od = torch.full((q.shape[0], k), -1.0, dtype=torch.float64, device="cuda")
         oi = torch.full((q.shape[0], k), -1, dtype=torch.int64, device="cuda")
+        cnt = torch.zeros(3, dtype=torch.int64, device="cuda")  # survivors, near ties, full reruns
         st = L.kd_query_device_path(tree._h, P(dq.data_ptr()), dq.numel(), k, p, int(md is not None),
-                                    float(md or 0.0), 0.0, P(od.data_ptr()), P(oi.data_ptr()), None, path, None)
+                                    float(md or 0.0), 0.0, P(od.data_ptr()), P(oi.data_ptr()), None, path,
+                                    P(cnt.data_ptr()))
         assert st == 0, core._last_error()
         _exact((od.cpu().numpy(), oi.cpu().numpy()), ref_d, ref_i, f"path {name}")
+        flagged, rerun = int(cnt[1].item()), int(cnt[2].item())
+        assert 0 <= rerun <= flagged <= q.shape[0]
+        RERUNS[name] = RERUNS.get(name, 0) + rerun
     # the drop-in surface (host buffers)
     _exact(tree.query(q, k=k, p=p, max_distance=md), ref_d, ref_i, "KDTree.query")
+
+
+RERUNS = {}
+
+
+def test_gate_test_sends_divergent_queries_to_the_rerun():
+    """Across the cases, some queries of the fast paths must fail the gate
+    test: in these inputs the reference's own descent does leave a point of the
+    exact top-k out, which only a rerun in its order reproduces."""
+    if not RERUNS:
+        pytest.skip("runs after test_every_path_returns_the_reference_answer")
+    assert sum(RERUNS.get(n, 0) for n in ("packet", "warp", "tensor_core", "auto")) > 0, RERUNS
 
 
 def test_batch_plan_returns_the_reference_answers():

@@ -33,7 +33,7 @@ def _path_query(tree, q, k, path, max_distance=None):
     dq = torch.from_numpy(np.ascontiguousarray(q)).cuda()
     od = torch.empty((q.shape[0], k), dtype=torch.float64, device="cuda")
     oi = torch.empty((q.shape[0], k), dtype=torch.int64, device="cuda")
-    surv = torch.zeros(2, dtype=torch.int64, device="cuda")  # filter survivors, near-tie reruns
+    surv = torch.zeros(3, dtype=torch.int64, device="cuda")  # filter survivors, near ties, full reruns
     st = L.kd_query_device_path(tree._h, P(dq.data_ptr()), dq.numel(), k, 2.0, int(max_distance is not None),
                                 float(max_distance or 0.0), 0.0, P(od.data_ptr()), P(oi.data_ptr()), None, path,
                                 P(surv.data_ptr()))

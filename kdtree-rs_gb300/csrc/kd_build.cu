@@ -26,9 +26,10 @@
 // evaluated sequentially in shared memory for small segments and by pointer
 // jumping for large ones.  Only data with duplicated split coordinates takes it.
 //
-// Segments up to SMALL_MAX rows are processed entirely by one CTA in shared
-// memory; larger ones (the top levels) by grids of CTAs over row chunks with
-// global histograms, counts and scans.
+// Segments above SMALL_MAX rows (the top levels) are processed level by level
+// by grids of CTAs over row chunks with global histograms, counts and scans;
+// from the first level at or below it, one CTA builds each segment's whole
+// subtree in shared memory.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -43,7 +44,6 @@ namespace {
 constexpr uint32_t HOLE = 0xffffffffu;
 constexpr uint32_t NONE = 0xffffffffu;
 constexpr int SMALL_MAX = 8192;  // rows a single CTA partitions in shared memory
-constexpr int SMALL_THREADS = 512;
 constexpr int LG_THREADS = 256;
 constexpr int LG_ITEMS = 8;
 constexpr int LG_CHUNK = LG_THREADS * LG_ITEMS;  // rows per CTA in the large path
@@ -267,102 +267,358 @@ __device__ uint32_t block_sum(uint32_t v, uint32_t* sh_warp) {
 }
 
 // ---------------------------------------------------------------------------
-// Small path: one CTA per segment of at most SMALL_MAX rows, in shared memory.
+// Small subtrees.  From the first depth whose segments have at most SMALL_MAX
+// rows, one CTA builds the whole subtree below each segment -- every node's box
+// (build.rs:175-181), split dimension, pivot, exact partition permutation and
+// record, down to the leaves -- and then writes the subtree's rows once, in
+// their final order.  The rows stay where the level above left them: the CTA
+// permutes 16-bit local row numbers (perm: position -> local row) and keeps each
+// local row's key on its segment's current split dimension (krow).  A segment
+// longer than WARP_SEG rows is split by the whole CTA, shorter ones by one warp
+// each, the segments of a depth spread over the warps.  Segment (depth j, index
+// s) is reached from the subtree root by the bits of s, with the node counts of
+// the at most two segment lengths of each depth.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(SMALL_THREADS) k_small_level(Level L) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  uint64_t* keys = reinterpret_cast<uint64_t*>(smem);              // SMALL_MAX
-  uint16_t* cur = reinterpret_cast<uint16_t*>(keys + SMALL_MAX);    // SMALL_MAX
-  uint16_t* plist = cur + SMALL_MAX;                                // SMALL_MAX
-  __shared__ uint32_t sh_warp[SMALL_THREADS / 32];
-  __shared__ uint32_t hist[256];
-  __shared__ uint64_t s_pivot;
-  __shared__ uint32_t s_dim, s_rank;
-  __shared__ uint64_t s_prefix;
+constexpr int SUB_THREADS = 512;
+constexpr int SUB_WARPS = SUB_THREADS / 32;
+constexpr int WARP_SEG = 512;  // longest segment one warp splits (16 keys a lane)
+constexpr uint32_t FULL = 0xffffffffu;
 
-  const uint64_t slot = blockIdx.x;
-  const uint32_t node = L.seg_node[slot];
-  if (node == HOLE) {
-    if (threadIdx.x == 0) {
-      L.nseg_node[2 * slot] = HOLE;
-      L.nseg_node[2 * slot + 1] = HOLE;
-      L.nseg_len[2 * slot] = 0;
-      L.nseg_len[2 * slot + 1] = 0;
+struct SubArgs {
+  const double* din;
+  const uint32_t* iin;
+  double* dout;
+  uint32_t* iout;
+  uint64_t d;
+  uint32_t leafsize;
+  const uint32_t* seg_node;
+  const uint32_t* seg_start;
+  const uint32_t* seg_len;
+  DNode* nodes;
+  uint64_t* boxkeys;
+  uint32_t* node_len;
+  int check_finite;
+  uint32_t* status;
+};
+
+struct SubShared {
+  uint64_t krow[SMALL_MAX];   // key of each local row on its segment's split dimension
+  uint16_t perm[SMALL_MAX];   // position -> local row
+  uint16_t plist[SMALL_MAX];  // misplaced positions (relative to their segment), by rank
+};
+
+struct SubSeg {
+  uint32_t node, pos, len;  // pos: first position within the subtree
+};
+
+__device__ __forceinline__ uint64_t warp_min64(uint64_t v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const uint64_t w = __shfl_xor_sync(FULL, v, o);
+    v = w < v ? w : v;
+  }
+  return v;
+}
+__device__ __forceinline__ uint64_t warp_max64(uint64_t v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    const uint64_t w = __shfl_xor_sync(FULL, v, o);
+    v = w > v ? w : v;
+  }
+  return v;
+}
+
+// Segment (depth j, index s) of the subtree rooted at (node0, length l0), or
+// false when an ancestor of it is a leaf.
+__device__ __forceinline__ bool sub_segment(const uint32_t* lo_len, const uint32_t (*cn)[2], uint32_t node0,
+                                            uint32_t l0, uint32_t leafsize, int j, uint32_t s, SubSeg* g) {
+  uint32_t node = node0, pos = 0, len = l0;
+  for (int i = 0; i < j; ++i) {
+    if (len <= leafsize) return false;
+    const uint32_t mid = len / 2;
+    if (!((s >> (j - 1 - i)) & 1u)) {
+      node += 1;
+      len = mid;
+    } else {
+      node += 1 + cn[i + 1][mid - lo_len[i + 1]];
+      pos += mid;
+      len -= mid;
+    }
+  }
+  *g = SubSeg{node, pos, len};
+  return true;
+}
+
+// The inner node's record (expand_inner without the next level's segments).
+__device__ __forceinline__ void sub_record(const SubArgs& A, const uint32_t (*cn)[2], const uint32_t* lo_len,
+                                           int j, const SubSeg& g, uint32_t dim, uint64_t pivot_key) {
+  const uint32_t mid = g.len / 2;
+  DNode nd;
+  nd.split = from_total_key(pivot_key);
+  nd.right = g.node + 1 + cn[j + 1][mid - lo_len[j + 1]];
+  nd.meta = dim;
+  A.nodes[g.node] = nd;
+  A.node_len[g.node] = g.len;
+}
+
+// One segment split by one warp (g.len <= WARP_SEG).  Keys live in registers
+// (positions pos + 32 t + lane); the pivot is found bit by bit from the first
+// bit where the segment's smallest and largest keys differ.
+__device__ void sub_split_warp(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2], const uint32_t* lo_len,
+                               int j, const SubSeg& g, uint64_t row0, bool* bad) {
+  constexpr int T = WARP_SEG / 32;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t d = A.d;
+  uint32_t best_dim = 0;
+  double best_span = 0.0;
+  uint64_t blo = 0, bhi = 0;
+  for (uint64_t dj = 0; dj < d; ++dj) {
+    uint64_t lo = KEY_MAX, hi = 0;
+#pragma unroll
+    for (int t = 0; t < T; ++t) {
+      const uint32_t p = 32u * t + lane;
+      if (p < g.len) {
+        const double v = A.din[(row0 + S.perm[g.pos + p]) * d + dj];
+        *bad |= !isfinite(v);
+        const uint64_t k = total_key(v);
+        lo = k < lo ? k : lo;
+        hi = k > hi ? k : hi;
+      }
+    }
+    lo = warp_min64(lo);
+    hi = warp_max64(hi);
+    if (lane == 0) {
+      A.boxkeys[static_cast<uint64_t>(g.node) * 2 * d + dj] = lo;
+      A.boxkeys[static_cast<uint64_t>(g.node) * 2 * d + d + dj] = hi;
+    }
+    const double span = dsub(from_total_key(hi), from_total_key(lo));  // widest_axis (layout.rs:168-179)
+    if (dj == 0 || span > best_span) {
+      best_span = span;
+      best_dim = static_cast<uint32_t>(dj);
+      blo = lo;
+      bhi = hi;
+    }
+  }
+  if (g.len <= A.leafsize) {
+    if (lane == 0) {
+      write_leaf(A.nodes, g.node, static_cast<uint32_t>(row0) + g.pos, g.len);
+      A.node_len[g.node] = g.len;
     }
     return;
   }
-  const uint32_t start = L.seg_start[slot], len = L.seg_len[slot];
-  const uint64_t d = L.d;
-  const double* din = L.din + static_cast<uint64_t>(start) * d;
-  double* dout = L.dout + static_cast<uint64_t>(start) * d;
-  const uint32_t* iin = L.iin + start;
-  uint32_t* iout = L.iout + start;
-
-  if (len <= L.leafsize) {  // a leaf at this depth: rows stay where they are
-    for (uint64_t f = threadIdx.x; f < static_cast<uint64_t>(len) * d; f += SMALL_THREADS) dout[f] = din[f];
-    for (uint32_t i = threadIdx.x; i < len; i += SMALL_THREADS) iout[i] = iin[i];
-    if (threadIdx.x == 0) close_leaf(L, slot, node, start, len);
-    return;
+  const uint32_t dim = best_dim, mid = g.len / 2;
+  uint64_t key[T];
+#pragma unroll
+  for (int t = 0; t < T; ++t) {
+    const uint32_t p = 32u * t + lane;
+    key[t] = 0;
+    if (p < g.len) {
+      const uint32_t lr = S.perm[g.pos + p];
+      key[t] = total_key(A.din[(row0 + lr) * d + dim]);
+      S.krow[lr] = key[t];
+    }
   }
-
-  if (threadIdx.x == 0) s_dim = widest_axis_keys(L.boxkeys + static_cast<uint64_t>(node) * 2 * d, d);
-  __syncthreads();
-  const uint32_t dim = s_dim;
-  const uint32_t mid = len / 2;
-  for (uint32_t i = threadIdx.x; i < len; i += SMALL_THREADS) keys[i] = total_key(din[i * d + dim]);
-  __syncthreads();
-
   // pivot = the mid-th smallest key under total order (select_nth_unstable_by)
-  if (len <= SMALL_THREADS) {
-    if (threadIdx.x < len) {
-      const uint64_t ki = keys[threadIdx.x];
-      uint32_t cl = 0, ce = 0;
-      for (uint32_t j = 0; j < len; ++j) {
-        uint64_t kj = keys[j];
-        cl += kj < ki;
-        ce += kj == ki;
+  uint64_t pivot = blo;
+  if (blo != bhi) {
+    const int hb = 63 - __clzll(static_cast<long long>(blo ^ bhi));
+    uint64_t prefix = hb == 63 ? 0 : (blo >> (hb + 1)) << (hb + 1);
+    uint32_t rank = mid;
+    for (int b = hb; b >= 0; --b) {
+      uint32_t c0 = 0;
+#pragma unroll
+      for (int t = 0; t < T; ++t) {
+        const uint32_t p = 32u * t + lane;
+        const uint64_t k = key[t];
+        c0 += p < g.len && ((k ^ prefix) >> b) == 0;  // matches the prefix, bit b clear
       }
-      if (cl <= mid && mid < cl + ce) s_pivot = ki;  // all writers agree
+      c0 = __reduce_add_sync(FULL, c0);
+      if (rank >= c0) {
+        rank -= c0;
+        prefix |= 1ull << b;
+      }
     }
-  } else {
-    if (threadIdx.x == 0) {
-      s_prefix = 0;
-      s_rank = mid;
+    pivot = prefix;
+  }
+  const uint64_t pc = canon(pivot);
+  // lt = #{key < pivot} under f64 '<' (build.rs:209)
+  uint32_t my_lt = 0;
+#pragma unroll
+  for (int t = 0; t < T; ++t) my_lt += (32u * t + lane < g.len) && canon(key[t]) < pc;
+  const uint32_t lt = __reduce_add_sync(FULL, my_lt);
+  // misplaced positions in ascending order (ranks from ballots)
+  uint32_t n2 = 0;
+#pragma unroll
+  for (int t = 0; t < T; ++t) {
+    const uint32_t p = 32u * t + lane;
+    const bool below = canon(key[t]) < pc;
+    const bool mis = p < g.len && ((p < lt) ? !below : below);
+    const uint32_t m = __ballot_sync(FULL, mis);
+    if (mis) S.plist[g.pos + n2 + __popc(m & ((1u << lane) - 1))] = static_cast<uint16_t>(p);
+    n2 += __popc(m);
+  }
+  __syncwarp();
+  // swap R[i] <-> L[n-1-i]: the row at plist[n2-1-j] lands on plist[j]
+  uint16_t moved[T];
+#pragma unroll
+  for (int t = 0; t < T; ++t) {
+    const uint32_t jj = 32u * t + lane;
+    moved[t] = jj < n2 ? S.perm[g.pos + S.plist[g.pos + n2 - 1 - jj]] : 0;
+  }
+  __syncwarp();
+#pragma unroll
+  for (int t = 0; t < T; ++t) {
+    const uint32_t jj = 32u * t + lane;
+    if (jj < n2) S.perm[g.pos + S.plist[g.pos + jj]] = moved[t];
+  }
+  __syncwarp();
+  if (mid > lt && lane == 0) {
+    // pivot-equal fix-up (build.rs:303-313), sequentially
+    uint32_t place = lt, scan = lt;
+    while (place < mid && scan < g.len) {
+      if (canon(S.krow[S.perm[g.pos + scan]]) == pc) {
+        const uint16_t x = S.perm[g.pos + scan];
+        S.perm[g.pos + scan] = S.perm[g.pos + place];
+        S.perm[g.pos + place] = x;
+        ++place;
+      }
+      ++scan;
     }
-    for (int pass = 0; pass < RADIX_PASSES; ++pass) {
-      const int shift = 56 - 8 * pass;
-      for (int b = threadIdx.x; b < 256; b += SMALL_THREADS) hist[b] = 0;
+  }
+  __syncwarp();
+  if (lane == 0) sub_record(A, cn, lo_len, j, g, dim, pivot);
+}
+
+// Block-wide min / max of u64 values and sum of u32 ones (every thread gets
+// the result; `red` holds SUB_WARPS words of each).
+struct SubReduce {
+  uint64_t lo[SUB_WARPS], hi[SUB_WARPS];
+  uint32_t sum[SUB_WARPS];
+};
+__device__ __forceinline__ void block_minmax(uint64_t* lo, uint64_t* hi, SubReduce* red) {
+  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint64_t a = warp_min64(*lo), b = warp_max64(*hi);
+  if (lane == 0) {
+    red->lo[w] = a;
+    red->hi[w] = b;
+  }
+  __syncthreads();
+  a = red->lo[0];
+  b = red->hi[0];
+#pragma unroll
+  for (int i = 1; i < SUB_WARPS; ++i) {
+    a = red->lo[i] < a ? red->lo[i] : a;
+    b = red->hi[i] > b ? red->hi[i] : b;
+  }
+  __syncthreads();
+  *lo = a;
+  *hi = b;
+}
+__device__ __forceinline__ uint32_t block_add(uint32_t v, SubReduce* red) {
+  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v = __reduce_add_sync(FULL, v);
+  if (lane == 0) red->sum[w] = v;
+  __syncthreads();
+  uint32_t t = 0;
+#pragma unroll
+  for (int i = 0; i < SUB_WARPS; ++i) t += red->sum[i];
+  __syncthreads();
+  return t;
+}
+
+// One segment split by the whole CTA (WARP_SEG < g.len <= SMALL_MAX): 8-bit
+// radix select from the first byte where the segment's smallest and largest
+// keys differ, the digit counts aggregated per warp before the shared atomics.
+__device__ void sub_split_block(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2], const uint32_t* lo_len,
+                                int j, const SubSeg& g, uint64_t row0, bool* bad, SubReduce* red,
+                                uint32_t* hist, uint32_t* sh_warp, uint64_t* s_sel, uint32_t* s_rank) {
+  const uint32_t tid = threadIdx.x, lane = tid & 31;
+  const uint64_t d = A.d;
+  uint32_t best_dim = 0;
+  double best_span = 0.0;
+  uint64_t blo = 0, bhi = 0;
+  for (uint64_t dj = 0; dj < d; ++dj) {
+    uint64_t lo = KEY_MAX, hi = 0;
+    for (uint32_t p = tid; p < g.len; p += SUB_THREADS) {
+      const double v = A.din[(row0 + S.perm[g.pos + p]) * d + dj];
+      *bad |= !isfinite(v);
+      const uint64_t k = total_key(v);
+      lo = k < lo ? k : lo;
+      hi = k > hi ? k : hi;
+    }
+    block_minmax(&lo, &hi, red);
+    if (tid == 0) {
+      A.boxkeys[static_cast<uint64_t>(g.node) * 2 * d + dj] = lo;
+      A.boxkeys[static_cast<uint64_t>(g.node) * 2 * d + d + dj] = hi;
+    }
+    const double span = dsub(from_total_key(hi), from_total_key(lo));
+    if (dj == 0 || span > best_span) {
+      best_span = span;
+      best_dim = static_cast<uint32_t>(dj);
+      blo = lo;
+      bhi = hi;
+    }
+  }
+  if (g.len <= A.leafsize) {
+    if (tid == 0) {
+      write_leaf(A.nodes, g.node, static_cast<uint32_t>(row0) + g.pos, g.len);
+      A.node_len[g.node] = g.len;
+    }
+    return;
+  }
+  const uint32_t dim = best_dim, mid = g.len / 2;
+  for (uint32_t p = tid; p < g.len; p += SUB_THREADS) {
+    const uint32_t lr = S.perm[g.pos + p];
+    S.krow[lr] = total_key(A.din[(row0 + lr) * d + dim]);
+  }
+  __syncthreads();
+  uint64_t pivot = blo;
+  if (blo != bhi) {
+    const int hb = 63 - __clzll(static_cast<long long>(blo ^ bhi));
+    const int top = hb / 8 * 8;  // lowest bit of the first byte that differs
+    if (tid == 0) {
+      *s_sel = top == 56 ? 0 : (blo >> (top + 8)) << (top + 8);
+      *s_rank = mid;
+    }
+    for (int shift = top; shift >= 0; shift -= 8) {
+      for (int b = tid; b < 256; b += SUB_THREADS) hist[b] = 0;
       __syncthreads();
-      const uint64_t prefix = s_prefix;
-      for (uint32_t i = threadIdx.x; i < len; i += SMALL_THREADS) {
-        uint64_t k = keys[i];
-        if (pass == 0 || ((k ^ prefix) >> (shift + 8)) == 0) atomicAdd(&hist[(k >> shift) & 255], 1u);
+      const uint64_t prefix = *s_sel;
+      for (uint32_t base = 0; base < g.len; base += SUB_THREADS) {
+        const uint32_t p = base + tid;
+        bool in = false;
+        uint32_t digit = 256 + lane;  // distinct per lane when not counted
+        if (p < g.len) {
+          const uint64_t k = S.krow[S.perm[g.pos + p]];
+          in = shift == 56 || ((k ^ prefix) >> (shift + 8)) == 0;
+          if (in) digit = static_cast<uint32_t>(k >> shift) & 255u;
+        }
+        const uint32_t same = __match_any_sync(FULL, digit);
+        if (in && lane == static_cast<uint32_t>(__ffs(same) - 1)) atomicAdd(&hist[digit], __popc(same));
       }
       __syncthreads();
-      if (threadIdx.x < 32) {
-        // warp 0 scans the 256 bins, 8 per lane
-        const int lane = threadIdx.x;
-        uint32_t c[8], s = 0;
+      if (tid < 32) {
+        uint32_t c[8], sum = 0;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
           c[i] = hist[lane * 8 + i];
-          s += c[i];
+          sum += c[i];
         }
-        uint32_t x = s;
+        uint32_t x = sum;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-          uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+          const uint32_t y = __shfl_up_sync(FULL, x, o);
           if (lane >= o) x += y;
         }
-        uint32_t excl = x - s;
-        const uint32_t rank = s_rank;
+        const uint32_t excl = x - sum, rank = *s_rank;
+        __syncwarp();
         if (excl <= rank && rank < x) {
           uint32_t acc = excl;
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
             if (acc <= rank && rank < acc + c[i]) {
-              s_prefix = prefix | (static_cast<uint64_t>(lane * 8 + i) << shift);
-              s_rank = rank - acc;
+              *s_sel = prefix | (static_cast<uint64_t>(lane * 8 + i) << shift);
+              *s_rank = rank - acc;
             }
             acc += c[i];
           }
@@ -370,66 +626,116 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_small_level(Level L) {
       }
       __syncthreads();
     }
-    if (threadIdx.x == 0) s_pivot = s_prefix;
+    pivot = *s_sel;
+    __syncthreads();
   }
-  __syncthreads();
-  const uint64_t pk = s_pivot;
-  const uint64_t pc = canon(pk);
-
-  // lt = #{key < pivot} under f64 '<' (build.rs:209)
+  const uint64_t pc = canon(pivot);
   uint32_t my_lt = 0;
-  for (uint32_t i = threadIdx.x; i < len; i += SMALL_THREADS) my_lt += canon(keys[i]) < pc;
-  const uint32_t lt = block_sum<SMALL_THREADS>(my_lt, sh_warp);
-
-  // misplaced rows: key >= pivot in [0, lt), key < pivot in [lt, len); each
-  // thread owns a contiguous run of positions so ranks come out ascending.
-  const uint32_t per = (len + SMALL_THREADS - 1) / SMALL_THREADS;
-  const uint32_t b0 = min(len, threadIdx.x * per), b1 = min(len, b0 + per);
+  for (uint32_t p = tid; p < g.len; p += SUB_THREADS) my_lt += canon(S.krow[S.perm[g.pos + p]]) < pc;
+  const uint32_t lt = block_add(my_lt, red);
+  // misplaced positions: each thread owns a contiguous run, so ranks ascend
+  const uint32_t per = (g.len + SUB_THREADS - 1) / SUB_THREADS;
+  const uint32_t b0 = min(g.len, tid * per), b1 = min(g.len, b0 + per);
   uint32_t cnt = 0;
   for (uint32_t i = b0; i < b1; ++i) {
-    bool below = canon(keys[i]) < pc;
+    const bool below = canon(S.krow[S.perm[g.pos + i]]) < pc;
     cnt += (i < lt) ? !below : below;
   }
   uint32_t n2;
-  uint32_t r = block_excl_scan<SMALL_THREADS>(cnt, &n2, sh_warp);
+  uint32_t r = block_excl_scan<SUB_THREADS>(cnt, &n2, sh_warp);
   for (uint32_t i = b0; i < b1; ++i) {
-    bool below = canon(keys[i]) < pc;
-    if ((i < lt) ? !below : below) plist[r++] = static_cast<uint16_t>(i);
+    const bool below = canon(S.krow[S.perm[g.pos + i]]) < pc;
+    if ((i < lt) ? !below : below) S.plist[g.pos + r++] = static_cast<uint16_t>(i);
   }
-  for (uint32_t i = threadIdx.x; i < len; i += SMALL_THREADS) cur[i] = static_cast<uint16_t>(i);
   __syncthreads();
-  // swap R[i] <-> L[n-1-i]: the row at plist[2n-1-j] lands on plist[j]
-  for (uint32_t j = threadIdx.x; j < n2; j += SMALL_THREADS) cur[plist[j]] = plist[n2 - 1 - j];
+  constexpr int MV = SMALL_MAX / SUB_THREADS;
+  uint16_t moved[MV];
+#pragma unroll
+  for (int t = 0; t < MV; ++t) {
+    const uint32_t jj = tid + SUB_THREADS * t;
+    moved[t] = jj < n2 ? S.perm[g.pos + S.plist[g.pos + n2 - 1 - jj]] : 0;
+  }
   __syncthreads();
-  if (mid > lt && threadIdx.x == 0) {
-    // pivot-equal fix-up (build.rs:303-313), sequentially on the shared copy
+#pragma unroll
+  for (int t = 0; t < MV; ++t) {
+    const uint32_t jj = tid + SUB_THREADS * t;
+    if (jj < n2) S.perm[g.pos + S.plist[g.pos + jj]] = moved[t];
+  }
+  __syncthreads();
+  if (mid > lt && tid == 0) {
     uint32_t place = lt, scan = lt;
-    while (place < mid && scan < len) {
-      if (canon(keys[cur[scan]]) == pc) {
-        uint16_t t = cur[scan];
-        cur[scan] = cur[place];
-        cur[place] = t;
+    while (place < mid && scan < g.len) {
+      if (canon(S.krow[S.perm[g.pos + scan]]) == pc) {
+        const uint16_t x = S.perm[g.pos + scan];
+        S.perm[g.pos + scan] = S.perm[g.pos + place];
+        S.perm[g.pos + place] = x;
         ++place;
       }
       ++scan;
     }
   }
+  if (tid == 0) sub_record(A, cn, lo_len, j, g, dim, pivot);
   __syncthreads();
-  // gather rows into their new positions
-  for (uint64_t f = threadIdx.x; f < static_cast<uint64_t>(len) * d; f += SMALL_THREADS) {
-    uint32_t p = static_cast<uint32_t>(f / d);
-    uint32_t j = static_cast<uint32_t>(f - static_cast<uint64_t>(p) * d);
-    dout[f] = din[static_cast<uint64_t>(cur[p]) * d + j];
+}
+
+__global__ void __launch_bounds__(SUB_THREADS) k_small_subtree(SubArgs A) {
+  extern __shared__ __align__(16) unsigned char sub_smem[];
+  SubShared& S = *reinterpret_cast<SubShared*>(sub_smem);
+  __shared__ uint32_t lo_len[KD_MAX_DEPTH + 1];
+  __shared__ uint32_t cn[KD_MAX_DEPTH + 1][2];
+  __shared__ SubReduce red;
+  __shared__ uint32_t hist[256];
+  __shared__ uint32_t sh_warp[SUB_WARPS];
+  __shared__ uint64_t s_sel;
+  __shared__ uint32_t s_rank;
+  __shared__ int s_depths;
+
+  const uint32_t node0 = A.seg_node[blockIdx.x];
+  if (node0 == HOLE) return;
+  const uint32_t row0 = A.seg_start[blockIdx.x], l0 = A.seg_len[blockIdx.x];
+  const uint64_t d = A.d;
+  if (threadIdx.x == 0) {
+    // segment lengths at depth i are floor / ceil of l0 / 2^i
+    int i = 0;
+    for (;; ++i) {
+      const uint32_t lo = l0 >> i, hi = (l0 + (1u << i) - 1) >> i;
+      lo_len[i] = lo;
+      cn[i][0] = static_cast<uint32_t>(count_nodes_impl(lo, A.leafsize));
+      cn[i][1] = static_cast<uint32_t>(count_nodes_impl(lo + 1, A.leafsize));
+      if (hi <= A.leafsize || i == KD_MAX_DEPTH) break;
+    }
+    s_depths = i + 1;  // depths 0 .. i hold segments
   }
-  for (uint32_t i = threadIdx.x; i < len; i += SMALL_THREADS) iout[i] = iin[cur[i]];
-  if (threadIdx.x == 0) expand_inner(L, slot, node, start, len, dim, pk);
-  // children's boxes start at the identities of min / max
-  uint64_t* cl = L.boxkeys + static_cast<uint64_t>(node + 1) * 2 * d;
-  uint64_t* cr = L.boxkeys + static_cast<uint64_t>(node + 1 + count_nodes_impl(mid, L.leafsize)) * 2 * d;
-  for (uint64_t j = threadIdx.x; j < 2 * d; j += SMALL_THREADS) {
-    cl[j] = (j < d) ? KEY_MAX : 0;
-    cr[j] = (j < d) ? KEY_MAX : 0;
+  for (uint32_t p = threadIdx.x; p < l0; p += SUB_THREADS) S.perm[p] = static_cast<uint16_t>(p);
+  __syncthreads();
+  bool bad = false;
+  const uint32_t wid = threadIdx.x >> 5;
+  for (int j = 0; j < s_depths; ++j) {
+    const uint32_t hi_len = (l0 + (1u << j) - 1) >> j;
+    const uint32_t n_seg = 1u << j;
+    if (hi_len > static_cast<uint32_t>(WARP_SEG)) {
+      for (uint32_t sidx = 0; sidx < n_seg; ++sidx) {
+        SubSeg g;
+        if (!sub_segment(lo_len, cn, node0, l0, A.leafsize, j, sidx, &g)) continue;  // uniform
+        sub_split_block(A, S, cn, lo_len, j, g, row0, &bad, &red, hist, sh_warp, &s_sel, &s_rank);
+      }
+    } else {
+      for (uint32_t sidx = wid; sidx < n_seg; sidx += SUB_WARPS) {
+        SubSeg g;
+        if (!sub_segment(lo_len, cn, node0, l0, A.leafsize, j, sidx, &g)) continue;  // uniform per warp
+        sub_split_warp(A, S, cn, lo_len, j, g, row0, &bad);
+      }
+    }
+    __syncthreads();
   }
+  if (A.check_finite && bad) atomicOr(A.status, 1u);
+  // the subtree's rows, once, in their final order
+  for (uint64_t f = threadIdx.x; f < static_cast<uint64_t>(l0) * d; f += SUB_THREADS) {
+    const uint32_t p = static_cast<uint32_t>(f / d);
+    const uint32_t jd = static_cast<uint32_t>(f - static_cast<uint64_t>(p) * d);
+    A.dout[static_cast<uint64_t>(row0) * d + f] = A.din[(static_cast<uint64_t>(row0) + S.perm[p]) * d + jd];
+  }
+  for (uint32_t p = threadIdx.x; p < l0; p += SUB_THREADS) A.iout[row0 + p] = A.iin[row0 + S.perm[p]];
 }
 
 // ---------------------------------------------------------------------------
@@ -937,11 +1243,20 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
     if (s.any_inner && s.max_len > static_cast<uint64_t>(SMALL_MAX)) large_slots = std::max(large_slots, s.slots);
   const uint32_t max_chunks = static_cast<uint32_t>((n + LG_CHUNK - 1) / LG_CHUNK);
 
-  // Rows are permuted once per level with an inner node (every level but the
-  // last).  Level 0 reads the input itself; the levels then alternate between
-  // the tree's own row array and a scratch one, arranged so that the last level
-  // writes the tree's.
-  const size_t n_perm = shape.size() - 1;
+  // The levels above SMALL_MAX rows permute rows level by level (large path);
+  // from the first level at or below it, one CTA per segment builds the rest
+  // of that segment's subtree and writes its rows in their final order.  When
+  // that level holds leaves only and lies below a large level (leafsize >
+  // SMALL_MAX / 2), it just records them.  Level 0 reads the input itself; the
+  // levels alternate between the tree's own row array and a scratch one,
+  // arranged so that the last writer writes the tree's.
+  size_t lv_small = 0;
+  while (lv_small + 1 < shape.size() && shape[lv_small].max_len > static_cast<uint64_t>(SMALL_MAX) &&
+         shape[lv_small].any_inner)
+    ++lv_small;
+  const bool by_subtree = shape[lv_small].max_len <= static_cast<uint64_t>(SMALL_MAX) &&
+                          (lv_small == 0 || shape[lv_small].any_inner);
+  const size_t n_perm = lv_small + (by_subtree ? 1 : 0);  // writers: large levels (+ the subtree kernel)
   const bool need_pad = padded_rows(d) && (d + 3) / 4 * 4 != d;
   const uint64_t w32 = (d + 3) / 4 * 4;
 
@@ -1007,14 +1322,15 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
     carve_tree(ct);
     carve_scratch(cs);
   }
-  // level lv writes the tree's arrays when (n_perm - 1 - lv) is even
+  // writer lv (the large levels, then the subtree kernel) writes the tree's
+  // arrays when (n_perm - 1 - lv) is even
   auto writes_tree = [&](size_t lv) { return ((n_perm - 1 - lv) & 1) == 0; };
 
   k_init_boxkeys<<<grid1(2 * d, 256), 256, 0, st>>>(T.boxes, 1, d);
   KD_TRY_CUDA(cudaMemsetAsync(X.status, 0, sizeof(uint32_t), st));
   const double* din;
   const uint32_t* iin;
-  if (n_perm == 0) {  // the root is a leaf
+  if (n_perm == 0) {  // the root is a leaf of more than SMALL_MAX rows
     KD_TRY_CUDA(cudaMemcpyAsync(T.data, d_src, n * d * sizeof(double), cudaMemcpyDeviceToDevice, st));
     k_iota<<<grid1(n, 256), 256, 0, st>>>(T.idx, n);
     din = T.data;
@@ -1028,8 +1344,8 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
   }
   k_root_segment<<<1, 1, 0, st>>>(X.seg[0][0], X.seg[0][1], X.seg[0][2], static_cast<uint32_t>(n));
   KD_TRY_CUDA(cudaGetLastError());
-  KD_TRY_CUDA(cudaFuncSetAttribute(k_small_level, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   static_cast<int>(SMALL_MAX * (sizeof(uint64_t) + 2 * sizeof(uint16_t)))));
+  KD_TRY_CUDA(cudaFuncSetAttribute(k_small_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(sizeof(SubShared))));
 
   int cur = 0;
   const unsigned bbox_threads = d <= 256 ? static_cast<unsigned>(d * (256 / d)) : 256u;
@@ -1046,10 +1362,19 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
             X.seg[cur][0], X.seg[cur][1], X.seg[cur][2],
             X.seg[cur ^ 1][0], X.seg[cur ^ 1][1], X.seg[cur ^ 1][2],
             T.nodes, T.boxes, X.node_len, s.slots};
-    // Boxes: the root and every level below the large path's levels come from
-    // the bbox kernel (the small path initialises its children's box keys).
-    // Level 0 also checks that every coordinate is finite; the status is read
-    // once the build has finished (non-finite keys still order consistently).
+    if (lv == lv_small && by_subtree) {
+      // every box, split and record below, and the rows in their final order;
+      // at level 0 it also checks that every coordinate is finite
+      SubArgs A{din, iin, dout, iout, d, static_cast<uint32_t>(leafsize),
+                X.seg[cur][0], X.seg[cur][1], X.seg[cur][2], T.nodes, T.boxes, X.node_len, lv == 0, X.status};
+      k_small_subtree<<<static_cast<unsigned>(s.slots), SUB_THREADS, sizeof(SubShared), st>>>(A);
+      KD_TRY_CUDA(cudaGetLastError());
+      break;
+    }
+    // Boxes of the large levels (and of a leaves-only last level) come from the
+    // bbox kernel.  Level 0 also checks that every coordinate is finite; the
+    // status is read once the build has finished (non-finite keys still order
+    // consistently).
     {
       const uint64_t chunk_rows = std::max<uint64_t>(1, (bbox_threads * 8) / d);
       const uint64_t nchunk = (s.max_len + chunk_rows - 1) / chunk_rows;
@@ -1063,11 +1388,7 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
       KD_TRY_CUDA(cudaGetLastError());
       break;
     }
-    if (s.max_len <= static_cast<uint64_t>(SMALL_MAX)) {
-      const size_t smem = SMALL_MAX * (sizeof(uint64_t) + 2 * sizeof(uint16_t));
-      k_small_level<<<static_cast<unsigned>(s.slots), SMALL_THREADS, smem, st>>>(L);
-      KD_TRY_CUDA(cudaGetLastError());
-    } else {
+    {
       const LargeScratch& S = X.lg;
       const uint32_t nch = static_cast<uint32_t>((s.max_len + LG_CHUNK - 1) / LG_CHUNK);
       dim3 g(static_cast<unsigned>(s.slots), std::min<uint32_t>(nch, 65535u));

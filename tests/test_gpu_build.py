@@ -2,8 +2,9 @@
 tree-ordered rows, original indices, node records (including order_by_box),
 split values and per-node boxes (src/build.rs, src/tree.rs, src/layout.rs).
 
-The cases cover the one-CTA shared-memory path (segments <= 8192 rows), the
-multi-CTA path of the top levels, the pivot-equal fix-up of partition_rows in
+The cases cover the one-CTA subtree path (segments <= 8192 rows, split by the
+whole CTA above 512 rows and by one warp below), the multi-CTA path of the top
+levels, a leaves-only last level below them (large leafsize), the pivot-equal fix-up of partition_rows in
 both (duplicated coordinates), a root that is a leaf, leafsize 1, widths 1 to
 64, data on a line that sets order_by_box, and the parallel flag."""
 import zlib
@@ -52,6 +53,10 @@ CASES = {
     "grid-ties": (lambda r: np.stack(np.meshgrid(np.arange(40.0), np.arange(40.0)), -1).reshape(-1, 2), 3),
     "large-leafsize": (lambda r: r.normal(size=(50_000, 2)), 10_000),
     "big-range": (lambda r: r.normal(size=(10_000, 3)) * 1e300, 16),
+    "root-leaf-above-8192": (lambda r: r.normal(size=(9000, 2)), 10_000),
+    "n-8192": (lambda r: r.uniform(size=(8192, 3)), 16),
+    "n-8193": (lambda r: r.uniform(size=(8193, 3)), 16),
+    "signed-zeros": (lambda r: r.choice([-0.0, 0.0, 1.0, -1.0], size=(20_000, 2)), 8),
 }
 
 

@@ -273,15 +273,16 @@ __device__ uint32_t block_sum(uint32_t v, uint32_t* sh_warp) {
 // record, down to the leaves -- and then writes the subtree's rows once, in
 // their final order.  The rows stay where the level above left them: the CTA
 // permutes 16-bit local row numbers (perm: position -> local row) and keeps each
-// local row's key on its segment's current split dimension (krow).  A segment
-// longer than WARP_SEG rows is split by the whole CTA, shorter ones by one warp
-// each, the segments of a depth spread over the warps.  Segment (depth j, index
-// s) is reached from the subtree root by the bits of s, with the node counts of
-// the at most two segment lengths of each depth.
+// local row's key on its segment's current split dimension (krow).  All the
+// segments of a depth are split at once, each by a group of warps (the whole
+// CTA for the subtree root, one warp each for segments of at most WARP_SEG
+// rows) synchronised on its own named barrier.  Segment (depth j, index s) is
+// reached from the subtree root by the bits of s, with the node counts of the
+// at most two segment lengths of each depth.
 // ---------------------------------------------------------------------------
 constexpr int SUB_THREADS = 512;
 constexpr int SUB_WARPS = SUB_THREADS / 32;
-constexpr int WARP_SEG = 512;  // longest segment one warp splits (16 keys a lane)
+constexpr int WARP_SEG = 512;  // rows a warp of a group takes (16 keys a lane)
 constexpr uint32_t FULL = 0xffffffffu;
 
 struct SubArgs {
@@ -361,14 +362,102 @@ __device__ __forceinline__ void sub_record(const SubArgs& A, const uint32_t (*cn
   A.node_len[g.node] = g.len;
 }
 
-// One segment split by one warp (g.len <= WARP_SEG).  Keys live in registers
-// (positions pos + 32 t + lane); the pivot is found bit by bit from the first
+// Group-wide collectives for G warps (G = 1, 2, 4, 8, 16) of group `gid`:
+// every thread of the group gets the result.  `red` holds one word per warp.
+struct SubReduce {
+  uint64_t lo[SUB_WARPS], hi[SUB_WARPS];
+  uint32_t sum[SUB_WARPS];
+};
+template <int G>
+__device__ __forceinline__ void group_sync(uint32_t gid) {
+  if constexpr (G == 1) {
+    __syncwarp();
+  } else if constexpr (G == SUB_WARPS) {
+    __syncthreads();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + gid), "r"(G * 32) : "memory");
+  }
+}
+template <int G>
+__device__ __forceinline__ uint32_t group_add(uint32_t v, SubReduce* red, uint32_t gid) {
+  v = __reduce_add_sync(FULL, v);
+  if constexpr (G == 1) {
+    return v;
+  } else {
+    const uint32_t w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) red->sum[w] = v;
+    group_sync<G>(gid);
+    uint32_t t = 0;
+#pragma unroll
+    for (int i = 0; i < G; ++i) t += red->sum[gid * G + i];
+    group_sync<G>(gid);
+    return t;
+  }
+}
+template <int G>
+__device__ __forceinline__ void group_minmax(uint64_t* lo, uint64_t* hi, SubReduce* red, uint32_t gid) {
+  uint64_t a = warp_min64(*lo), b = warp_max64(*hi);
+  if constexpr (G > 1) {
+    const uint32_t w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+      red->lo[w] = a;
+      red->hi[w] = b;
+    }
+    group_sync<G>(gid);
+    a = red->lo[gid * G];
+    b = red->hi[gid * G];
+#pragma unroll
+    for (int i = 1; i < G; ++i) {
+      a = red->lo[gid * G + i] < a ? red->lo[gid * G + i] : a;
+      b = red->hi[gid * G + i] > b ? red->hi[gid * G + i] : b;
+    }
+    group_sync<G>(gid);
+  }
+  *lo = a;
+  *hi = b;
+}
+// Exclusive prefix of v over the group's threads in order; *total: the sum.
+template <int G>
+__device__ __forceinline__ uint32_t group_excl_scan(uint32_t v, uint32_t* total, SubReduce* red, uint32_t gid) {
+  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(FULL, x, o);
+    if (lane >= static_cast<uint32_t>(o)) x += y;
+  }
+  const uint32_t wtot = __shfl_sync(FULL, x, 31);
+  if constexpr (G == 1) {
+    *total = wtot;
+    return x - v;
+  } else {
+    if (lane == 0) red->sum[w] = wtot;
+    group_sync<G>(gid);
+    uint32_t before = 0, all = 0;
+#pragma unroll
+    for (int i = 0; i < G; ++i) {
+      const uint32_t c = red->sum[gid * G + i];
+      before += (gid * G + i < w) ? c : 0;
+      all += c;
+    }
+    group_sync<G>(gid);
+    *total = all;
+    return before + x - v;
+  }
+}
+
+// One segment split by a group of G warps (g.len <= 512 G): each thread owns
+// a contiguous run of at most 16 positions, so misplaced ranks ascend in thread
+// order.  The pivot is found bit by bit (a group sum per bit) from the first
 // bit where the segment's smallest and largest keys differ.
-__device__ void sub_split_warp(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2], const uint32_t* lo_len,
-                               int j, const SubSeg& g, uint64_t row0, bool* bad) {
-  constexpr int T = WARP_SEG / 32;
-  const uint32_t lane = threadIdx.x & 31;
+template <int G>
+__device__ void sub_split(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2], const uint32_t* lo_len, int j,
+                          const SubSeg& g, uint64_t row0, bool* bad, SubReduce* red, uint32_t gid) {
+  constexpr int T = WARP_SEG / 32;  // positions a thread owns, at most
+  const uint32_t tg = (threadIdx.x & 31) + 32u * ((threadIdx.x >> 5) % G);  // thread within the group
   const uint64_t d = A.d;
+  const uint32_t per = (g.len + 32u * G - 1) / (32u * G);
+  const uint32_t b0 = min(g.len, tg * per), nown = min(g.len, b0 + per) - b0;
   uint32_t best_dim = 0;
   double best_span = 0.0;
   uint64_t blo = 0, bhi = 0;
@@ -376,18 +465,16 @@ __device__ void sub_split_warp(const SubArgs& A, SubShared& S, const uint32_t (*
     uint64_t lo = KEY_MAX, hi = 0;
 #pragma unroll
     for (int t = 0; t < T; ++t) {
-      const uint32_t p = 32u * t + lane;
-      if (p < g.len) {
-        const double v = A.din[(row0 + S.perm[g.pos + p]) * d + dj];
+      if (t < static_cast<int>(nown)) {
+        const double v = A.din[(row0 + S.perm[g.pos + b0 + t]) * d + dj];
         *bad |= !isfinite(v);
         const uint64_t k = total_key(v);
         lo = k < lo ? k : lo;
         hi = k > hi ? k : hi;
       }
     }
-    lo = warp_min64(lo);
-    hi = warp_max64(hi);
-    if (lane == 0) {
+    group_minmax<G>(&lo, &hi, red, gid);
+    if (tg == 0) {
       A.boxkeys[static_cast<uint64_t>(g.node) * 2 * d + dj] = lo;
       A.boxkeys[static_cast<uint64_t>(g.node) * 2 * d + d + dj] = hi;
     }
@@ -400,7 +487,7 @@ __device__ void sub_split_warp(const SubArgs& A, SubShared& S, const uint32_t (*
     }
   }
   if (g.len <= A.leafsize) {
-    if (lane == 0) {
+    if (tg == 0) {
       write_leaf(A.nodes, g.node, static_cast<uint32_t>(row0) + g.pos, g.len);
       A.node_len[g.node] = g.len;
     }
@@ -410,10 +497,9 @@ __device__ void sub_split_warp(const SubArgs& A, SubShared& S, const uint32_t (*
   uint64_t key[T];
 #pragma unroll
   for (int t = 0; t < T; ++t) {
-    const uint32_t p = 32u * t + lane;
     key[t] = 0;
-    if (p < g.len) {
-      const uint32_t lr = S.perm[g.pos + p];
+    if (t < static_cast<int>(nown)) {
+      const uint32_t lr = S.perm[g.pos + b0 + t];
       key[t] = total_key(A.din[(row0 + lr) * d + dim]);
       S.krow[lr] = key[t];
     }
@@ -427,13 +513,9 @@ __device__ void sub_split_warp(const SubArgs& A, SubShared& S, const uint32_t (*
     for (int b = hb; b >= 0; --b) {
       uint32_t c0 = 0;
 #pragma unroll
-      for (int t = 0; t < T; ++t) {
-        const uint32_t p = 32u * t + lane;
-        const uint64_t k = key[t];
-        c0 += p < g.len && ((k ^ prefix) >> b) == 0;  // matches the prefix, bit b clear
-      }
-      c0 = __reduce_add_sync(FULL, c0);
-      if (rank >= c0) {
+      for (int t = 0; t < T; ++t) c0 += t < static_cast<int>(nown) && ((key[t] ^ prefix) >> b) == 0;
+      c0 = group_add<G>(c0, red, gid);
+      if (rank >= c0) {  // every thread of the group decides alike
         rank -= c0;
         prefix |= 1ull << b;
       }
@@ -444,35 +526,39 @@ __device__ void sub_split_warp(const SubArgs& A, SubShared& S, const uint32_t (*
   // lt = #{key < pivot} under f64 '<' (build.rs:209)
   uint32_t my_lt = 0;
 #pragma unroll
-  for (int t = 0; t < T; ++t) my_lt += (32u * t + lane < g.len) && canon(key[t]) < pc;
-  const uint32_t lt = __reduce_add_sync(FULL, my_lt);
-  // misplaced positions in ascending order (ranks from ballots)
-  uint32_t n2 = 0;
+  for (int t = 0; t < T; ++t) my_lt += t < static_cast<int>(nown) && canon(key[t]) < pc;
+  const uint32_t lt = group_add<G>(my_lt, red, gid);
+  // misplaced positions: key >= pivot in [0, lt), key < pivot in [lt, len)
+  uint32_t cnt = 0;
 #pragma unroll
   for (int t = 0; t < T; ++t) {
-    const uint32_t p = 32u * t + lane;
     const bool below = canon(key[t]) < pc;
-    const bool mis = p < g.len && ((p < lt) ? !below : below);
-    const uint32_t m = __ballot_sync(FULL, mis);
-    if (mis) S.plist[g.pos + n2 + __popc(m & ((1u << lane) - 1))] = static_cast<uint16_t>(p);
-    n2 += __popc(m);
+    cnt += t < static_cast<int>(nown) && ((b0 + t < lt) ? !below : below);
   }
-  __syncwarp();
+  uint32_t n2;
+  uint32_t r = group_excl_scan<G>(cnt, &n2, red, gid);
+#pragma unroll
+  for (int t = 0; t < T; ++t) {
+    const bool below = canon(key[t]) < pc;
+    if (t < static_cast<int>(nown) && ((b0 + t < lt) ? !below : below))
+      S.plist[g.pos + r++] = static_cast<uint16_t>(b0 + t);
+  }
+  group_sync<G>(gid);
   // swap R[i] <-> L[n-1-i]: the row at plist[n2-1-j] lands on plist[j]
   uint16_t moved[T];
 #pragma unroll
   for (int t = 0; t < T; ++t) {
-    const uint32_t jj = 32u * t + lane;
+    const uint32_t jj = tg + 32u * G * t;
     moved[t] = jj < n2 ? S.perm[g.pos + S.plist[g.pos + n2 - 1 - jj]] : 0;
   }
-  __syncwarp();
+  group_sync<G>(gid);
 #pragma unroll
   for (int t = 0; t < T; ++t) {
-    const uint32_t jj = 32u * t + lane;
+    const uint32_t jj = tg + 32u * G * t;
     if (jj < n2) S.perm[g.pos + S.plist[g.pos + jj]] = moved[t];
   }
-  __syncwarp();
-  if (mid > lt && lane == 0) {
+  group_sync<G>(gid);
+  if (mid > lt && tg == 0) {
     // pivot-equal fix-up (build.rs:303-313), sequentially
     uint32_t place = lt, scan = lt;
     while (place < mid && scan < g.len) {
@@ -485,197 +571,20 @@ __device__ void sub_split_warp(const SubArgs& A, SubShared& S, const uint32_t (*
       ++scan;
     }
   }
-  __syncwarp();
-  if (lane == 0) sub_record(A, cn, lo_len, j, g, dim, pivot);
+  if (tg == 0) sub_record(A, cn, lo_len, j, g, dim, pivot);
+  group_sync<G>(gid);
 }
 
-// Block-wide min / max of u64 values and sum of u32 ones (every thread gets
-// the result; `red` holds SUB_WARPS words of each).
-struct SubReduce {
-  uint64_t lo[SUB_WARPS], hi[SUB_WARPS];
-  uint32_t sum[SUB_WARPS];
-};
-__device__ __forceinline__ void block_minmax(uint64_t* lo, uint64_t* hi, SubReduce* red) {
-  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  uint64_t a = warp_min64(*lo), b = warp_max64(*hi);
-  if (lane == 0) {
-    red->lo[w] = a;
-    red->hi[w] = b;
+// Every segment of depth j, split by groups of G warps.
+template <int G>
+__device__ void sub_depth(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2], const uint32_t* lo_len, int j,
+                          uint32_t node0, uint32_t l0, uint64_t row0, bool* bad, SubReduce* red) {
+  const uint32_t gid = (threadIdx.x >> 5) / G;
+  for (uint32_t sidx = gid; sidx < (1u << j); sidx += SUB_WARPS / G) {
+    SubSeg g;
+    if (!sub_segment(lo_len, cn, node0, l0, A.leafsize, j, sidx, &g)) continue;  // uniform per group
+    sub_split<G>(A, S, cn, lo_len, j, g, row0, bad, red, gid);
   }
-  __syncthreads();
-  a = red->lo[0];
-  b = red->hi[0];
-#pragma unroll
-  for (int i = 1; i < SUB_WARPS; ++i) {
-    a = red->lo[i] < a ? red->lo[i] : a;
-    b = red->hi[i] > b ? red->hi[i] : b;
-  }
-  __syncthreads();
-  *lo = a;
-  *hi = b;
-}
-__device__ __forceinline__ uint32_t block_add(uint32_t v, SubReduce* red) {
-  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  v = __reduce_add_sync(FULL, v);
-  if (lane == 0) red->sum[w] = v;
-  __syncthreads();
-  uint32_t t = 0;
-#pragma unroll
-  for (int i = 0; i < SUB_WARPS; ++i) t += red->sum[i];
-  __syncthreads();
-  return t;
-}
-
-// One segment split by the whole CTA (WARP_SEG < g.len <= SMALL_MAX): 8-bit
-// radix select from the first byte where the segment's smallest and largest
-// keys differ, the digit counts aggregated per warp before the shared atomics.
-__device__ void sub_split_block(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2], const uint32_t* lo_len,
-                                int j, const SubSeg& g, uint64_t row0, bool* bad, SubReduce* red,
-                                uint32_t* hist, uint32_t* sh_warp, uint64_t* s_sel, uint32_t* s_rank) {
-  const uint32_t tid = threadIdx.x, lane = tid & 31;
-  const uint64_t d = A.d;
-  uint32_t best_dim = 0;
-  double best_span = 0.0;
-  uint64_t blo = 0, bhi = 0;
-  for (uint64_t dj = 0; dj < d; ++dj) {
-    uint64_t lo = KEY_MAX, hi = 0;
-    for (uint32_t p = tid; p < g.len; p += SUB_THREADS) {
-      const double v = A.din[(row0 + S.perm[g.pos + p]) * d + dj];
-      *bad |= !isfinite(v);
-      const uint64_t k = total_key(v);
-      lo = k < lo ? k : lo;
-      hi = k > hi ? k : hi;
-    }
-    block_minmax(&lo, &hi, red);
-    if (tid == 0) {
-      A.boxkeys[static_cast<uint64_t>(g.node) * 2 * d + dj] = lo;
-      A.boxkeys[static_cast<uint64_t>(g.node) * 2 * d + d + dj] = hi;
-    }
-    const double span = dsub(from_total_key(hi), from_total_key(lo));
-    if (dj == 0 || span > best_span) {
-      best_span = span;
-      best_dim = static_cast<uint32_t>(dj);
-      blo = lo;
-      bhi = hi;
-    }
-  }
-  if (g.len <= A.leafsize) {
-    if (tid == 0) {
-      write_leaf(A.nodes, g.node, static_cast<uint32_t>(row0) + g.pos, g.len);
-      A.node_len[g.node] = g.len;
-    }
-    return;
-  }
-  const uint32_t dim = best_dim, mid = g.len / 2;
-  for (uint32_t p = tid; p < g.len; p += SUB_THREADS) {
-    const uint32_t lr = S.perm[g.pos + p];
-    S.krow[lr] = total_key(A.din[(row0 + lr) * d + dim]);
-  }
-  __syncthreads();
-  uint64_t pivot = blo;
-  if (blo != bhi) {
-    const int hb = 63 - __clzll(static_cast<long long>(blo ^ bhi));
-    const int top = hb / 8 * 8;  // lowest bit of the first byte that differs
-    if (tid == 0) {
-      *s_sel = top == 56 ? 0 : (blo >> (top + 8)) << (top + 8);
-      *s_rank = mid;
-    }
-    for (int shift = top; shift >= 0; shift -= 8) {
-      for (int b = tid; b < 256; b += SUB_THREADS) hist[b] = 0;
-      __syncthreads();
-      const uint64_t prefix = *s_sel;
-      for (uint32_t base = 0; base < g.len; base += SUB_THREADS) {
-        const uint32_t p = base + tid;
-        bool in = false;
-        uint32_t digit = 256 + lane;  // distinct per lane when not counted
-        if (p < g.len) {
-          const uint64_t k = S.krow[S.perm[g.pos + p]];
-          in = shift == 56 || ((k ^ prefix) >> (shift + 8)) == 0;
-          if (in) digit = static_cast<uint32_t>(k >> shift) & 255u;
-        }
-        const uint32_t same = __match_any_sync(FULL, digit);
-        if (in && lane == static_cast<uint32_t>(__ffs(same) - 1)) atomicAdd(&hist[digit], __popc(same));
-      }
-      __syncthreads();
-      if (tid < 32) {
-        uint32_t c[8], sum = 0;
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          c[i] = hist[lane * 8 + i];
-          sum += c[i];
-        }
-        uint32_t x = sum;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t y = __shfl_up_sync(FULL, x, o);
-          if (lane >= o) x += y;
-        }
-        const uint32_t excl = x - sum, rank = *s_rank;
-        __syncwarp();
-        if (excl <= rank && rank < x) {
-          uint32_t acc = excl;
-#pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            if (acc <= rank && rank < acc + c[i]) {
-              *s_sel = prefix | (static_cast<uint64_t>(lane * 8 + i) << shift);
-              *s_rank = rank - acc;
-            }
-            acc += c[i];
-          }
-        }
-      }
-      __syncthreads();
-    }
-    pivot = *s_sel;
-    __syncthreads();
-  }
-  const uint64_t pc = canon(pivot);
-  uint32_t my_lt = 0;
-  for (uint32_t p = tid; p < g.len; p += SUB_THREADS) my_lt += canon(S.krow[S.perm[g.pos + p]]) < pc;
-  const uint32_t lt = block_add(my_lt, red);
-  // misplaced positions: each thread owns a contiguous run, so ranks ascend
-  const uint32_t per = (g.len + SUB_THREADS - 1) / SUB_THREADS;
-  const uint32_t b0 = min(g.len, tid * per), b1 = min(g.len, b0 + per);
-  uint32_t cnt = 0;
-  for (uint32_t i = b0; i < b1; ++i) {
-    const bool below = canon(S.krow[S.perm[g.pos + i]]) < pc;
-    cnt += (i < lt) ? !below : below;
-  }
-  uint32_t n2;
-  uint32_t r = block_excl_scan<SUB_THREADS>(cnt, &n2, sh_warp);
-  for (uint32_t i = b0; i < b1; ++i) {
-    const bool below = canon(S.krow[S.perm[g.pos + i]]) < pc;
-    if ((i < lt) ? !below : below) S.plist[g.pos + r++] = static_cast<uint16_t>(i);
-  }
-  __syncthreads();
-  constexpr int MV = SMALL_MAX / SUB_THREADS;
-  uint16_t moved[MV];
-#pragma unroll
-  for (int t = 0; t < MV; ++t) {
-    const uint32_t jj = tid + SUB_THREADS * t;
-    moved[t] = jj < n2 ? S.perm[g.pos + S.plist[g.pos + n2 - 1 - jj]] : 0;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int t = 0; t < MV; ++t) {
-    const uint32_t jj = tid + SUB_THREADS * t;
-    if (jj < n2) S.perm[g.pos + S.plist[g.pos + jj]] = moved[t];
-  }
-  __syncthreads();
-  if (mid > lt && tid == 0) {
-    uint32_t place = lt, scan = lt;
-    while (place < mid && scan < g.len) {
-      if (canon(S.krow[S.perm[g.pos + scan]]) == pc) {
-        const uint16_t x = S.perm[g.pos + scan];
-        S.perm[g.pos + scan] = S.perm[g.pos + place];
-        S.perm[g.pos + place] = x;
-        ++place;
-      }
-      ++scan;
-    }
-  }
-  if (tid == 0) sub_record(A, cn, lo_len, j, g, dim, pivot);
-  __syncthreads();
 }
 
 __global__ void __launch_bounds__(SUB_THREADS) k_small_subtree(SubArgs A) {
@@ -684,10 +593,6 @@ __global__ void __launch_bounds__(SUB_THREADS) k_small_subtree(SubArgs A) {
   __shared__ uint32_t lo_len[KD_MAX_DEPTH + 1];
   __shared__ uint32_t cn[KD_MAX_DEPTH + 1][2];
   __shared__ SubReduce red;
-  __shared__ uint32_t hist[256];
-  __shared__ uint32_t sh_warp[SUB_WARPS];
-  __shared__ uint64_t s_sel;
-  __shared__ uint32_t s_rank;
   __shared__ int s_depths;
 
   const uint32_t node0 = A.seg_node[blockIdx.x];
@@ -709,23 +614,16 @@ __global__ void __launch_bounds__(SUB_THREADS) k_small_subtree(SubArgs A) {
   for (uint32_t p = threadIdx.x; p < l0; p += SUB_THREADS) S.perm[p] = static_cast<uint16_t>(p);
   __syncthreads();
   bool bad = false;
-  const uint32_t wid = threadIdx.x >> 5;
   for (int j = 0; j < s_depths; ++j) {
+    // warps a segment of this depth gets: the longest is split by groups of
+    // at least ceil(len / 512) warps, so a thread owns at most 16 positions
     const uint32_t hi_len = (l0 + (1u << j) - 1) >> j;
-    const uint32_t n_seg = 1u << j;
-    if (hi_len > static_cast<uint32_t>(WARP_SEG)) {
-      for (uint32_t sidx = 0; sidx < n_seg; ++sidx) {
-        SubSeg g;
-        if (!sub_segment(lo_len, cn, node0, l0, A.leafsize, j, sidx, &g)) continue;  // uniform
-        sub_split_block(A, S, cn, lo_len, j, g, row0, &bad, &red, hist, sh_warp, &s_sel, &s_rank);
-      }
-    } else {
-      for (uint32_t sidx = wid; sidx < n_seg; sidx += SUB_WARPS) {
-        SubSeg g;
-        if (!sub_segment(lo_len, cn, node0, l0, A.leafsize, j, sidx, &g)) continue;  // uniform per warp
-        sub_split_warp(A, S, cn, lo_len, j, g, row0, &bad);
-      }
-    }
+    const uint32_t need = (hi_len + WARP_SEG - 1) / WARP_SEG;
+    if (need > 8) sub_depth<16>(A, S, cn, lo_len, j, node0, l0, row0, &bad, &red);
+    else if (need > 4) sub_depth<8>(A, S, cn, lo_len, j, node0, l0, row0, &bad, &red);
+    else if (need > 2) sub_depth<4>(A, S, cn, lo_len, j, node0, l0, row0, &bad, &red);
+    else if (need > 1) sub_depth<2>(A, S, cn, lo_len, j, node0, l0, row0, &bad, &red);
+    else sub_depth<1>(A, S, cn, lo_len, j, node0, l0, row0, &bad, &red);
     __syncthreads();
   }
   if (A.check_finite && bad) atomicOr(A.status, 1u);
@@ -754,6 +652,7 @@ struct LargeScratch {
   uint32_t* seg_lt;     // slots
   uint32_t* chunk_cnt;  // slots * n_chunks
   uint32_t* seg_mis;    // slots
+  uint32_t* seg_first;  // slots: first radix pass whose byte the segment's keys do not share (8: all equal)
 };
 
 __global__ void k_lg_prepare(Level L, LargeScratch S) {
@@ -764,9 +663,17 @@ __global__ void k_lg_prepare(Level L, LargeScratch S) {
     S.seg_dim[slot] = NONE;
     return;
   }
-  S.seg_dim[slot] = widest_axis_keys(L.boxkeys + static_cast<uint64_t>(node) * 2 * L.d, L.d);
-  S.sel_prefix[slot * (RADIX_PASSES + 1)] = 0;
-  S.sel_rank[slot * (RADIX_PASSES + 1)] = L.seg_len[slot] / 2;
+  const uint64_t* box = L.boxkeys + static_cast<uint64_t>(node) * 2 * L.d;
+  const uint32_t dim = widest_axis_keys(box, L.d);
+  S.seg_dim[slot] = dim;
+  // every key lies between the box's smallest and largest on dim: the bytes
+  // those share need no histogram pass
+  const uint64_t blo = box[dim], bhi = box[L.d + dim];
+  const int first = blo == bhi ? RADIX_PASSES : __clzll(static_cast<long long>(blo ^ bhi)) / 8;
+  const uint64_t prefix = first == 0 ? 0 : (first == RADIX_PASSES ? blo : (blo >> (64 - 8 * first)) << (64 - 8 * first));
+  S.seg_first[slot] = static_cast<uint32_t>(first);
+  S.sel_prefix[slot * (RADIX_PASSES + 1) + first] = prefix;
+  S.sel_rank[slot * (RADIX_PASSES + 1) + first] = L.seg_len[slot] / 2;
   S.seg_lt[slot] = 0;
 }
 
@@ -813,12 +720,14 @@ __global__ void k_lg_hist(Level L, LargeScratch S, int pass) {
   __shared__ uint64_t s_prefix;
   const uint64_t slot = blockIdx.x;
   if (S.seg_dim[slot] == NONE) return;
+  const int first = static_cast<int>(S.seg_first[slot]);
+  if (pass < first) return;  // a byte every key of the segment shares
   const uint32_t start = L.seg_start[slot], len = L.seg_len[slot];
   if (blockIdx.y * LG_CHUNK >= len) return;
   for (int b = threadIdx.x; b < 256; b += LG_THREADS) sh[b] = 0;
   if (threadIdx.x == 0) {
-    uint64_t prefix = S.sel_prefix[slot * (RADIX_PASSES + 1) + (pass > 0 ? pass - 1 : 0)];
-    if (pass > 0) {
+    uint64_t prefix = S.sel_prefix[slot * (RADIX_PASSES + 1) + (pass > first ? pass - 1 : pass)];
+    if (pass > first) {
       uint32_t rank = S.sel_rank[slot * (RADIX_PASSES + 1) + pass - 1], nr;
       uint64_t np;
       pick_digit(S.hist + (slot * RADIX_PASSES + pass - 1) * 256, pass - 1, prefix, rank, &np, &nr);
@@ -833,10 +742,22 @@ __global__ void k_lg_hist(Level L, LargeScratch S, int pass) {
   __syncthreads();
   const uint64_t prefix = s_prefix;
   const int shift = 56 - 8 * pass;
+  const uint32_t lane = threadIdx.x & 31;
   KD_FOR_CHUNKS(len) {
-    for (uint32_t i = r0 + threadIdx.x; i < min(len, r0 + LG_CHUNK); i += LG_THREADS) {
-      uint64_t k = S.keys[static_cast<uint64_t>(start) + i];
-      if (pass == 0 || ((k ^ prefix) >> (shift + 8)) == 0) atomicAdd(&sh[(k >> shift) & 255], 1u);
+    const uint32_t end = min(len, r0 + LG_CHUNK);
+    for (uint32_t base = r0; base < end; base += LG_THREADS) {  // uniform: whole warps count together
+      const uint32_t i = base + threadIdx.x;
+      bool in = false;
+      uint32_t digit = 256 + lane;  // distinct per lane when not counted
+      if (i < end) {
+        const uint64_t k = S.keys[static_cast<uint64_t>(start) + i];
+        in = pass == 0 || ((k ^ prefix) >> (shift + 8)) == 0;
+        if (in) digit = static_cast<uint32_t>(k >> shift) & 255u;
+      }
+      // one shared atomic per distinct digit of the warp (uniform data puts
+      // most keys of a pass in a few bins)
+      const uint32_t same = __match_any_sync(0xffffffffu, digit);
+      if (in && lane == static_cast<uint32_t>(__ffs(same) - 1)) atomicAdd(&sh[digit], __popc(same));
     }
   }
   __syncthreads();
@@ -855,10 +776,11 @@ __global__ void k_lg_count_lt(Level L, LargeScratch S) {
   if (blockIdx.y * LG_CHUNK >= len) return;
   if (threadIdx.x == 0) {
     const int p = RADIX_PASSES - 1;
-    uint64_t np;
+    uint64_t np = S.sel_prefix[slot * (RADIX_PASSES + 1) + RADIX_PASSES];  // every key equal
     uint32_t nr;
-    pick_digit(S.hist + (slot * RADIX_PASSES + p) * 256, p, S.sel_prefix[slot * (RADIX_PASSES + 1) + p],
-               S.sel_rank[slot * (RADIX_PASSES + 1) + p], &np, &nr);
+    if (S.seg_first[slot] < static_cast<uint32_t>(RADIX_PASSES))
+      pick_digit(S.hist + (slot * RADIX_PASSES + p) * 256, p, S.sel_prefix[slot * (RADIX_PASSES + 1) + p],
+                 S.sel_rank[slot * (RADIX_PASSES + 1) + p], &np, &nr);
     s_pivot = np;
     if (blockIdx.y == 0) S.seg_pivot[slot] = np;
   }
@@ -1308,6 +1230,7 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
       X.lg.seg_lt = c.take<uint32_t>(large_slots);
       X.lg.chunk_cnt = c.take<uint32_t>(large_slots * static_cast<uint64_t>(max_chunks));
       X.lg.seg_mis = c.take<uint32_t>(large_slots);
+      X.lg.seg_first = c.take<uint32_t>(large_slots);
     }
   };
   PoolBlock tree_block, scratch_block;

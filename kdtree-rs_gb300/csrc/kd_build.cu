@@ -306,6 +306,7 @@ struct SubShared {
   uint64_t krow[SMALL_MAX];   // key of each local row on its segment's split dimension
   uint16_t perm[SMALL_MAX];   // position -> local row
   uint16_t plist[SMALL_MAX];  // misplaced positions (relative to their segment), by rank
+  uint16_t moved[SMALL_MAX];  // the partition's moves, staged
 };
 
 struct SubSeg {
@@ -465,6 +466,7 @@ __device__ void sub_split(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2
     uint64_t lo = KEY_MAX, hi = 0;
 #pragma unroll
     for (int t = 0; t < T; ++t) {
+      if (t >= static_cast<int>(per)) break;  // group-uniform
       if (t < static_cast<int>(nown)) {
         const double v = A.din[(row0 + S.perm[g.pos + b0 + t]) * d + dj];
         *bad |= !isfinite(v);
@@ -498,6 +500,7 @@ __device__ void sub_split(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2
 #pragma unroll
   for (int t = 0; t < T; ++t) {
     key[t] = 0;
+    if (t >= static_cast<int>(per)) continue;
     if (t < static_cast<int>(nown)) {
       const uint32_t lr = S.perm[g.pos + b0 + t];
       key[t] = total_key(A.din[(row0 + lr) * d + dim]);
@@ -506,14 +509,29 @@ __device__ void sub_split(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2
   }
   // pivot = the mid-th smallest key under total order (select_nth_unstable_by)
   uint64_t pivot = blo;
-  if (blo != bhi) {
+  if (blo != bhi && G == 1 && g.len <= 32) {
+    // one key a lane: its rank among the segment's keys, by shuffles
+    const uint32_t lane = threadIdx.x & 31;
+    const bool mine = lane < g.len;
+    uint32_t cl = 0, ce = 0;
+    for (uint32_t q = 0; q < g.len; ++q) {
+      const uint64_t kq = __shfl_sync(FULL, key[0], static_cast<int>(q));
+      cl += kq < key[0];
+      ce += kq == key[0];
+    }
+    const uint32_t at = __ballot_sync(FULL, mine && cl <= mid && mid < cl + ce);  // those lanes agree
+    pivot = __shfl_sync(FULL, key[0], __ffs(at) - 1);
+  } else if (blo != bhi) {
     const int hb = 63 - __clzll(static_cast<long long>(blo ^ bhi));
     uint64_t prefix = hb == 63 ? 0 : (blo >> (hb + 1)) << (hb + 1);
     uint32_t rank = mid;
     for (int b = hb; b >= 0; --b) {
       uint32_t c0 = 0;
 #pragma unroll
-      for (int t = 0; t < T; ++t) c0 += t < static_cast<int>(nown) && ((key[t] ^ prefix) >> b) == 0;
+      for (int t = 0; t < T; ++t) {
+        if (t >= static_cast<int>(per)) break;
+        c0 += t < static_cast<int>(nown) && ((key[t] ^ prefix) >> b) == 0;
+      }
       c0 = group_add<G>(c0, red, gid);
       if (rank >= c0) {  // every thread of the group decides alike
         rank -= c0;
@@ -526,12 +544,16 @@ __device__ void sub_split(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2
   // lt = #{key < pivot} under f64 '<' (build.rs:209)
   uint32_t my_lt = 0;
 #pragma unroll
-  for (int t = 0; t < T; ++t) my_lt += t < static_cast<int>(nown) && canon(key[t]) < pc;
+  for (int t = 0; t < T; ++t) {
+    if (t >= static_cast<int>(per)) break;
+    my_lt += t < static_cast<int>(nown) && canon(key[t]) < pc;
+  }
   const uint32_t lt = group_add<G>(my_lt, red, gid);
   // misplaced positions: key >= pivot in [0, lt), key < pivot in [lt, len)
   uint32_t cnt = 0;
 #pragma unroll
   for (int t = 0; t < T; ++t) {
+    if (t >= static_cast<int>(per)) break;
     const bool below = canon(key[t]) < pc;
     cnt += t < static_cast<int>(nown) && ((b0 + t < lt) ? !below : below);
   }
@@ -539,23 +561,20 @@ __device__ void sub_split(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2
   uint32_t r = group_excl_scan<G>(cnt, &n2, red, gid);
 #pragma unroll
   for (int t = 0; t < T; ++t) {
+    if (t >= static_cast<int>(per)) break;
     const bool below = canon(key[t]) < pc;
     if (t < static_cast<int>(nown) && ((b0 + t < lt) ? !below : below))
       S.plist[g.pos + r++] = static_cast<uint16_t>(b0 + t);
   }
   group_sync<G>(gid);
   // swap R[i] <-> L[n-1-i]: the row at plist[n2-1-j] lands on plist[j]
-  uint16_t moved[T];
-#pragma unroll
-  for (int t = 0; t < T; ++t) {
-    const uint32_t jj = tg + 32u * G * t;
-    moved[t] = jj < n2 ? S.perm[g.pos + S.plist[g.pos + n2 - 1 - jj]] : 0;
-  }
+  // (through `moved`, so that no read sees a written place)
+  for (uint32_t jj = tg; jj < n2; jj += 32u * G)
+    S.moved[g.pos + S.plist[g.pos + jj]] = S.perm[g.pos + S.plist[g.pos + n2 - 1 - jj]];
   group_sync<G>(gid);
-#pragma unroll
-  for (int t = 0; t < T; ++t) {
-    const uint32_t jj = tg + 32u * G * t;
-    if (jj < n2) S.perm[g.pos + S.plist[g.pos + jj]] = moved[t];
+  for (uint32_t jj = tg; jj < n2; jj += 32u * G) {
+    const uint32_t at = g.pos + S.plist[g.pos + jj];
+    S.perm[at] = S.moved[at];
   }
   group_sync<G>(gid);
   if (mid > lt && tg == 0) {

@@ -764,12 +764,19 @@ __global__ void k_lg_hist(Level L, LargeScratch S, int pass) {
   const uint32_t lane = threadIdx.x & 31;
   KD_FOR_CHUNKS(len) {
     const uint32_t end = min(len, r0 + LG_CHUNK);
-    for (uint32_t base = r0; base < end; base += LG_THREADS) {  // uniform: whole warps count together
-      const uint32_t i = base + threadIdx.x;
+    uint64_t kk[LG_ITEMS];  // the thread's keys, loaded together
+#pragma unroll
+    for (int t = 0; t < LG_ITEMS; ++t) {
+      const uint32_t i = r0 + threadIdx.x + t * LG_THREADS;
+      kk[t] = i < end ? S.keys[static_cast<uint64_t>(start) + i] : 0;
+    }
+#pragma unroll
+    for (int t = 0; t < LG_ITEMS; ++t) {  // uniform: whole warps count together
+      const uint32_t i = r0 + threadIdx.x + t * LG_THREADS;
       bool in = false;
       uint32_t digit = 256 + lane;  // distinct per lane when not counted
       if (i < end) {
-        const uint64_t k = S.keys[static_cast<uint64_t>(start) + i];
+        const uint64_t k = kk[t];
         in = pass == 0 || ((k ^ prefix) >> (shift + 8)) == 0;
         if (in) digit = static_cast<uint32_t>(k >> shift) & 255u;
       }
@@ -807,8 +814,15 @@ __global__ void k_lg_count_lt(Level L, LargeScratch S) {
   const uint64_t pc = canon(s_pivot);
   uint32_t c = 0;
   KD_FOR_CHUNKS(len) {
-    for (uint32_t i = r0 + threadIdx.x; i < min(len, r0 + LG_CHUNK); i += LG_THREADS)
-      c += canon(S.keys[static_cast<uint64_t>(start) + i]) < pc;
+    const uint32_t end = min(len, r0 + LG_CHUNK);
+    uint64_t kk[LG_ITEMS];
+#pragma unroll
+    for (int t = 0; t < LG_ITEMS; ++t) {
+      const uint32_t i = r0 + threadIdx.x + t * LG_THREADS;
+      kk[t] = i < end ? S.keys[static_cast<uint64_t>(start) + i] : KEY_MAX;
+    }
+#pragma unroll
+    for (int t = 0; t < LG_ITEMS; ++t) c += r0 + threadIdx.x + t * LG_THREADS < end && canon(kk[t]) < pc;
   }
   uint32_t total = block_sum<LG_THREADS>(c, sh_warp);
   if (threadIdx.x == 0 && total) atomicAdd(&S.seg_lt[slot], total);
@@ -828,8 +842,18 @@ __global__ void k_lg_flagcount(Level L, LargeScratch S, uint32_t n_chunks) {
   const uint32_t lt = S.seg_lt[slot];
   KD_FOR_CHUNKS(len) {
     uint32_t c = 0;
-    for (uint32_t i = r0 + threadIdx.x; i < min(len, r0 + LG_CHUNK); i += LG_THREADS)
-      c += misplaced(S.keys[static_cast<uint64_t>(start) + i], pc, i, lt);
+    const uint32_t end = min(len, r0 + LG_CHUNK);
+    uint64_t kk[LG_ITEMS];
+#pragma unroll
+    for (int t = 0; t < LG_ITEMS; ++t) {
+      const uint32_t i = r0 + threadIdx.x + t * LG_THREADS;
+      kk[t] = i < end ? S.keys[static_cast<uint64_t>(start) + i] : 0;
+    }
+#pragma unroll
+    for (int t = 0; t < LG_ITEMS; ++t) {
+      const uint32_t i = r0 + threadIdx.x + t * LG_THREADS;
+      c += i < end && misplaced(kk[t], pc, i, lt);
+    }
     uint32_t total = block_sum<LG_THREADS>(c, sh_warp);
     if (threadIdx.x == 0) S.chunk_cnt[slot * n_chunks + chunk] = total;
   }

@@ -311,6 +311,7 @@ struct SubShared {
 
 struct SubSeg {
   uint32_t node, pos, len;  // pos: first position within the subtree
+  bool ok;                  // false: an ancestor is a leaf (no such segment)
 };
 
 __device__ __forceinline__ uint64_t warp_min64(uint64_t v) {
@@ -330,13 +331,13 @@ __device__ __forceinline__ uint64_t warp_max64(uint64_t v) {
   return v;
 }
 
-// Segment (depth j, index s) of the subtree rooted at (node0, length l0), or
-// false when an ancestor of it is a leaf.
-__device__ __forceinline__ bool sub_segment(const uint32_t* lo_len, const uint32_t (*cn)[2], uint32_t node0,
-                                            uint32_t l0, uint32_t leafsize, int j, uint32_t s, SubSeg* g) {
+// Segment (depth j, index s) of the subtree rooted at (node0, length l0);
+// ok = false when an ancestor of it is a leaf.
+__device__ __forceinline__ SubSeg sub_segment(const uint32_t* lo_len, const uint32_t (*cn)[2], uint32_t node0,
+                                              uint32_t l0, uint32_t leafsize, int j, uint32_t s) {
   uint32_t node = node0, pos = 0, len = l0;
   for (int i = 0; i < j; ++i) {
-    if (len <= leafsize) return false;
+    if (len <= leafsize) return SubSeg{0, 0, 0, false};
     const uint32_t mid = len / 2;
     if (!((s >> (j - 1 - i)) & 1u)) {
       node += 1;
@@ -347,8 +348,7 @@ __device__ __forceinline__ bool sub_segment(const uint32_t* lo_len, const uint32
       len -= mid;
     }
   }
-  *g = SubSeg{node, pos, len};
-  return true;
+  return SubSeg{node, pos, len, true};
 }
 
 // The inner node's record (expand_inner without the next level's segments).
@@ -452,8 +452,10 @@ __device__ __forceinline__ uint32_t group_excl_scan(uint32_t v, uint32_t* total,
 // order.  The pivot is found bit by bit (a group sum per bit) from the first
 // bit where the segment's smallest and largest keys differ.
 template <int G>
-__device__ void sub_split(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2], const uint32_t* lo_len, int j,
-                          const SubSeg& g, uint64_t row0, bool* bad, SubReduce* red, uint32_t gid) {
+__device__ __forceinline__ bool sub_split(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2],
+                                          const uint32_t* lo_len, int j, const SubSeg g, uint64_t row0,
+                                          SubReduce* red, uint32_t gid) {
+  bool bad = false;  // a non-finite coordinate among the segment's rows
   constexpr int T = WARP_SEG / 32;  // positions a thread owns, at most
   const uint32_t tg = (threadIdx.x & 31) + 32u * ((threadIdx.x >> 5) % G);  // thread within the group
   const uint64_t d = A.d;
@@ -469,7 +471,7 @@ __device__ void sub_split(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2
       if (t >= static_cast<int>(per)) break;  // group-uniform
       if (t < static_cast<int>(nown)) {
         const double v = A.din[(row0 + S.perm[g.pos + b0 + t]) * d + dj];
-        *bad |= !isfinite(v);
+        bad |= !isfinite(v);
         const uint64_t k = total_key(v);
         lo = k < lo ? k : lo;
         hi = k > hi ? k : hi;
@@ -493,7 +495,7 @@ __device__ void sub_split(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2
       write_leaf(A.nodes, g.node, static_cast<uint32_t>(row0) + g.pos, g.len);
       A.node_len[g.node] = g.len;
     }
-    return;
+    return bad;
   }
   const uint32_t dim = best_dim, mid = g.len / 2;
   uint64_t key[T];
@@ -592,18 +594,22 @@ __device__ void sub_split(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2
   }
   if (tg == 0) sub_record(A, cn, lo_len, j, g, dim, pivot);
   group_sync<G>(gid);
+  return bad;
 }
 
 // Every segment of depth j, split by groups of G warps.
 template <int G>
-__device__ void sub_depth(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2], const uint32_t* lo_len, int j,
-                          uint32_t node0, uint32_t l0, uint64_t row0, bool* bad, SubReduce* red) {
+__device__ __forceinline__ bool sub_depth(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2],
+                                          const uint32_t* lo_len, int j, uint32_t node0, uint32_t l0, uint64_t row0,
+                                          SubReduce* red) {
   const uint32_t gid = (threadIdx.x >> 5) / G;
+  bool bad = false;
   for (uint32_t sidx = gid; sidx < (1u << j); sidx += SUB_WARPS / G) {
-    SubSeg g;
-    if (!sub_segment(lo_len, cn, node0, l0, A.leafsize, j, sidx, &g)) continue;  // uniform per group
-    sub_split<G>(A, S, cn, lo_len, j, g, row0, bad, red, gid);
+    const SubSeg g = sub_segment(lo_len, cn, node0, l0, A.leafsize, j, sidx);
+    if (!g.ok) continue;  // uniform per group
+    bad |= sub_split<G>(A, S, cn, lo_len, j, g, row0, red, gid);
   }
+  return bad;
 }
 
 __global__ void __launch_bounds__(SUB_THREADS) k_small_subtree(SubArgs A) {
@@ -638,19 +644,25 @@ __global__ void __launch_bounds__(SUB_THREADS) k_small_subtree(SubArgs A) {
     // at least ceil(len / 512) warps, so a thread owns at most 16 positions
     const uint32_t hi_len = (l0 + (1u << j) - 1) >> j;
     const uint32_t need = (hi_len + WARP_SEG - 1) / WARP_SEG;
-    if (need > 8) sub_depth<16>(A, S, cn, lo_len, j, node0, l0, row0, &bad, &red);
-    else if (need > 4) sub_depth<8>(A, S, cn, lo_len, j, node0, l0, row0, &bad, &red);
-    else if (need > 2) sub_depth<4>(A, S, cn, lo_len, j, node0, l0, row0, &bad, &red);
-    else if (need > 1) sub_depth<2>(A, S, cn, lo_len, j, node0, l0, row0, &bad, &red);
-    else sub_depth<1>(A, S, cn, lo_len, j, node0, l0, row0, &bad, &red);
+    if (need > 8) bad |= sub_depth<16>(A, S, cn, lo_len, j, node0, l0, row0, &red);
+    else if (need > 4) bad |= sub_depth<8>(A, S, cn, lo_len, j, node0, l0, row0, &red);
+    else if (need > 2) bad |= sub_depth<4>(A, S, cn, lo_len, j, node0, l0, row0, &red);
+    else if (need > 1) bad |= sub_depth<2>(A, S, cn, lo_len, j, node0, l0, row0, &red);
+    else bad |= sub_depth<1>(A, S, cn, lo_len, j, node0, l0, row0, &red);
     __syncthreads();
   }
   if (A.check_finite && bad) atomicOr(A.status, 1u);
   // the subtree's rows, once, in their final order
-  for (uint64_t f = threadIdx.x; f < static_cast<uint64_t>(l0) * d; f += SUB_THREADS) {
-    const uint32_t p = static_cast<uint32_t>(f / d);
-    const uint32_t jd = static_cast<uint32_t>(f - static_cast<uint64_t>(p) * d);
-    A.dout[static_cast<uint64_t>(row0) * d + f] = A.din[(static_cast<uint64_t>(row0) + S.perm[p]) * d + jd];
+  if (static_cast<uint64_t>(l0) * d < (1ull << 32)) {
+    const uint32_t dd = static_cast<uint32_t>(d);
+    for (uint32_t f = threadIdx.x; f < l0 * dd; f += SUB_THREADS) {
+      const uint32_t p = f / dd, jd = f - p * dd;
+      A.dout[static_cast<uint64_t>(row0) * d + f] = A.din[(static_cast<uint64_t>(row0) + S.perm[p]) * d + jd];
+    }
+  } else {  // very wide rows: a warp a row
+    for (uint32_t p = threadIdx.x >> 5; p < l0; p += SUB_WARPS)
+      for (uint64_t jd = threadIdx.x & 31; jd < d; jd += 32)
+        A.dout[(static_cast<uint64_t>(row0) + p) * d + jd] = A.din[(static_cast<uint64_t>(row0) + S.perm[p]) * d + jd];
   }
   for (uint32_t p = threadIdx.x; p < l0; p += SUB_THREADS) A.iout[row0 + p] = A.iin[row0 + S.perm[p]];
 }
@@ -696,23 +708,35 @@ __global__ void k_lg_prepare(Level L, LargeScratch S) {
   S.seg_lt[slot] = 0;
 }
 
-// Pick the digit bucket of pass `pass` holding the wanted rank; returns the
-// state after that pass.  Every CTA of the segment computes the same answer.
-__device__ void pick_digit(const uint32_t* hist, int pass, uint64_t prefix_in, uint32_t rank_in,
-                           uint64_t* prefix_out, uint32_t* rank_out) {
-  uint32_t acc = 0;
-  const int shift = 56 - 8 * pass;
-  for (int b = 0; b < 256; ++b) {
-    uint32_t c = hist[b];
-    if (rank_in < acc + c) {
-      *prefix_out = prefix_in | (static_cast<uint64_t>(b) << shift);
-      *rank_out = rank_in - acc;
-      return;
-    }
-    acc += c;
+// Pick the digit bucket of pass `pass` holding the wanted rank; returns (to
+// every thread of the block) the state after that pass.  Every CTA of the
+// segment computes the same answer.  The block's LG_THREADS = 256 threads load
+// one bin each and scan them; `scratch` holds LG_THREADS / 32 + 3 words.
+static_assert(LG_THREADS == 256, "one bin per thread");
+__device__ void pick_digit_block(const uint32_t* hist, int pass, uint64_t prefix_in, uint32_t rank_in,
+                                 uint64_t* prefix_out, uint32_t* rank_out, uint32_t* scratch) {
+  const uint32_t b = threadIdx.x;
+  const uint32_t c = hist[b];
+  uint32_t total;
+  const uint32_t excl = block_excl_scan<LG_THREADS>(c, &total, scratch);
+  uint32_t* found = scratch + LG_THREADS / 32;  // [bin, rank in it, flag]
+  if (b == 0) found[2] = 0;
+  __syncthreads();
+  if (excl <= rank_in && rank_in < excl + c) {  // exactly one bin
+    found[0] = b;
+    found[1] = rank_in - excl;
+    found[2] = 1;
   }
-  *prefix_out = prefix_in;
-  *rank_out = rank_in;
+  __syncthreads();
+  const int shift = 56 - 8 * pass;
+  if (found[2]) {
+    *prefix_out = prefix_in | (static_cast<uint64_t>(found[0]) << shift);
+    *rank_out = found[1];
+  } else {
+    *prefix_out = prefix_in;
+    *rank_out = rank_in;
+  }
+  __syncthreads();
 }
 
 // Chunks of one segment: CTA (slot, y) handles chunks y, y + gridDim.y, ...
@@ -737,6 +761,7 @@ __global__ void k_lg_keys(Level L, LargeScratch S) {
 __global__ void k_lg_hist(Level L, LargeScratch S, int pass) {
   __shared__ uint32_t sh[256];
   __shared__ uint64_t s_prefix;
+  __shared__ uint32_t pick_scratch[LG_THREADS / 32 + 3];
   const uint64_t slot = blockIdx.x;
   if (S.seg_dim[slot] == NONE) return;
   const int first = static_cast<int>(S.seg_first[slot]);
@@ -744,19 +769,21 @@ __global__ void k_lg_hist(Level L, LargeScratch S, int pass) {
   const uint32_t start = L.seg_start[slot], len = L.seg_len[slot];
   if (blockIdx.y * LG_CHUNK >= len) return;
   for (int b = threadIdx.x; b < 256; b += LG_THREADS) sh[b] = 0;
-  if (threadIdx.x == 0) {
-    uint64_t prefix = S.sel_prefix[slot * (RADIX_PASSES + 1) + (pass > first ? pass - 1 : pass)];
-    if (pass > first) {
-      uint32_t rank = S.sel_rank[slot * (RADIX_PASSES + 1) + pass - 1], nr;
-      uint64_t np;
-      pick_digit(S.hist + (slot * RADIX_PASSES + pass - 1) * 256, pass - 1, prefix, rank, &np, &nr);
-      prefix = np;
-      if (blockIdx.y == 0) {  // publish the state for the next pass (all CTAs agree)
+  if (pass > first) {  // replay the previous pass's pick (every CTA of the segment agrees)
+    uint64_t np;
+    uint32_t nr;
+    pick_digit_block(S.hist + (slot * RADIX_PASSES + pass - 1) * 256, pass - 1,
+                     S.sel_prefix[slot * (RADIX_PASSES + 1) + pass - 1],
+                     S.sel_rank[slot * (RADIX_PASSES + 1) + pass - 1], &np, &nr, pick_scratch);
+    if (threadIdx.x == 0) {
+      s_prefix = np;
+      if (blockIdx.y == 0) {  // publish the state for the next pass
         S.sel_prefix[slot * (RADIX_PASSES + 1) + pass] = np;
         S.sel_rank[slot * (RADIX_PASSES + 1) + pass] = nr;
       }
     }
-    s_prefix = prefix;
+  } else if (threadIdx.x == 0) {
+    s_prefix = S.sel_prefix[slot * (RADIX_PASSES + 1) + pass];
   }
   __syncthreads();
   const uint64_t prefix = s_prefix;
@@ -796,19 +823,22 @@ __global__ void k_lg_hist(Level L, LargeScratch S, int pass) {
 __global__ void k_lg_count_lt(Level L, LargeScratch S) {
   __shared__ uint32_t sh_warp[LG_THREADS / 32];
   __shared__ uint64_t s_pivot;
+  __shared__ uint32_t pick_scratch[LG_THREADS / 32 + 3];
   const uint64_t slot = blockIdx.x;
   if (S.seg_dim[slot] == NONE) return;
   const uint32_t start = L.seg_start[slot], len = L.seg_len[slot];
   if (blockIdx.y * LG_CHUNK >= len) return;
-  if (threadIdx.x == 0) {
+  {
     const int p = RADIX_PASSES - 1;
     uint64_t np = S.sel_prefix[slot * (RADIX_PASSES + 1) + RADIX_PASSES];  // every key equal
     uint32_t nr;
     if (S.seg_first[slot] < static_cast<uint32_t>(RADIX_PASSES))
-      pick_digit(S.hist + (slot * RADIX_PASSES + p) * 256, p, S.sel_prefix[slot * (RADIX_PASSES + 1) + p],
-                 S.sel_rank[slot * (RADIX_PASSES + 1) + p], &np, &nr);
-    s_pivot = np;
-    if (blockIdx.y == 0) S.seg_pivot[slot] = np;
+      pick_digit_block(S.hist + (slot * RADIX_PASSES + p) * 256, p, S.sel_prefix[slot * (RADIX_PASSES + 1) + p],
+                       S.sel_rank[slot * (RADIX_PASSES + 1) + p], &np, &nr, pick_scratch);
+    if (threadIdx.x == 0) {
+      s_pivot = np;
+      if (blockIdx.y == 0) S.seg_pivot[slot] = np;
+    }
   }
   __syncthreads();
   const uint64_t pc = canon(s_pivot);

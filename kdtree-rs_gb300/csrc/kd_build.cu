@@ -417,6 +417,20 @@ __device__ __forceinline__ void group_minmax(uint64_t* lo, uint64_t* hi, SubRedu
   *lo = a;
   *hi = b;
 }
+template <int G>
+__device__ __forceinline__ uint64_t group_max64(uint64_t v, SubReduce* red, uint32_t gid) {
+  v = warp_max64(v);
+  if constexpr (G > 1) {
+    const uint32_t w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) red->hi[w] = v;
+    group_sync<G>(gid);
+    v = red->hi[gid * G];
+#pragma unroll
+    for (int i = 1; i < G; ++i) v = red->hi[gid * G + i] > v ? red->hi[gid * G + i] : v;
+    group_sync<G>(gid);
+  }
+  return v;
+}
 // Exclusive prefix of v over the group's threads in order; *total: the sum.
 template <int G>
 __device__ __forceinline__ uint32_t group_excl_scan(uint32_t v, uint32_t* total, SubReduce* red, uint32_t gid) {
@@ -450,12 +464,12 @@ __device__ __forceinline__ uint32_t group_excl_scan(uint32_t v, uint32_t* total,
 // One segment split by a group of G warps (g.len <= 512 G): each thread owns
 // a contiguous run of at most 16 positions, so misplaced ranks ascend in thread
 // order.  The pivot is found bit by bit (a group sum per bit) from the first
-// bit where the segment's smallest and largest keys differ.
+// bit where the segment's smallest and largest keys differ, until one
+// candidate key is left (distinct keys: about log2(len) bits).
 template <int G>
-__device__ __forceinline__ bool sub_split(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2],
+__device__ __forceinline__ void sub_split(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2],
                                           const uint32_t* lo_len, int j, const SubSeg g, uint64_t row0,
                                           SubReduce* red, uint32_t gid) {
-  bool bad = false;  // a non-finite coordinate among the segment's rows
   constexpr int T = WARP_SEG / 32;  // positions a thread owns, at most
   const uint32_t tg = (threadIdx.x & 31) + 32u * ((threadIdx.x >> 5) % G);  // thread within the group
   const uint64_t d = A.d;
@@ -470,9 +484,7 @@ __device__ __forceinline__ bool sub_split(const SubArgs& A, SubShared& S, const 
     for (int t = 0; t < T; ++t) {
       if (t >= static_cast<int>(per)) break;  // group-uniform
       if (t < static_cast<int>(nown)) {
-        const double v = A.din[(row0 + S.perm[g.pos + b0 + t]) * d + dj];
-        bad |= !isfinite(v);
-        const uint64_t k = total_key(v);
+        const uint64_t k = total_key(A.din[(row0 + S.perm[g.pos + b0 + t]) * d + dj]);
         lo = k < lo ? k : lo;
         hi = k > hi ? k : hi;
       }
@@ -495,7 +507,7 @@ __device__ __forceinline__ bool sub_split(const SubArgs& A, SubShared& S, const 
       write_leaf(A.nodes, g.node, static_cast<uint32_t>(row0) + g.pos, g.len);
       A.node_len[g.node] = g.len;
     }
-    return bad;
+    return;
   }
   const uint32_t dim = best_dim, mid = g.len / 2;
   uint64_t key[T];
@@ -526,8 +538,9 @@ __device__ __forceinline__ bool sub_split(const SubArgs& A, SubShared& S, const 
   } else if (blo != bhi) {
     const int hb = 63 - __clzll(static_cast<long long>(blo ^ bhi));
     uint64_t prefix = hb == 63 ? 0 : (blo >> (hb + 1)) << (hb + 1);
-    uint32_t rank = mid;
-    for (int b = hb; b >= 0; --b) {
+    uint32_t rank = mid, n_cand = g.len;  // keys matching prefix on the bits above b
+    int b = hb;
+    for (; b >= 0; --b) {
       uint32_t c0 = 0;
 #pragma unroll
       for (int t = 0; t < T; ++t) {
@@ -538,9 +551,23 @@ __device__ __forceinline__ bool sub_split(const SubArgs& A, SubShared& S, const 
       if (rank >= c0) {  // every thread of the group decides alike
         rank -= c0;
         prefix |= 1ull << b;
+        n_cand -= c0;
+      } else {
+        n_cand = c0;
       }
+      if (n_cand == 1) break;  // that key is the pivot
     }
-    pivot = prefix;
+    if (b > 0 && n_cand == 1) {  // the one key matching prefix on bits b and above
+      uint64_t found = 0;
+#pragma unroll
+      for (int t = 0; t < T; ++t) {
+        if (t >= static_cast<int>(per)) break;
+        if (t < static_cast<int>(nown) && ((key[t] ^ prefix) >> b) == 0) found = key[t];
+      }
+      pivot = group_max64<G>(found, red, gid);
+    } else {
+      pivot = prefix;  // every bit decided
+    }
   }
   const uint64_t pc = canon(pivot);
   // lt = #{key < pivot} under f64 '<' (build.rs:209)
@@ -594,22 +621,19 @@ __device__ __forceinline__ bool sub_split(const SubArgs& A, SubShared& S, const 
   }
   if (tg == 0) sub_record(A, cn, lo_len, j, g, dim, pivot);
   group_sync<G>(gid);
-  return bad;
 }
 
 // Every segment of depth j, split by groups of G warps.
 template <int G>
-__device__ __forceinline__ bool sub_depth(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2],
+__device__ __forceinline__ void sub_depth(const SubArgs& A, SubShared& S, const uint32_t (*cn)[2],
                                           const uint32_t* lo_len, int j, uint32_t node0, uint32_t l0, uint64_t row0,
                                           SubReduce* red) {
   const uint32_t gid = (threadIdx.x >> 5) / G;
-  bool bad = false;
   for (uint32_t sidx = gid; sidx < (1u << j); sidx += SUB_WARPS / G) {
     const SubSeg g = sub_segment(lo_len, cn, node0, l0, A.leafsize, j, sidx);
     if (!g.ok) continue;  // uniform per group
-    bad |= sub_split<G>(A, S, cn, lo_len, j, g, row0, red, gid);
+    sub_split<G>(A, S, cn, lo_len, j, g, row0, red, gid);
   }
-  return bad;
 }
 
 __global__ void __launch_bounds__(SUB_THREADS) k_small_subtree(SubArgs A) {
@@ -644,26 +668,33 @@ __global__ void __launch_bounds__(SUB_THREADS) k_small_subtree(SubArgs A) {
     // at least ceil(len / 512) warps, so a thread owns at most 16 positions
     const uint32_t hi_len = (l0 + (1u << j) - 1) >> j;
     const uint32_t need = (hi_len + WARP_SEG - 1) / WARP_SEG;
-    if (need > 8) bad |= sub_depth<16>(A, S, cn, lo_len, j, node0, l0, row0, &red);
-    else if (need > 4) bad |= sub_depth<8>(A, S, cn, lo_len, j, node0, l0, row0, &red);
-    else if (need > 2) bad |= sub_depth<4>(A, S, cn, lo_len, j, node0, l0, row0, &red);
-    else if (need > 1) bad |= sub_depth<2>(A, S, cn, lo_len, j, node0, l0, row0, &red);
-    else bad |= sub_depth<1>(A, S, cn, lo_len, j, node0, l0, row0, &red);
+    if (need > 8) sub_depth<16>(A, S, cn, lo_len, j, node0, l0, row0, &red);
+    else if (need > 4) sub_depth<8>(A, S, cn, lo_len, j, node0, l0, row0, &red);
+    else if (need > 2) sub_depth<4>(A, S, cn, lo_len, j, node0, l0, row0, &red);
+    else if (need > 1) sub_depth<2>(A, S, cn, lo_len, j, node0, l0, row0, &red);
+    else sub_depth<1>(A, S, cn, lo_len, j, node0, l0, row0, &red);
     __syncthreads();
   }
-  if (A.check_finite && bad) atomicOr(A.status, 1u);
-  // the subtree's rows, once, in their final order
+  // the subtree's rows, once, in their final order (and, at level 0, the
+  // finiteness check: an exponent field of all ones is inf or NaN)
+  const double* din = A.din;
+  auto move = [&](uint64_t to, uint64_t from) {
+    const double v = din[from];
+    bad |= (static_cast<uint64_t>(__double_as_longlong(v)) & 0x7ff0000000000000ull) == 0x7ff0000000000000ull;
+    A.dout[to] = v;
+  };
   if (static_cast<uint64_t>(l0) * d < (1ull << 32)) {
     const uint32_t dd = static_cast<uint32_t>(d);
     for (uint32_t f = threadIdx.x; f < l0 * dd; f += SUB_THREADS) {
       const uint32_t p = f / dd, jd = f - p * dd;
-      A.dout[static_cast<uint64_t>(row0) * d + f] = A.din[(static_cast<uint64_t>(row0) + S.perm[p]) * d + jd];
+      move(static_cast<uint64_t>(row0) * d + f, (static_cast<uint64_t>(row0) + S.perm[p]) * d + jd);
     }
   } else {  // very wide rows: a warp a row
     for (uint32_t p = threadIdx.x >> 5; p < l0; p += SUB_WARPS)
       for (uint64_t jd = threadIdx.x & 31; jd < d; jd += 32)
-        A.dout[(static_cast<uint64_t>(row0) + p) * d + jd] = A.din[(static_cast<uint64_t>(row0) + S.perm[p]) * d + jd];
+        move((static_cast<uint64_t>(row0) + p) * d + jd, (static_cast<uint64_t>(row0) + S.perm[p]) * d + jd);
   }
+  if (A.check_finite && bad) atomicOr(A.status, 1u);
   for (uint32_t p = threadIdx.x; p < l0; p += SUB_THREADS) A.iout[row0 + p] = A.iin[row0 + S.perm[p]];
 }
 

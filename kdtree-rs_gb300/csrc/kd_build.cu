@@ -33,6 +33,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <utility>
 #include <vector>
 
 #include "kd_internal.hpp"
@@ -40,6 +41,28 @@
 namespace kd {
 
 namespace {
+
+// The build is a chain of dependent launches on one stream.  Each is launched
+// with programmatic stream serialisation, so the next kernel's launch is
+// processed while its predecessor runs; every kernel first waits for the
+// grids it depends on (griddepcontrol.wait: all of their memory operations
+// are then visible), so the ordering is that of plain stream launches.
+__device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... P, typename... A>
+cudaError_t chain(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, A&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+}
 
 constexpr uint32_t HOLE = 0xffffffffu;
 constexpr uint32_t NONE = 0xffffffffu;
@@ -169,12 +192,14 @@ __device__ void close_leaf(const Level& L, uint64_t slot, uint32_t node, uint32_
 // registers.  Level 0 also checks finiteness (all_finite, kernel.rs:67-74).
 // ---------------------------------------------------------------------------
 __global__ void k_init_boxkeys(uint64_t* boxkeys, uint64_t n_nodes, uint64_t d) {
+  wait_prior_grid();
   uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
   uint64_t total = n_nodes * 2 * d;
   if (i < total) boxkeys[i] = ((i / d) & 1) ? 0ull : KEY_MAX;
 }
 
 __global__ void k_bbox(Level L, uint32_t chunk_rows, uint32_t n_chunks, int check_finite, uint32_t* status) {
+  wait_prior_grid();
   extern __shared__ uint64_t sbox[];  // [lo d | hi d]
   const uint64_t slot = blockIdx.x;
   const uint32_t node = L.seg_node[slot];
@@ -637,6 +662,7 @@ __device__ __forceinline__ void sub_depth(const SubArgs& A, SubShared& S, const 
 }
 
 __global__ void __launch_bounds__(SUB_THREADS) k_small_subtree(SubArgs A) {
+  wait_prior_grid();
   extern __shared__ __align__(16) unsigned char sub_smem[];
   SubShared& S = *reinterpret_cast<SubShared*>(sub_smem);
   __shared__ uint32_t lo_len[KD_MAX_DEPTH + 1];
@@ -718,6 +744,7 @@ struct LargeScratch {
 };
 
 __global__ void k_lg_prepare(Level L, LargeScratch S) {
+  wait_prior_grid();
   uint64_t slot = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
   if (slot >= L.n_slots) return;
   uint32_t node = L.seg_node[slot];
@@ -776,9 +803,12 @@ __device__ void pick_digit_block(const uint32_t* hist, int pass, uint64_t prefix
        chunk += gridDim.y, r0 = chunk * LG_CHUNK)
 
 __global__ void k_lg_keys(Level L, LargeScratch S) {
+  wait_prior_grid();
   const uint64_t slot = blockIdx.x;
   const uint32_t dim = S.seg_dim[slot];
   if (dim == NONE) return;
+  if (blockIdx.y == 0)  // the segment's histograms for this level's passes start empty
+    for (uint32_t b = threadIdx.x; b < RADIX_PASSES * 256; b += LG_THREADS) S.hist[slot * RADIX_PASSES * 256 + b] = 0;
   const uint32_t start = L.seg_start[slot], len = L.seg_len[slot];
   KD_FOR_CHUNKS(len) {
     for (uint32_t i = r0 + threadIdx.x; i < min(len, r0 + LG_CHUNK); i += LG_THREADS) {
@@ -790,6 +820,7 @@ __global__ void k_lg_keys(Level L, LargeScratch S) {
 
 // Histogram pass `pass`; first replays the pick of pass-1 from its histogram.
 __global__ void k_lg_hist(Level L, LargeScratch S, int pass) {
+  wait_prior_grid();
   __shared__ uint32_t sh[256];
   __shared__ uint64_t s_prefix;
   __shared__ uint32_t pick_scratch[LG_THREADS / 32 + 3];
@@ -852,6 +883,7 @@ __global__ void k_lg_hist(Level L, LargeScratch S, int pass) {
 
 // Final pick -> pivot; then lt = #{key < pivot}.
 __global__ void k_lg_count_lt(Level L, LargeScratch S) {
+  wait_prior_grid();
   __shared__ uint32_t sh_warp[LG_THREADS / 32];
   __shared__ uint64_t s_pivot;
   __shared__ uint32_t pick_scratch[LG_THREADS / 32 + 3];
@@ -895,6 +927,7 @@ __device__ __forceinline__ bool misplaced(uint64_t key, uint64_t pc, uint32_t i,
 }
 
 __global__ void k_lg_flagcount(Level L, LargeScratch S, uint32_t n_chunks) {
+  wait_prior_grid();
   __shared__ uint32_t sh_warp[LG_THREADS / 32];
   const uint64_t slot = blockIdx.x;
   if (S.seg_dim[slot] == NONE) return;
@@ -921,6 +954,7 @@ __global__ void k_lg_flagcount(Level L, LargeScratch S, uint32_t n_chunks) {
 }
 
 __global__ void k_lg_chunkscan(Level L, LargeScratch S, uint32_t n_chunks) {
+  wait_prior_grid();
   __shared__ uint32_t sh_warp[1024 / 32];
   __shared__ uint32_t s_run;
   const uint64_t slot = blockIdx.x;
@@ -943,6 +977,7 @@ __global__ void k_lg_chunkscan(Level L, LargeScratch S, uint32_t n_chunks) {
 }
 
 __global__ void k_lg_lists(Level L, LargeScratch S, uint32_t n_chunks) {
+  wait_prior_grid();
   __shared__ uint32_t sh_warp[LG_THREADS / 32];
   const uint64_t slot = blockIdx.x;
   if (S.seg_dim[slot] == NONE) return;
@@ -981,6 +1016,7 @@ __global__ void k_lg_lists(Level L, LargeScratch S, uint32_t n_chunks) {
 
 // Move rows to their post-swap positions; leaf segments copy through.
 __global__ void k_lg_move(Level L, LargeScratch S) {
+  wait_prior_grid();
   const uint64_t slot = blockIdx.x;
   const uint32_t node = L.seg_node[slot];
   if (node == HOLE) return;
@@ -1007,6 +1043,7 @@ __global__ void k_lg_move(Level L, LargeScratch S) {
 // segment, in place on the moved rows; only segments with mid > lt do work.
 constexpr int FIX_THREADS = 1024;
 __global__ void __launch_bounds__(FIX_THREADS) k_lg_fixup(Level L, LargeScratch S) {
+  wait_prior_grid();
   __shared__ uint32_t sh_warp[FIX_THREADS / 32];
   __shared__ uint32_t s_count, s_changed, s_stop;
   const uint64_t slot = blockIdx.x;
@@ -1090,6 +1127,7 @@ __global__ void __launch_bounds__(FIX_THREADS) k_lg_fixup(Level L, LargeScratch 
 }
 
 __global__ void k_lg_expand(Level L, LargeScratch S) {
+  wait_prior_grid();
   uint64_t slot = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
   if (slot >= L.n_slots) return;
   const uint32_t node = L.seg_node[slot];
@@ -1117,6 +1155,7 @@ __global__ void k_lg_expand(Level L, LargeScratch S) {
 
 // All-leaf level: record the leaves.
 __global__ void k_leaf_records(Level L) {
+  wait_prior_grid();
   uint64_t slot = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
   if (slot >= L.n_slots) return;
   const uint32_t node = L.seg_node[slot];
@@ -1128,6 +1167,7 @@ __global__ void k_leaf_records(Level L) {
 // order_by_box (src/build.rs:234-238, 248-252), after every box is known.
 __global__ void k_order_by_box(DNode* nodes, const uint64_t* boxkeys, const uint32_t* node_len,
                                uint64_t n_nodes, uint64_t d) {
+  wait_prior_grid();
   uint64_t id = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
   if (id >= n_nodes) return;
   DNode nd = nodes[id];
@@ -1149,22 +1189,26 @@ __global__ void k_order_by_box(DNode* nodes, const uint64_t* boxkeys, const uint
 }
 
 __global__ void k_boxes_finalize(uint64_t* boxkeys, uint64_t total) {
+  wait_prior_grid();
   uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
   if (i < total) boxkeys[i] = from_total_key_bits(boxkeys[i]);
 }
 
 __global__ void k_root_segment(uint32_t* node, uint32_t* start, uint32_t* len, uint32_t n) {
+  wait_prior_grid();
   *node = 0;
   *start = 0;
   *len = n;
 }
 
 __global__ void k_invert_rows(const uint32_t* idx, uint32_t* rows_of, uint64_t n) {
+  wait_prior_grid();
   const uint64_t r = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
   if (r < n) rows_of[idx[r]] = static_cast<uint32_t>(r);
 }
 
 __global__ void k_iota(uint32_t* idx, uint64_t n) {
+  wait_prior_grid();
   uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
   if (i < n) idx[i] = static_cast<uint32_t>(i);
 }
@@ -1172,6 +1216,7 @@ __global__ void k_iota(uint32_t* idx, uint64_t n) {
 // FP32 filter copies: data rounded to nearest; boxes rounded outward.
 __global__ void k_make_f32(const double* data, float* data32, uint64_t n_el, const double* boxes, float* boxes32,
                            uint64_t n_nodes, uint64_t d) {
+  wait_prior_grid();
   uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
   if (i < n_el) data32[i] = __double2float_rn(data[i]);
   uint64_t nb = n_nodes * 2 * d;
@@ -1184,6 +1229,7 @@ __global__ void k_make_f32(const double* data, float* data32, uint64_t n_el, con
 // Rows of `d` floats copied to rows of `w` (>= d) floats, zero padded: the
 // runtime-width warp kernels load every row as whole float4 vectors.
 __global__ void k_pad_rows(const float* src, uint64_t n, uint64_t d, uint64_t w, float* dst) {
+  wait_prior_grid();
   const uint64_t f = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
   if (f >= n * w) return;
   const uint64_t r = f / w, j = f - r * w;
@@ -1353,23 +1399,23 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
   // arrays when (n_perm - 1 - lv) is even
   auto writes_tree = [&](size_t lv) { return ((n_perm - 1 - lv) & 1) == 0; };
 
-  k_init_boxkeys<<<grid1(2 * d, 256), 256, 0, st>>>(T.boxes, 1, d);
+  KD_TRY_CUDA(chain(k_init_boxkeys, grid1(2 * d, 256), 256, 0, st, T.boxes, 1, d));
   KD_TRY_CUDA(cudaMemsetAsync(X.status, 0, sizeof(uint32_t), st));
   const double* din;
   const uint32_t* iin;
   if (n_perm == 0) {  // the root is a leaf of more than SMALL_MAX rows
     KD_TRY_CUDA(cudaMemcpyAsync(T.data, d_src, n * d * sizeof(double), cudaMemcpyDeviceToDevice, st));
-    k_iota<<<grid1(n, 256), 256, 0, st>>>(T.idx, n);
+    KD_TRY_CUDA(chain(k_iota, grid1(n, 256), 256, 0, st, T.idx, n));
     din = T.data;
     iin = T.idx;
   } else {
     // the identity permutation sits in the index array level 0 does not write
     uint32_t* iota = writes_tree(0) ? X.idx : T.idx;
-    k_iota<<<grid1(n, 256), 256, 0, st>>>(iota, n);
+    KD_TRY_CUDA(chain(k_iota, grid1(n, 256), 256, 0, st, iota, n));
     din = d_src;
     iin = iota;
   }
-  k_root_segment<<<1, 1, 0, st>>>(X.seg[0][0], X.seg[0][1], X.seg[0][2], static_cast<uint32_t>(n));
+  KD_TRY_CUDA(chain(k_root_segment, 1, 1, 0, st, X.seg[0][0], X.seg[0][1], X.seg[0][2], static_cast<uint32_t>(n)));
   KD_TRY_CUDA(cudaGetLastError());
   KD_TRY_CUDA(cudaFuncSetAttribute(k_small_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(sizeof(SubShared))));
@@ -1394,7 +1440,7 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
       // at level 0 it also checks that every coordinate is finite
       SubArgs A{din, iin, dout, iout, d, static_cast<uint32_t>(leafsize),
                 X.seg[cur][0], X.seg[cur][1], X.seg[cur][2], T.nodes, T.boxes, X.node_len, lv == 0, X.status};
-      k_small_subtree<<<static_cast<unsigned>(s.slots), SUB_THREADS, sizeof(SubShared), st>>>(A);
+      KD_TRY_CUDA(chain(k_small_subtree, static_cast<unsigned>(s.slots), SUB_THREADS, sizeof(SubShared), st, A));
       KD_TRY_CUDA(cudaGetLastError());
       break;
     }
@@ -1406,12 +1452,12 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
       const uint64_t chunk_rows = std::max<uint64_t>(1, (bbox_threads * 8) / d);
       const uint64_t nchunk = (s.max_len + chunk_rows - 1) / chunk_rows;
       dim3 g(static_cast<unsigned>(s.slots), static_cast<unsigned>(std::min<uint64_t>(nchunk, 65535)));
-      k_bbox<<<g, bbox_threads, 2 * d * sizeof(uint64_t), st>>>(L, static_cast<uint32_t>(chunk_rows),
-                                                                static_cast<uint32_t>(nchunk), lv == 0, X.status);
+      KD_TRY_CUDA(chain(k_bbox, g, bbox_threads, 2 * d * sizeof(uint64_t), st, L, static_cast<uint32_t>(chunk_rows),
+                                                                static_cast<uint32_t>(nchunk), lv == 0, X.status));
       KD_TRY_CUDA(cudaGetLastError());
     }
     if (!s.any_inner) {
-      k_leaf_records<<<grid1(s.slots, 256), 256, 0, st>>>(L);
+      KD_TRY_CUDA(chain(k_leaf_records, grid1(s.slots, 256), 256, 0, st, L));
       KD_TRY_CUDA(cudaGetLastError());
       break;
     }
@@ -1419,17 +1465,16 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
       const LargeScratch& S = X.lg;
       const uint32_t nch = static_cast<uint32_t>((s.max_len + LG_CHUNK - 1) / LG_CHUNK);
       dim3 g(static_cast<unsigned>(s.slots), std::min<uint32_t>(nch, 65535u));
-      KD_TRY_CUDA(cudaMemsetAsync(S.hist, 0, s.slots * RADIX_PASSES * 256 * sizeof(uint32_t), st));
-      k_lg_prepare<<<grid1(s.slots, 256), 256, 0, st>>>(L, S);
-      k_lg_keys<<<g, LG_THREADS, 0, st>>>(L, S);
-      for (int pass = 0; pass < RADIX_PASSES; ++pass) k_lg_hist<<<g, LG_THREADS, 0, st>>>(L, S, pass);
-      k_lg_count_lt<<<g, LG_THREADS, 0, st>>>(L, S);
-      k_lg_flagcount<<<g, LG_THREADS, 0, st>>>(L, S, nch);
-      k_lg_chunkscan<<<static_cast<unsigned>(s.slots), 1024, 0, st>>>(L, S, nch);
-      k_lg_lists<<<g, LG_THREADS, 0, st>>>(L, S, nch);
-      k_lg_move<<<g, LG_THREADS, 0, st>>>(L, S);
-      k_lg_fixup<<<static_cast<unsigned>(s.slots), FIX_THREADS, 0, st>>>(L, S);
-      k_lg_expand<<<grid1(s.slots, 256), 256, 0, st>>>(L, S);
+      KD_TRY_CUDA(chain(k_lg_prepare, grid1(s.slots, 256), 256, 0, st, L, S));
+      KD_TRY_CUDA(chain(k_lg_keys, g, LG_THREADS, 0, st, L, S));
+      for (int pass = 0; pass < RADIX_PASSES; ++pass) KD_TRY_CUDA(chain(k_lg_hist, g, LG_THREADS, 0, st, L, S, pass));
+      KD_TRY_CUDA(chain(k_lg_count_lt, g, LG_THREADS, 0, st, L, S));
+      KD_TRY_CUDA(chain(k_lg_flagcount, g, LG_THREADS, 0, st, L, S, nch));
+      KD_TRY_CUDA(chain(k_lg_chunkscan, static_cast<unsigned>(s.slots), 1024, 0, st, L, S, nch));
+      KD_TRY_CUDA(chain(k_lg_lists, g, LG_THREADS, 0, st, L, S, nch));
+      KD_TRY_CUDA(chain(k_lg_move, g, LG_THREADS, 0, st, L, S));
+      KD_TRY_CUDA(chain(k_lg_fixup, static_cast<unsigned>(s.slots), FIX_THREADS, 0, st, L, S));
+      KD_TRY_CUDA(chain(k_lg_expand, grid1(s.slots, 256), 256, 0, st, L, S));
       KD_TRY_CUDA(cudaGetLastError());
     }
     din = dout;
@@ -1437,20 +1482,20 @@ int build_on_device(const double* d_src, uint64_t n, uint64_t d, uint64_t leafsi
     cur ^= 1;
   }
 
-  k_order_by_box<<<grid1(n_nodes, 256), 256, 0, st>>>(T.nodes, T.boxes, X.node_len, n_nodes, d);
-  k_boxes_finalize<<<grid1(n_nodes * 2 * d, 256), 256, 0, st>>>(T.boxes, n_nodes * 2 * d);
+  KD_TRY_CUDA(chain(k_order_by_box, grid1(n_nodes, 256), 256, 0, st, T.nodes, T.boxes, X.node_len, n_nodes, d));
+  KD_TRY_CUDA(chain(k_boxes_finalize, grid1(n_nodes * 2 * d, 256), 256, 0, st, T.boxes, n_nodes * 2 * d));
   KD_TRY_CUDA(cudaGetLastError());
 
   // The final row order sits in the tree's row array (din).
-  k_invert_rows<<<grid1(n, 256), 256, 0, st>>>(T.idx, T.rows_of, n);
-  k_make_f32<<<grid1(std::max(n * d, n_nodes * 2 * d), 256), 256, 0, st>>>(
-      T.data, T.data32, n * d, reinterpret_cast<const double*>(T.boxes), T.boxes32, n_nodes, d);
+  KD_TRY_CUDA(chain(k_invert_rows, grid1(n, 256), 256, 0, st, T.idx, T.rows_of, n));
+  KD_TRY_CUDA(chain(k_make_f32, grid1(std::max(n * d, n_nodes * 2 * d), 256), 256, 0, st, 
+      T.data, T.data32, n * d, reinterpret_cast<const double*>(T.boxes), T.boxes32, n_nodes, d));
   KD_TRY_CUDA(cudaGetLastError());
   // FP32 rows padded to a multiple of 4 floats for width 3 and the
   // runtime-width warp kernels (widths other than 1, 2, 3, 4, 8, 16, up to
   // 128): the FP32 copy itself when d is a multiple of 4
   if (need_pad) {
-    k_pad_rows<<<grid1(n * w32, 256), 256, 0, st>>>(T.data32, n, d, w32, T.data32w);
+    KD_TRY_CUDA(chain(k_pad_rows, grid1(n * w32, 256), 256, 0, st, T.data32, n, d, w32, T.data32w));
     KD_TRY_CUDA(cudaGetLastError());
   }
   // The one host synchronisation: the finiteness status and the root box.

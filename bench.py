@@ -781,6 +781,62 @@ def run_profile_case(name):
     return 0
 
 
+WORK_NAMES = ["warps", "live_queries", "seed_rows", "node_pops", "nodes_entered", "lane_nodes_needed",
+              "leaves_scanned", "rows_scanned", "lane_rows_needed", "rows_past_filter", "offers"]
+
+
+def run_work_counts():
+    """The packet traversal's work on the bench workload (uniform N=1M, d=3,
+    k=16, 1M queries), counted by the measurement build of the library
+    (KD_WORK_COUNTS), against the oracle's per-query work of the reference's
+    own descent (nodes visited V_q, rows scanned S_q)."""
+    import torch
+
+    sys.path.insert(0, str(ROOT / "kdtree-rs_gb300"))
+    import build_lib
+
+    L = ctypes.CDLL(str(build_lib.build(counting=True)))
+    VP, u64, dbl = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double
+    L.kd_build.argtypes = [VP, u64, u64, u64, ctypes.c_int, ctypes.POINTER(VP)]
+    L.kd_query_device_path.argtypes = [VP, VP, u64, u64, dbl, ctypes.c_int, dbl, dbl, VP, VP, VP, ctypes.c_int, VP]
+    L.kd_work_counts.argtypes = [ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int, ctypes.c_int]
+    L.kd_free.argtypes = [VP]
+    data, q = workload(0)
+    h = VP()
+    assert L.kd_build(VP(data.ctypes.data), data.size, DIM, LEAFSIZE, 0, ctypes.byref(h)) == 0
+    dq = torch.from_numpy(q).cuda()
+    od = torch.empty((len(q), K), dtype=torch.float64, device="cuda")
+    oi = torch.empty((len(q), K), dtype=torch.int64, device="cuda")
+    buf = (ctypes.c_ulonglong * 16)()
+    assert L.kd_work_counts(buf, 16, 1) == 0  # reset
+    assert L.kd_query_device_path(h, VP(dq.data_ptr()), dq.numel(), K, P, 0, 0.0, 0.0, VP(od.data_ptr()),
+                                  VP(oi.data_ptr()), None, PATH_PACKET, None) == 0
+    assert L.kd_work_counts(buf, 16, 0) == 0
+    c = dict(zip(WORK_NAMES, [int(x) for x in buf[:len(WORK_NAMES)]]))
+    L.kd_free(h)
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import kdtree_oracle
+
+    ot = kdtree_oracle.OracleKDTree(data, leafsize=LEAFSIZE, parallel=True)
+    ot.query(q, k=K, p=P, threads=os.cpu_count())
+    v_q, s_q = ot.last_counts[0] / len(q), ot.last_counts[1] / len(q)
+    nq, w = c["live_queries"], c["warps"]
+    rows_lane = (c["rows_scanned"] + 0.0) / w + c["seed_rows"] / nq  # rows a lane evaluates
+    out = {"work_counts": c, "per_query": {
+        "reference_nodes_visited": v_q, "reference_rows_scanned": s_q,
+        "rows_evaluated_per_lane": rows_lane, "rows_needed_per_query": (c["lane_rows_needed"] + c["seed_rows"]) / nq,
+        "nodes_entered_per_warp": c["nodes_entered"] / w, "node_pops_per_warp": c["node_pops"] / w,
+        "lane_nodes_needed_per_query": c["lane_nodes_needed"] / nq,
+        "leaves_scanned_per_warp": c["leaves_scanned"] / w, "offers_per_query": c["offers"] / nq,
+        "rows_past_filter_per_query": c["rows_past_filter"] / nq},
+        "inflation": {"rows_evaluated_over_reference": rows_lane / s_q,
+                      "rows_needed_over_reference": (c["lane_rows_needed"] + c["seed_rows"]) / nq / s_q,
+                      "lane_utilisation_in_leaves": c["lane_rows_needed"] / max(1, 32 * c["rows_scanned"]),
+                      "nodes_entered_per_warp_over_reference": c["nodes_entered"] / w / v_q}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_profile_tc():
     """A tensor-core-path case small enough for an ncu capture: one CTA-filling
     batch (152 x 128 queries) against 100,000 points, d=64, k=32."""
@@ -840,9 +896,13 @@ def main():
     ap.add_argument("--profile-tc", action="store_true",
                     help="only run the tensor-core path on a profiling-sized case (N=100k, d=64, "
                          "19,456 queries, k=32), 3 calls")
+    ap.add_argument("--work-counts", action="store_true",
+                    help="count the packet traversal's work with the measurement build and print it")
     ap.add_argument("--profile-case", default=None,
                     help="only run one small scenario for a per-kernel ncu capture: " + ", ".join(PROFILE_CASES))
     args = ap.parse_args()
+    if args.work_counts:
+        return run_work_counts()
     if args.profile_case:
         return run_profile_case(args.profile_case)
     if args.impl == "reference":

@@ -3,6 +3,11 @@
 Each translation unit is compiled for sm_103a in parallel, then linked into one
 shared library in `_build/` next to this file.  Usable as a script
 (`python kdtree-rs_gb300/build_lib.py`) or through `build()`.
+
+`build(counting=True)` makes a measurement variant, `_build/counts/
+libkdtree_gb300_counts.so`, compiled with KD_WORK_COUNTS: the packet traversal
+then counts the work it does (nodes, leaves, rows, offers) in device counters
+that kd_work_counts reads.  The product library never has them.
 """
 from __future__ import annotations
 
@@ -44,15 +49,18 @@ def _stale(obj: Path, src: Path) -> bool:
     return any(d.stat().st_mtime > obj.stat().st_mtime for d in deps if d.exists())
 
 
-def build(verbose: bool = False, force: bool = False) -> Path:
-    OUT.mkdir(exist_ok=True)
+def build(verbose: bool = False, force: bool = False, counting: bool = False) -> Path:
+    out = OUT / "counts" if counting else OUT
+    lib = out / "libkdtree_gb300_counts.so" if counting else LIB
+    flags = [*NVCC_FLAGS, "-DKD_WORK_COUNTS"] if counting else NVCC_FLAGS
+    out.mkdir(parents=True, exist_ok=True)
     nvcc = _nvcc()
     jobs = []
     for s in SOURCES:
         src = CSRC / s
-        obj = OUT / (s + ".o")
+        obj = out / (s + ".o")
         if force or _stale(obj, src):
-            jobs.append([nvcc, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)])
+            jobs.append([nvcc, *flags, "-c", str(src), "-o", str(obj)])
 
     def run(cmd):
         if verbose:
@@ -65,12 +73,12 @@ def build(verbose: bool = False, force: bool = False) -> Path:
 
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         list(ex.map(run, jobs))
-    objs = [str(OUT / (s + ".o")) for s in SOURCES]
-    if jobs or not LIB.exists():
-        tmp = OUT / "libkdtree_gb300.so.tmp"
+    objs = [str(out / (s + ".o")) for s in SOURCES]
+    if jobs or not lib.exists():
+        tmp = out / (lib.name + ".tmp")
         run([nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", *objs, "-o", str(tmp), "-lcudart"])
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

@@ -94,3 +94,20 @@ int launch_packet_query(const QArgs& a, int metric, cudaStream_t st) {
 }
 
 }  // namespace kd
+
+#ifdef KD_WORK_COUNTS
+// The packet traversal's work counters (kd_query_packet.cuh), added up since
+// the last reset: out[0 .. n) (n <= 16); reset != 0 zeroes them afterwards.
+extern "C" int kd_work_counts(unsigned long long* out, int n, int reset) {
+  if (n < 0 || n > 16) return 1;
+  unsigned long long h[16] = {};
+  if (cudaDeviceSynchronize() != cudaSuccess || cudaMemcpyFromSymbol(h, kd::g_work, sizeof(h)) != cudaSuccess)
+    return 2;
+  for (int i = 0; i < n; ++i) out[i] = h[i];
+  if (reset) {
+    const unsigned long long z[16] = {};
+    if (cudaMemcpyToSymbol(kd::g_work, z, sizeof(z)) != cudaSuccess) return 2;
+  }
+  return 0;
+}
+#endif

@@ -23,6 +23,20 @@
 
 constexpr int PACKET_STACK = 2 * KD_MAX_DEPTH;
 
+// Work counters of the measurement build (KD_WORK_COUNTS; kd_work_counts reads
+// them): what the warps of this translation unit's packet traversals did.
+//   0 warps, 1 live queries, 2 seed-leaf rows (per query), 3 node pops (per
+//   warp), 4 nodes entered (per warp), 5 lane-nodes needed (sum over entered
+//   nodes of the lanes that need them), 6 leaves scanned (per warp), 7 rows
+//   scanned (per warp: every lane evaluates them), 8 lane-rows needed, 9 rows
+//   offered or noted after the filter (per query), 10 offers (per query)
+#ifdef KD_WORK_COUNTS
+__device__ unsigned long long g_work[16];
+#define KD_WORK(i, v) atomicAdd(&g_work[i], static_cast<unsigned long long>(v))
+#else
+#define KD_WORK(i, v) ((void)0)
+#endif
+
 // Cheap rigorous point filter.  With a = p32 - q32 (exact reals) and every
 // coordinate within E = 2^-24 (|coordinate bound| + |q|) + 2^-148 of its FP32
 // copy, the triangle inequality gives |p - q| >= |a| - sqrt(d) E (L2; d E for L1,
@@ -172,6 +186,15 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
     live &= isfinite(q.v[i]);
   }
   if (in_range && !live) atomicOr(a.status, 1u);
+#ifdef KD_WORK_COUNTS
+  {
+    const uint32_t lv = __popc(__ballot_sync(0xffffffffu, live));
+    if ((threadIdx.x & 31) == 0) {
+      KD_WORK(0, 1);
+      KD_WORK(1, lv);
+    }
+  }
+#endif
   if (!live) {
 #pragma unroll
     for (int i = 0; i < D; ++i) q.v[i] = 0.0;
@@ -221,6 +244,7 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
     own = n;
     const uint64_t se = dbits(nd.split);
     const uint32_t start = static_cast<uint32_t>(se), end = static_cast<uint32_t>(se >> 32);
+    KD_WORK(2, end - start);
     const uint32_t chunk_end = (D == 8 && M != M_LINF) ? start + (end - start) / 8 * 8 : end;
     for (uint32_t r = start; r < end; ++r) {
       const float sr = row_sum(r);
@@ -249,6 +273,15 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
     const bool need = live && !(lb > best.b_hi);
     if (live && !need) best.note(lb);
     const uint32_t need_mask = __ballot_sync(0xffffffffu, need);
+#ifdef KD_WORK_COUNTS
+    if ((threadIdx.x & 31) == 0) {
+      KD_WORK(3, 1);
+      if (need_mask) {
+        KD_WORK(4, 1);
+        KD_WORK(5, __popc(need_mask));
+      }
+    }
+#endif
     if (!need_mask) continue;  // every lane's points there exceed its bound
     const DNode nd = a.nodes[node];
     if (nd.meta & KD_NODE_LEAF) {
@@ -257,6 +290,16 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
       const uint64_t se = dbits(nd.split);
       const uint32_t start = static_cast<uint32_t>(se), end = static_cast<uint32_t>(se >> 32);
       const uint32_t chunk_end = (D == 8 && M != M_LINF) ? start + (end - start) / 8 * 8 : end;
+#ifdef KD_WORK_COUNTS
+      {
+        const uint32_t takers = __popc(__ballot_sync(0xffffffffu, take));
+        if ((threadIdx.x & 31) == 0) {
+          KD_WORK(6, 1);
+          KD_WORK(7, end - start);
+          KD_WORK(8, takers * (end - start));
+        }
+      }
+#endif
       for (uint32_t c0 = start; c0 < end; c0 += 32) {
         const uint32_t c1 = min(end, c0 + 32);
         // 1. which of these points can this lane's bound admit (or lie in
@@ -272,10 +315,12 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
             const uint32_t r = c0 + __ffs(pending) - 1;
             pending &= pending - 1;
             const float sr = row_sum(r);
+            KD_WORK(9, 1);
             if (!(sr > thr2)) {  // the bound may have tightened meanwhile
               float clo, chi;
               filt.enclose(sr, &clo, &chi);
               if (!(sr > thr) && !(clo > best.b_hi)) {
+                KD_WORK(10, 1);
                 best.offer(clo, chi, r, r < chunk_end);
                 thr = filt.threshold(best.b_hi);
                 thr2 = filt.threshold(band_of(best.b_hi));

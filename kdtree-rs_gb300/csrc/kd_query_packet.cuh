@@ -112,6 +112,25 @@ struct PointFilter {
   // (filter_rows): one 16-byte load.
   __device__ __forceinline__ float sum(const float* p32) const {
     float p[D];
+    load(p32, p);
+    return reduce_of(p, q32);
+  }
+  // The FP32 reduced distance of the loaded row p to the FP32 query q, in
+  // dimension order: every filter sum of the packet traversal is this one
+  // sequence of operations, so two evaluations of a (row, query) agree.
+  static __device__ __forceinline__ float reduce_of(const float (&p)[D], const float (&q)[D]) {
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      const float t = __fsub_rn(p[i], q[i]);
+      if (M == M_L2) s = __fmaf_rn(t, t, s);
+      else if (M == M_L1) s = __fadd_rn(s, fabsf(t));
+      else s = fmaxf(s, fabsf(t));
+    }
+    return s;
+  }
+  // The row at p32 loaded (widths: as sum)
+  static __device__ __forceinline__ void load(const float* p32, float (&p)[D]) {
     if constexpr (D == 3) {
       const float4 v = *reinterpret_cast<const float4*>(p32);
       p[0] = v.x;
@@ -137,15 +156,6 @@ struct PointFilter {
 #pragma unroll
       for (int i = 0; i < D; ++i) p[i] = p32[i];
     }
-    float s = 0.f;
-#pragma unroll
-    for (int i = 0; i < D; ++i) {
-      const float t = __fsub_rn(p[i], q32[i]);
-      if (M == M_L2) s = __fmaf_rn(t, t, s);
-      else if (M == M_L1) s = __fadd_rn(s, fabsf(t));
-      else s = fmaxf(s, fabsf(t));
-    }
-    return s;
   }
 };
 
@@ -286,28 +296,45 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
     const DNode nd = a.nodes[node];
     if (nd.meta & KD_NODE_LEAF) {
       const bool take = need && node != own;  // its own leaf was offered already
-      if (!__any_sync(0xffffffffu, take)) continue;
+      const uint32_t take_mask = __ballot_sync(0xffffffffu, take);
+      if (!take_mask) continue;
       const uint64_t se = dbits(nd.split);
       const uint32_t start = static_cast<uint32_t>(se), end = static_cast<uint32_t>(se >> 32);
       const uint32_t chunk_end = (D == 8 && M != M_LINF) ? start + (end - start) / 8 * 8 : end;
 #ifdef KD_WORK_COUNTS
-      {
-        const uint32_t takers = __popc(__ballot_sync(0xffffffffu, take));
-        if ((threadIdx.x & 31) == 0) {
-          KD_WORK(6, 1);
-          KD_WORK(7, end - start);
-          KD_WORK(8, takers * (end - start));
-        }
+      if ((threadIdx.x & 31) == 0) {
+        KD_WORK(6, 1);
+        KD_WORK(7, end - start);
+        KD_WORK(8, __popc(take_mask) * (end - start));
       }
 #endif
+      const uint32_t lane = threadIdx.x & 31;
+      const uint32_t n_take = __popc(take_mask);
+      const uint32_t my_rank = __popc(take_mask & ((1u << lane) - 1));  // among the lanes that take the leaf
       for (uint32_t c0 = start; c0 < end; c0 += 32) {
-        const uint32_t c1 = min(end, c0 + 32);
-        // 1. which of these points can this lane's bound admit (or lie in
-        //    the near-tie band just above it)?
+        // 1. which of these rows can each taker's bound admit (or put in the
+        //    near-tie band just above it)?  Lanes take the rows (gs lanes a
+        //    taker, 32 / gs takers a round) and get each taker's FP32 query
+        //    and band threshold by shuffle: only the takers' rows are summed.
+        const uint32_t rows = min(32u, end - c0);
+        const uint32_t gs = rows <= 8 ? 8u : (rows <= 16 ? 16u : 32u);
+        const uint32_t in_group = lane & (gs - 1), group = lane / gs;
+        float p[D];
+        PointFilter<M, D>::load(rows32 + static_cast<uint64_t>(c0 + min(in_group, rows - 1)) * filter_stride<D>(a), p);
         uint32_t pending = 0;
-        for (uint32_t r = c0; r < c1; ++r) {
-          const float s = row_sum(r);
-          if (take && !(s > thr2)) pending |= 1u << (r - c0);
+        for (uint32_t base = 0; base < n_take; base += 32 / gs) {  // uniform
+          const uint32_t j = base + group;
+          const uint32_t src = j < n_take ? __fns(take_mask, 0, static_cast<int>(j) + 1) : 0;
+          float q[D];
+#pragma unroll
+          for (int i = 0; i < D; ++i) q[i] = __shfl_sync(0xffffffffu, filt.q32[i], static_cast<int>(src));
+          const float th = __shfl_sync(0xffffffffu, thr2, static_cast<int>(src));
+          const float sv = PointFilter<M, D>::reduce_of(p, q);
+          const uint32_t bits = __ballot_sync(0xffffffffu, j < n_take && in_group < rows && !(sv > th));
+          if (take && my_rank >= base && my_rank < base + 32 / gs) {
+            const uint32_t sl = my_rank - base;
+            pending = (bits >> (sl * gs)) & (gs == 32 ? 0xffffffffu : ((1u << gs) - 1));
+          }
         }
         // 2. offer them, all lanes with a pending point together
         while (__any_sync(0xffffffffu, pending != 0)) {

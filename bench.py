@@ -782,7 +782,8 @@ def run_profile_case(name):
 
 
 WORK_NAMES = ["warps", "live_queries", "seed_rows", "node_pops", "nodes_entered", "lane_nodes_needed",
-              "leaves_scanned", "rows_scanned", "lane_rows_needed", "rows_past_filter", "offers"]
+              "leaves_scanned", "rows_scanned", "lane_rows_needed", "rows_past_filter", "offers",
+              "cycles_setup_and_seed", "cycles_nodes", "cycles_leaf_filter", "cycles_offers", "cycles_sort_write"]
 
 
 def run_work_counts():
@@ -813,6 +814,8 @@ def run_work_counts():
                                   VP(oi.data_ptr()), None, PATH_PACKET, None) == 0
     assert L.kd_work_counts(buf, 16, 0) == 0
     c = dict(zip(WORK_NAMES, [int(x) for x in buf[:len(WORK_NAMES)]]))
+    cyc = {k: v for k, v in c.items() if k.startswith("cycles_")}
+    tot = sum(cyc.values()) or 1
     L.kd_free(h)
     sys.path.insert(0, str(ROOT / "oracle"))
     import kdtree_oracle
@@ -829,6 +832,7 @@ def run_work_counts():
         "lane_nodes_needed_per_query": c["lane_nodes_needed"] / nq,
         "leaves_scanned_per_warp": c["leaves_scanned"] / w, "offers_per_query": c["offers"] / nq,
         "rows_past_filter_per_query": c["rows_past_filter"] / nq},
+        "phase_share": {k[len("cycles_"):]: v / tot for k, v in cyc.items()},
         "inflation": {"rows_evaluated_over_reference": rows_lane / s_q,
                       "rows_needed_over_reference": (c["lane_rows_needed"] + c["seed_rows"]) / nq / s_q,
                       "lane_utilisation_in_leaves": c["lane_rows_needed"] / max(1, 32 * c["rows_scanned"]),

@@ -30,11 +30,23 @@ constexpr int PACKET_STACK = 2 * KD_MAX_DEPTH;
 //   nodes of the lanes that need them), 6 leaves scanned (per warp), 7 rows
 //   scanned (per warp: every lane evaluates them), 8 lane-rows needed, 9 rows
 //   offered or noted after the filter (per query), 10 offers (per query)
+//   11..15: SM clock cycles of each phase, summed over warps (lane 0 reads
+//   clock64 at the phase boundaries, the warp synchronised there): 11 setup
+//   and seed leaf, 12 node steps, 13 leaf filter rounds, 14 offers, 15 sort
+//   and write.
 #ifdef KD_WORK_COUNTS
 __device__ unsigned long long g_work[16];
 #define KD_WORK(i, v) atomicAdd(&g_work[i], static_cast<unsigned long long>(v))
+#define KD_PHASE(i)                                          \
+  do {                                                       \
+    __syncwarp();                                            \
+    const long long kd_now_ = clock64();                     \
+    if ((threadIdx.x & 31) == 0) KD_WORK(i, kd_now_ - kd_t_); \
+    kd_t_ = kd_now_;                                         \
+  } while (0)
 #else
 #define KD_WORK(i, v) ((void)0)
+#define KD_PHASE(i) ((void)0)
 #endif
 
 // Cheap rigorous point filter.  With a = p32 - q32 (exact reals) and every
@@ -183,6 +195,9 @@ template <int M, int D, int K>
 __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, float* s_lo, float* s_hi,
                                                uint32_t* s_row, uint32_t* s_stack) {
   static_assert(D > 0 && M != M_LP, "packet path: compile-time width, metric without pow()");
+#ifdef KD_WORK_COUNTS
+  long long kd_t_ = clock64();
+#endif
   const bool in_range = tid < a.nq;
   const uint64_t qi = in_range ? (a.order ? a.order[tid] : tid) : 0;
   // Lanes past the batch end (or with a non-finite query) stay in the warp for
@@ -277,6 +292,7 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
   uint32_t* stack = s_stack + (threadIdx.x >> 5) * PACKET_STACK;
   int sp = 0;
   stack[sp++] = 0;
+  KD_PHASE(11);
   while (sp > 0) {
     const uint32_t node = stack[--sp];
     const float lb = box_lb<M, D>(a.boxes32 + static_cast<uint64_t>(node) * 2 * D, qlo, qhi);
@@ -298,6 +314,7 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
       const bool take = need && node != own;  // its own leaf was offered already
       const uint32_t take_mask = __ballot_sync(0xffffffffu, take);
       if (!take_mask) continue;
+      KD_PHASE(12);
       const uint64_t se = dbits(nd.split);
       const uint32_t start = static_cast<uint32_t>(se), end = static_cast<uint32_t>(se >> 32);
       const uint32_t chunk_end = (D == 8 && M != M_LINF) ? start + (end - start) / 8 * 8 : end;
@@ -336,6 +353,7 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
             pending = (bits >> (sl * gs)) & (gs == 32 ? 0xffffffffu : ((1u << gs) - 1));
           }
         }
+        KD_PHASE(13);
         // 2. offer them, all lanes with a pending point together
         while (__any_sync(0xffffffffu, pending != 0)) {
           if (pending) {
@@ -357,6 +375,7 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
             }
           }
         }
+        KD_PHASE(14);
       }
       continue;
     }
@@ -371,6 +390,7 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
     stack[sp++] = left_first ? nd.right : node + 1;
     stack[sp++] = left_first ? node + 1 : nd.right;
   }
+  KD_PHASE(12);
   if constexpr (K >= 8) {
     if (live) best.sort_exact();
     best.write_warp(live, a.out_d + qi * a.k, a.out_i + qi * a.k, a.k, a.n_points);
@@ -378,6 +398,7 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
   } else {
     if (live && best.write(a.out_d + qi * a.k, a.out_i + qi * a.k, a.k, a.n_points)) flag_rerun(a, qi);
   }
+  KD_PHASE(15);
 }
 
 template <int M, int D, int K>

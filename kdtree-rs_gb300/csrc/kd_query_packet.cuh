@@ -288,13 +288,16 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
   }
 
   // Every lane pushes the same ids to the same words and pops what it pushed
-  // itself, so no lane depends on another's store.
+  // itself, so no lane depends on another's store.  An entered inner node
+  // stacks its far child and continues with the near one.
   uint32_t* stack = s_stack + (threadIdx.x >> 5) * PACKET_STACK;
   int sp = 0;
-  stack[sp++] = 0;
+  uint32_t node = 0;  // the node at hand; the near child follows an entered node without a push
   KD_PHASE(11);
-  while (sp > 0) {
-    const uint32_t node = stack[--sp];
+  for (;;) {
+    // the record loads with the box: one round trip a pop (it is wasted only
+    // when no lane needs the node)
+    const DNode nd = a.nodes[node];
     const float lb = box_lb<M, D>(a.boxes32 + static_cast<uint64_t>(node) * 2 * D, qlo, qhi);
     const bool need = live && !(lb > best.b_hi);
     if (live && !need) best.note(lb);
@@ -308,12 +311,19 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
       }
     }
 #endif
-    if (!need_mask) continue;  // every lane's points there exceed its bound
-    const DNode nd = a.nodes[node];
+    if (!need_mask) {  // every lane's points there exceed its bound
+      if (sp == 0) break;
+      node = stack[--sp];
+      continue;
+    }
     if (nd.meta & KD_NODE_LEAF) {
       const bool take = need && node != own;  // its own leaf was offered already
       const uint32_t take_mask = __ballot_sync(0xffffffffu, take);
-      if (!take_mask) continue;
+      if (!take_mask) {
+        if (sp == 0) break;
+        node = stack[--sp];
+        continue;
+      }
       KD_PHASE(12);
       const uint64_t se = dbits(nd.split);
       const uint32_t start = static_cast<uint32_t>(se), end = static_cast<uint32_t>(se >> 32);
@@ -377,6 +387,8 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
         }
         KD_PHASE(14);
       }
+      if (sp == 0) break;
+      node = stack[--sp];
       continue;
     }
     // near child first, by majority of the lanes that need this node
@@ -388,7 +400,7 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
     const uint32_t left_votes = __popc(__ballot_sync(0xffffffffu, need && left));
     const bool left_first = 2 * left_votes >= static_cast<uint32_t>(__popc(need_mask));
     stack[sp++] = left_first ? nd.right : node + 1;
-    stack[sp++] = left_first ? node + 1 : nd.right;
+    node = left_first ? node + 1 : nd.right;
   }
   KD_PHASE(12);
   if constexpr (K >= 8) {

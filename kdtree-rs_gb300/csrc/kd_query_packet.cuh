@@ -277,9 +277,12 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
         float clo, chi;
         filt.enclose(sr, &clo, &chi);
         if (!(sr > thr) && !(clo > best.b_hi)) {
+          const float before = best.b_hi;
           best.offer(clo, chi, r, r < chunk_end);
-          thr = filt.threshold(best.b_hi);
-          thr2 = filt.threshold(band_of(best.b_hi));
+          if (best.b_hi != before) {  // the bound stays +inf (or unchanged) until the list fills
+            thr = filt.threshold(best.b_hi);
+            thr2 = filt.threshold(band_of(best.b_hi));
+          }
         } else {
           best.note_point(clo, r, r < chunk_end);
         }
@@ -376,9 +379,12 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
               filt.enclose(sr, &clo, &chi);
               if (!(sr > thr) && !(clo > best.b_hi)) {
                 KD_WORK(10, 1);
+                const float before = best.b_hi;
                 best.offer(clo, chi, r, r < chunk_end);
-                thr = filt.threshold(best.b_hi);
-                thr2 = filt.threshold(band_of(best.b_hi));
+                if (best.b_hi != before) {
+                  thr = filt.threshold(best.b_hi);
+                  thr2 = filt.threshold(band_of(best.b_hi));
+                }
               } else {
                 best.note_point(clo, r, r < chunk_end);
               }

@@ -68,7 +68,9 @@ struct TcArgs {
   const uint32_t* indices;
   const uint32_t* order;  // sorted row -> query index (rows are grouped by landing leaf)
   const uint32_t* tile_start;  // per query tile: the point tile holding its landing leaf
-  const float* q32;       // nq x d, FP32 copies of the queries, in sorted row order
+  const float* q32;       // nq x w32, FP32 copies of the queries (zero padded), in sorted row order
+  const float* data32w;   // tree-ordered points, FP32, rows padded to w32 floats (zeros)
+  uint32_t w32;           // d rounded up to a multiple of 4
   const float* qn2;       // |q_b|^2, FP32 sum
   const float* qnorm;     // |q_b| rounded up
   const float* pw;        // per point w (padded to whole tiles with +inf)
@@ -395,7 +397,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const uint64_t qi = a.order[qrow];  // the query's own index
       LazySetDyn<K> set;
       set.init(a.k, a.cutoff, DynPoint{a.queries + qi * a.d, a.data, a.d, a.strat}, a.indices);
-      const float* q32 = a.q32 + qrow * a.d;
+      const float* q32 = a.q32 + qrow * a.w32;
       float qmax = 0.f;
       for (uint64_t i = 0; i < a.d; ++i) qmax = fmaxf(qmax, fabsf(q32[i]));
       // enclosure of a survivor's exact distance from its FP32 coordinates
@@ -476,11 +478,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (p >= a.n_points) continue;
             surv += survivor;
             // FP32 sum of squares and its enclosure (triangle inequality, as the
-            // packet filter; the sqrt margin 2^-16 covers d <= 128)
-            const float* p32 = a.data32 + static_cast<uint64_t>(p) * a.d;
+            // packet filter; the sqrt margin 2^-16 covers d <= 128), in
+            // dimension order from the zero-padded rows, four floats a load
+            // and four loads in flight
+            const float4* p4 = reinterpret_cast<const float4*>(a.data32w + static_cast<uint64_t>(p) * a.w32);
+            const float4* q4 = reinterpret_cast<const float4*>(q32);
             float s2 = 0.f;
-            for (uint64_t i = 0; i < a.d; ++i) {
-              const float dd = __fsub_rn(p32[i], q32[i]);
+#pragma unroll 4
+            for (uint32_t i = 0; i < a.w32 / 4; ++i) {
+              const float4 pv4 = p4[i], qv4 = q4[i];
+              float dd = __fsub_rn(pv4.x, qv4.x);
+              s2 = __fmaf_rn(dd, dd, s2);
+              dd = __fsub_rn(pv4.y, qv4.y);
+              s2 = __fmaf_rn(dd, dd, s2);
+              dd = __fsub_rn(pv4.z, qv4.z);
+              s2 = __fmaf_rn(dd, dd, s2);
+              dd = __fsub_rn(pv4.w, qv4.w);
               s2 = __fmaf_rn(dd, dd, s2);
             }
             const float rr = s2 > 0.f ? s2 * rsqrtf(s2) : 0.f;
@@ -570,11 +583,12 @@ __global__ void k_tc_pad(float* w, float* v, uint64_t from, uint64_t to) {
   }
 }
 
-__global__ void k_f32_gather(const double* src, const uint32_t* order, uint64_t n, uint64_t d, float* dst) {
+__global__ void k_f32_gather(const double* src, const uint32_t* order, uint64_t n, uint64_t d, uint64_t w,
+                             float* dst) {
   const uint64_t f = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
-  if (f >= n * d) return;
-  const uint64_t r = f / d, j = f - r * d;
-  dst[f] = __double2float_rn(src[static_cast<uint64_t>(order[r]) * d + j]);
+  if (f >= n * w) return;
+  const uint64_t r = f / w, j = f - r * w;
+  dst[f] = j < d ? __double2float_rn(src[static_cast<uint64_t>(order[r]) * d + j]) : 0.f;
 }
 
 // FP32 box enclosure ([lo | hi], d each) of each tile of `rows` consecutive
@@ -720,7 +734,7 @@ int query_tc_on_device(kd_tree* t, const double* d_queries, uint64_t nq, const Q
   const uint32_t n_qt = static_cast<uint32_t>((nq + TC_M - 1) / TC_M);
   void* mem = nullptr;
   const uint64_t qbytes = nq * dpad * sizeof(uint16_t), fbytes = nq * sizeof(float);
-  const uint64_t q32_bytes = nq * d * sizeof(float);
+  const uint64_t q32_bytes = nq * t->w32 * sizeof(float);
   const uint64_t sort_words = 2 * nq + order_scratch_words(t) + n_qt;
   const uint64_t qbox_bytes = static_cast<uint64_t>(n_qt) * 2 * d * sizeof(float);
   // rounded to 256 bytes: the BF16 query rows after it are a TMA source (16-byte aligned base)
@@ -734,10 +748,12 @@ int query_tc_on_device(kd_tree* t, const double* d_queries, uint64_t nq, const Q
   uint32_t* rerun_count = static_cast<uint32_t*>(mem);
   uint64_t* rerun_list = reinterpret_cast<uint64_t*>(static_cast<unsigned char*>(mem) + 16);
   uint16_t* qb = reinterpret_cast<uint16_t*>(static_cast<unsigned char*>(mem) + rerun_bytes);
-  float* qn2 = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(qb) + qbytes);
+  // the FP32 rows follow the BF16 ones (a whole number of 128-byte rows), so
+  // they start on a 16-byte boundary for their float4 reads
+  float* q32 = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(qb) + qbytes);
+  float* qn2 = q32 + nq * t->w32;
   float* qnorm = qn2 + nq;
-  float* q32 = qnorm + nq;
-  float* qbox = q32 + nq * d;
+  float* qbox = qnorm + nq;
   uint32_t* leaf_of = reinterpret_cast<uint32_t*>(qbox + static_cast<uint64_t>(n_qt) * 2 * d);
   uint32_t* order = leaf_of + nq;
   uint32_t* tile_start = order + nq;
@@ -746,7 +762,8 @@ int query_tc_on_device(kd_tree* t, const double* d_queries, uint64_t nq, const Q
   k_tile_start<<<(n_qt + 127) / 128, 128, 0, st>>>(t->nodes, leaf_of, order, nq, n_qt, tile_start);
   k_tc_rows<<<static_cast<unsigned>((nq + 255) / 256), 256, 0, st>>>(d_queries, order, nq, d, dpad, t->tc_centre, qb,
                                                                       qn2, qnorm, nullptr, nullptr);
-  k_f32_gather<<<static_cast<unsigned>((nq * d + 255) / 256), 256, 0, st>>>(d_queries, order, nq, d, q32);
+  k_f32_gather<<<static_cast<unsigned>((nq * t->w32 + 255) / 256), 256, 0, st>>>(d_queries, order, nq, d, t->w32,
+                                                                                q32);
   k_tile_boxes<<<n_qt, 128, 0, st>>>(q32, nq, d, TC_M, qbox);
   CUtensorMap mq, mp;
   if ((rc = make_rows_map(&mq, qb, nq, dpad, TC_M)) || (rc = make_rows_map(&mp, t->tc_points, t->n_points, dpad, TC_N))) {
@@ -761,6 +778,8 @@ int query_tc_on_device(kd_tree* t, const double* d_queries, uint64_t nq, const Q
   a.order = order;
   a.tile_start = tile_start;
   a.q32 = q32;
+  a.data32w = t->data32w;
+  a.w32 = t->w32;
   a.qn2 = qn2;
   a.qnorm = qnorm;
   a.pw = t->tc_w;

@@ -433,25 +433,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           tmem_ld32(tmem + ((quarter * 32) << 16) + b * TC_N + c, r);
           const float4* w4 = reinterpret_cast<const float4*>(a.pw + base + c);
           const float4* v4 = reinterpret_cast<const float4*>(a.pv + base + c);
-          // The near-tie band's test is the looser one (its R is larger, v >= 0,
-          // and thr2 > thr): every survivor is in the band.  So the chunk's
-          // smallest band score decides whether any pair needs a closer look;
-          // the running sum turns NaN or infinite with any score that is (a
-          // NaN score passes the per-pair tests below, never fminf).
-          float m = __int_as_float(0x7f800000), chk = 0.f;
-#pragma unroll
-          for (int j4 = 0; j4 < 8; ++j4) {
-            const float4 w = __ldg(w4 + j4), v = __ldg(v4 + j4);
-            const float ww[4] = {w.x, w.y, w.z, w.w}, vv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              const float x0 = __fmaf_rn(-2.f, __uint_as_float(r[j4 * 4 + u]), ww[u]);
-              const float yb = __fmaf_rn(m2r2, vv[u], x0);
-              m = fminf(m, yb);
-              chk = __fadd_rn(chk, yb);
-            }
-          }
-          if (!active || (m > thr2 && fabsf(chk) < __int_as_float(0x7f800000))) continue;
           uint32_t mask = 0, band = 0;
 #pragma unroll
           for (int j4 = 0; j4 < 8; ++j4) {
@@ -466,6 +447,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
               band |= static_cast<uint32_t>(!(__fmaf_rn(m2r2, vv[u], x0) > thr2)) << j;
             }
           }
+          if (!active) mask = band = 0;
           // survivors, and the pairs the filter rejected inside the near-tie
           // band (farther than the bound): those are noted by their FP32
           // enclosure, and by their exact value when it lies in the window

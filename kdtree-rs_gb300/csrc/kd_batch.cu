@@ -667,6 +667,7 @@ struct Request {
 struct Piece {
   Request* r;
   uint64_t q0, nq;
+  double est_ns;  // estimated GPU time (the tree's calibrated cost per query)
 };
 
 // One batch in flight: device staging, batch buffers, pinned host tables.
@@ -697,8 +698,8 @@ struct kd_server {
   Slot slots[2];
   std::mutex mu;
   std::condition_variable cv;  // queue, slots, completions
-  uint64_t slice = 0;         // largest piece, in queries
-  uint64_t large_budget = 0;  // queries of large requests' pieces one batch admits
+  uint64_t slice = 0;              // largest piece, in queries
+  std::vector<double> ns_per_query;  // per tree: calibrated GPU time of one query (k = 16)
   std::deque<Piece> small_q;  // requests of one piece, arrival order
   std::deque<Piece> large_q;  // pieces of larger requests, arrival order
   std::deque<Slot*> inflight;
@@ -711,10 +712,74 @@ struct kd_server {
 namespace {
 
 constexpr uint64_t SERVER_JOBS = 4096;
-// Largest piece of a request, in queries: a batch holds every waiting small
-// request and at most one slice of the larger ones, so a small request waits
-// for at most about one slice's worth of GPU work ahead of it.
+// Work a batch takes on, and the size of a large request's pieces, in
+// estimated GPU time (a tree's cost per query differs a hundredfold between a
+// 3-wide tree of 1e5 points and a 16-wide one of 4e6): a batch holds every
+// waiting small request and large pieces up to about SERVER_BATCH_NS, so a
+// small request waits for at most about that much GPU work ahead of it.  The
+// largest piece is SERVER_SLICE queries whatever its cost; a large piece that
+// waited SERVER_AGE_NS goes into the next batch regardless.
 constexpr uint64_t SERVER_SLICE = 16384;
+constexpr double SERVER_BATCH_NS = 1.0e6;
+constexpr double SERVER_PIECE_NS = 1.0e6;
+constexpr double SERVER_AGE_NS = 20.0e6;
+
+// Estimated GPU time of nq queries of k results on tree t (cost grows with k).
+double piece_cost(const kd_server* s, uint32_t tree, uint64_t nq, uint64_t k) {
+  return static_cast<double>(nq) * s->ns_per_query[tree] * (0.5 + static_cast<double>(k) / 32.0);
+}
+
+__global__ void k_sample_rows(const double* data, uint64_t n, uint64_t d, uint64_t m, double* out) {
+  const uint64_t f = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  if (f >= m * d) return;
+  const uint64_t r = f / d, j = f - r * d;
+  out[f] = data[(r * (n / m)) * d + j];  // every (n / m)-th row of the tree
+}
+
+// Each tree's cost per query: one timed call of 2048 of its own points (rows
+// spread over the tree) as queries, k = 16, after an untimed one.
+int calibrate(kd_server* s) {
+  s->ns_per_query.assign(s->trees.size(), 0.0);
+  cudaStream_t st;
+  KD_TRY_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int rc = KD_OK;
+  for (size_t i = 0; i < s->trees.size() && !rc; ++i) {
+    const kd_tree* t = s->trees[i];
+    const uint64_t m = std::min<uint64_t>(2048, t->n_points), k = std::min<uint64_t>(16, t->n_points);
+    void* mem = nullptr;
+    const uint64_t bytes = round256(m * t->ndim * 8) + 2 * round256(m * k * 8) + 256;
+    if (dev_alloc(&mem, bytes, st) != cudaSuccess) {
+      cudaGetLastError();
+      rc = fail(KD_ERR_OUT_OF_MEMORY, "device allocation failed");
+      break;
+    }
+    double* q = static_cast<double*>(mem);
+    double* od = reinterpret_cast<double*>(static_cast<char*>(mem) + round256(m * t->ndim * 8));
+    int64_t* oi = reinterpret_cast<int64_t*>(reinterpret_cast<char*>(od) + round256(m * k * 8));
+    uint32_t* status = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(oi) + round256(m * k * 8));
+    k_sample_rows<<<static_cast<unsigned>((m * t->ndim + 255) / 256), 256, 0, st>>>(t->data, t->n_points, t->ndim,
+                                                                                    m, q);
+    QueryParams qp = s->qp;
+    qp.k = k;
+    cudaMemsetAsync(status, 0, 4, st);
+    rc = query_on_device(t, q, m, qp, od, oi, st, status, nullptr);
+    cudaEventRecord(e0, st);
+    if (!rc) rc = query_on_device(t, q, m, qp, od, oi, st, status, nullptr);
+    cudaEventRecord(e1, st);
+    cudaFreeAsync(mem, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess && !rc) rc = cuda_fail(cudaGetLastError(), "calibration");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    s->ns_per_query[i] = std::max(1.0, static_cast<double>(ms) * 1e6 / static_cast<double>(m));
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(st);
+  return rc;
+}
 
 uint64_t host_bytes(const kd_server* s) {
   return round256(s->cap_jobs * sizeof(BatchJob)) + 2 * round256((s->cap_jobs + 1) * 4) +
@@ -797,11 +862,16 @@ void scheduler_loop(kd_server* s) {
     });
     if (empty()) return;  // stopping, nothing left
     // continuous batching: every waiting single-piece request that fits, in
-    // arrival order, then pieces of larger requests up to large_budget queries
+    // arrival order, then pieces of larger requests while the batch's estimated
+    // GPU time stays within SERVER_BATCH_NS (at least one piece when no small
+    // request waits, or when the oldest piece waited SERVER_AGE_NS)
     Slot* sl = free_slot;
     sl->busy = true;
     sl->pieces.clear();
-    uint64_t q = 0, in = 0, out = 0, bins = 0, large = 0;
+    uint64_t q = 0, in = 0, out = 0, bins = 0;
+    double cost = 0.0;
+    int n_large = 0;
+    const Clock::time_point now = Clock::now();
     auto take = [&](std::deque<Piece>& from, bool budget) {
       while (!from.empty() && sl->pieces.size() < s->cap_jobs) {
         const Piece pc = from.front();
@@ -810,12 +880,18 @@ void scheduler_loop(kd_server* s) {
         if (!sl->pieces.empty() && (q + pc.nq > s->cap_q || in + pc.nq * t->ndim > s->cap_in ||
                                     out + pc.nq * pc.r->k > s->cap_out || bins + nb > s->cap_bins))
           return;
-        if (budget && large > 0 && large + pc.nq > s->large_budget) return;
+        if (budget) {
+          const bool first = n_large == 0;
+          const bool aged = std::chrono::duration<double, std::nano>(now - pc.r->t_submit).count() > SERVER_AGE_NS;
+          const bool fits = cost + pc.est_ns <= SERVER_BATCH_NS;
+          if (!(fits || (first && (sl->pieces.empty() || aged)))) return;
+          ++n_large;
+        }
         q += pc.nq;
         in += pc.nq * t->ndim;
         out += pc.nq * pc.r->k;
         bins += nb;
-        if (budget) large += pc.nq;
+        cost += pc.est_ns;
         sl->pieces.push_back(pc);
         from.pop_front();
       }
@@ -1049,7 +1125,6 @@ int kd_server_create(const kd_tree* const* trees, uint64_t n_trees, double p, in
   s->cap_jobs = SERVER_JOBS;
   s->cap_bins = std::max(2 * nodes, nodes_max + SERVER_JOBS);
   s->slice = std::min<uint64_t>(SERVER_SLICE, cap);
-  s->large_budget = s->slice;
   for (Slot& sl : s->slots) {
     char* extra = nullptr;
     const uint64_t extra_b = round256(s->cap_in * 8) + round256(s->cap_out * 8) * 2 + round256(SERVER_JOBS * 4);
@@ -1077,6 +1152,10 @@ int kd_server_create(const kd_tree* const* trees, uint64_t n_trees, double p, in
       return cuda_fail(e, "server set-up");
     }
   }
+  if ((rc = calibrate(s))) {
+    release_server(s);
+    return rc;
+  }
   try {
     s->scheduler = std::thread(scheduler_loop, s);
     s->completer = std::thread(completer_loop, s);
@@ -1095,8 +1174,11 @@ int kd_server_submit(kd_server* s, uint64_t tree, const double* queries, uint64_
   const kd_tree* t = s->trees[tree];
   int rc = job_error(t, n_queries, k, queries, out_distances, out_indices, s->device, "request");
   if (rc) return rc;
-  // a piece must fit one batch: the slice, fewer for wide rows or large k
-  const uint64_t piece = std::min({s->slice, s->cap_in / t->ndim, s->cap_out / k});
+  // a piece must fit one batch: about SERVER_PIECE_NS of estimated GPU time
+  // (256 to SERVER_SLICE queries), fewer for wide rows or large k
+  const double per_q = piece_cost(s, static_cast<uint32_t>(tree), 1, k);
+  const uint64_t by_cost = std::max<uint64_t>(256, static_cast<uint64_t>(SERVER_PIECE_NS / per_q));
+  const uint64_t piece = std::min({s->slice, by_cost, s->cap_in / t->ndim, s->cap_out / k});
   if (piece == 0)
     return fail(KD_ERR_INVALID_ARGUMENT, "k = " + std::to_string(k) + " exceeds the server's batch capacity (" +
                                              std::to_string(s->cap_out) + " results)");
@@ -1119,10 +1201,12 @@ int kd_server_submit(kd_server* s, uint64_t tree, const double* queries, uint64_
     r->ticket = s->next_ticket++;
     s->reqs[r->ticket] = r;
     if (r->pieces_left == 1) {
-      s->small_q.push_back(Piece{r, 0, n_queries});
+      s->small_q.push_back(Piece{r, 0, n_queries, per_q * static_cast<double>(n_queries)});
     } else {
-      for (uint64_t q0 = 0; q0 < n_queries; q0 += piece)
-        s->large_q.push_back(Piece{r, q0, std::min(piece, n_queries - q0)});
+      for (uint64_t q0 = 0; q0 < n_queries; q0 += piece) {
+        const uint64_t nq = std::min(piece, n_queries - q0);
+        s->large_q.push_back(Piece{r, q0, nq, per_q * static_cast<double>(nq)});
+      }
     }
   }
   s->cv.notify_all();

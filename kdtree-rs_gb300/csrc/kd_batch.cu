@@ -508,6 +508,15 @@ int job_error(const kd_tree* tree, uint64_t nq, uint64_t k, const void* q, const
   return KD_OK;
 }
 
+// Rows of a tree spread over it (every (n / m)-th), as queries for the
+// server's calibration.
+__global__ void k_sample_rows(const double* data, uint64_t n, uint64_t d, uint64_t m, double* out) {
+  const uint64_t f = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+  if (f >= m * d) return;
+  const uint64_t r = f / d, j = f - r * d;
+  out[f] = data[(r * (n / m)) * d + j];
+}
+
 }  // namespace
 }  // namespace kd
 
@@ -729,13 +738,6 @@ double piece_cost(const kd_server* s, uint32_t tree, uint64_t nq, uint64_t k) {
   return static_cast<double>(nq) * s->ns_per_query[tree] * (0.5 + static_cast<double>(k) / 32.0);
 }
 
-__global__ void k_sample_rows(const double* data, uint64_t n, uint64_t d, uint64_t m, double* out) {
-  const uint64_t f = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
-  if (f >= m * d) return;
-  const uint64_t r = f / d, j = f - r * d;
-  out[f] = data[(r * (n / m)) * d + j];  // every (n / m)-th row of the tree
-}
-
 // Each tree's cost per query: one timed call of 2048 of its own points (rows
 // spread over the tree) as queries, k = 16, after an untimed one.
 int calibrate(kd_server* s) {
@@ -760,8 +762,8 @@ int calibrate(kd_server* s) {
     double* od = reinterpret_cast<double*>(static_cast<char*>(mem) + round256(m * t->ndim * 8));
     int64_t* oi = reinterpret_cast<int64_t*>(reinterpret_cast<char*>(od) + round256(m * k * 8));
     uint32_t* status = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(oi) + round256(m * k * 8));
-    k_sample_rows<<<static_cast<unsigned>((m * t->ndim + 255) / 256), 256, 0, st>>>(t->data, t->n_points, t->ndim,
-                                                                                    m, q);
+    kd::k_sample_rows<<<static_cast<unsigned>((m * t->ndim + 255) / 256), 256, 0, st>>>(t->data, t->n_points,
+                                                                                        t->ndim, m, q);
     QueryParams qp = s->qp;
     qp.k = k;
     cudaMemsetAsync(status, 0, 4, st);

@@ -231,15 +231,16 @@ void kd_batch_free(kd_batch* batch);
 
 /* ---- Serving: continuous batching over a fixed set of trees --------------
  * No reference counterpart: a request loop in front of `Tree::query`
- * (src/query.rs:29-78).  At creation the server times each tree once (2048
- * of its own points as queries) for an estimate of its GPU time per query.  A
- * request runs as pieces of about 1 ms of that estimated time (256 to 16,384
- * queries, fewer for large k).  A scheduler thread forms a batch whenever one
- * of two batch slots is free: every waiting single-piece request that fits the
- * slot, in arrival order, then pieces of larger requests while the batch's
- * estimated time stays within about 1 ms (one piece at least when no small
- * request waits, or when a piece has waited 20 ms), so a small request waits
- * for about a millisecond of other work, not a large request's whole scan.
+ * (src/query.rs:29-78).  At creation the server times each tree once (up to
+ * 32,768 of its own points as queries) for an estimate of its GPU time per
+ * query.  A request runs as pieces of about 2 ms of that estimated time
+ * (2,048 to 16,384 queries, fewer for large k).  A scheduler thread forms a
+ * batch whenever one of two batch slots is free: every waiting single-piece
+ * request that fits the slot, in arrival order, then pieces of larger
+ * requests while the batch's estimated time stays within about 3 ms (one
+ * piece at least when no small request waits, or when a piece has waited
+ * 20 ms), so a small request waits for a few milliseconds of other work, not
+ * a large request's whole scan.
  * A batch runs the kernels of kd_batch_run (plus per-request launches for
  * requests outside the fused kernel).  A request's results are exactly
  * kd_query's for the same tree and queries, whatever it is batched with. */

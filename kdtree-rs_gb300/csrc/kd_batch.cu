@@ -729,8 +729,9 @@ constexpr uint64_t SERVER_JOBS = 4096;
 // largest piece is SERVER_SLICE queries whatever its cost; a large piece that
 // waited SERVER_AGE_NS goes into the next batch regardless.
 constexpr uint64_t SERVER_SLICE = 16384;
-constexpr double SERVER_BATCH_NS = 1.0e6;
-constexpr double SERVER_PIECE_NS = 1.0e6;
+constexpr double SERVER_BATCH_NS = 3.0e6;
+constexpr double SERVER_PIECE_NS = 2.0e6;
+constexpr uint64_t SERVER_MIN_PIECE = 2048;  // below this a batch cannot fill the GPU
 constexpr double SERVER_AGE_NS = 20.0e6;
 
 // Estimated GPU time of nq queries of k results on tree t (cost grows with k).
@@ -738,8 +739,9 @@ double piece_cost(const kd_server* s, uint32_t tree, uint64_t nq, uint64_t k) {
   return static_cast<double>(nq) * s->ns_per_query[tree] * (0.5 + static_cast<double>(k) / 32.0);
 }
 
-// Each tree's cost per query: one timed call of 2048 of its own points (rows
-// spread over the tree) as queries, k = 16, after an untimed one.
+// Each tree's cost per query at a batch size that fills the GPU: one timed
+// call of up to 32768 of its own points (rows spread over the tree) as
+// queries, k = 16, after an untimed one.
 int calibrate(kd_server* s) {
   s->ns_per_query.assign(s->trees.size(), 0.0);
   cudaStream_t st;
@@ -750,7 +752,7 @@ int calibrate(kd_server* s) {
   int rc = KD_OK;
   for (size_t i = 0; i < s->trees.size() && !rc; ++i) {
     const kd_tree* t = s->trees[i];
-    const uint64_t m = std::min<uint64_t>(2048, t->n_points), k = std::min<uint64_t>(16, t->n_points);
+    const uint64_t m = std::min<uint64_t>(32768, t->n_points), k = std::min<uint64_t>(16, t->n_points);
     void* mem = nullptr;
     const uint64_t bytes = round256(m * t->ndim * 8) + 2 * round256(m * k * 8) + 256;
     if (dev_alloc(&mem, bytes, st) != cudaSuccess) {
@@ -1179,7 +1181,7 @@ int kd_server_submit(kd_server* s, uint64_t tree, const double* queries, uint64_
   // a piece must fit one batch: about SERVER_PIECE_NS of estimated GPU time
   // (256 to SERVER_SLICE queries), fewer for wide rows or large k
   const double per_q = piece_cost(s, static_cast<uint32_t>(tree), 1, k);
-  const uint64_t by_cost = std::max<uint64_t>(256, static_cast<uint64_t>(SERVER_PIECE_NS / per_q));
+  const uint64_t by_cost = std::max<uint64_t>(SERVER_MIN_PIECE, static_cast<uint64_t>(SERVER_PIECE_NS / per_q));
   const uint64_t piece = std::min({s->slice, by_cost, s->cap_in / t->ndim, s->cap_out / k});
   if (piece == 0)
     return fail(KD_ERR_INVALID_ARGUMENT, "k = " + std::to_string(k) + " exceeds the server's batch capacity (" +

@@ -233,11 +233,11 @@ void kd_batch_free(kd_batch* batch);
  * No reference counterpart: a request loop in front of `Tree::query`
  * (src/query.rs:29-78).  At creation the server times each tree once (up to
  * 32,768 of its own points as queries) for an estimate of its GPU time per
- * query.  A request runs as pieces of about 2 ms of that estimated time
- * (2,048 to 16,384 queries, fewer for large k).  A scheduler thread forms a
+ * query.  A request runs as pieces of about 4 ms of that estimated time
+ * (4,096 to 16,384 queries, fewer for large k).  A scheduler thread forms a
  * batch whenever one of two batch slots is free: every waiting single-piece
  * request that fits the slot, in arrival order, then pieces of larger
- * requests while the batch's estimated time stays within about 3 ms (one
+ * requests while the batch's estimated time stays within about 5 ms (one
  * piece at least when no small request waits, or when a piece has waited
  * 20 ms), so a small request waits for a few milliseconds of other work, not
  * a large request's whole scan.

@@ -729,9 +729,9 @@ constexpr uint64_t SERVER_JOBS = 4096;
 // largest piece is SERVER_SLICE queries whatever its cost; a large piece that
 // waited SERVER_AGE_NS goes into the next batch regardless.
 constexpr uint64_t SERVER_SLICE = 16384;
-constexpr double SERVER_BATCH_NS = 3.0e6;
-constexpr double SERVER_PIECE_NS = 2.0e6;
-constexpr uint64_t SERVER_MIN_PIECE = 2048;  // below this a batch cannot fill the GPU
+constexpr double SERVER_BATCH_NS = 5.0e6;
+constexpr double SERVER_PIECE_NS = 4.0e6;
+constexpr uint64_t SERVER_MIN_PIECE = 4096;  // below this a batch cannot fill the GPU
 constexpr double SERVER_AGE_NS = 20.0e6;
 
 // Estimated GPU time of nq queries of k results on tree t (cost grows with k).

@@ -81,7 +81,7 @@ def test_bad_request_fails_alone():
 
 
 def test_large_requests_run_in_pieces_beside_small_ones():
-    """Requests above the piece size (about 2 ms of the tree's estimated GPU
+    """Requests above the piece size (about 4 ms of the tree's estimated GPU
     time, at most 16,384 queries) run as several pieces that small requests
     overtake; each result still equals a lone query, and a non-finite query in
     any piece fails the whole request."""

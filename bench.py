@@ -210,18 +210,26 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes (read + write) of one launch of the query kernel on this
-    workload, from the committed ncu summary (`traffic_bytes_per_launch: N`)."""
-    p = ROOT / "profiles" / "k_query_packet_uniform_n1m_d3_k16.md"
-    if p.exists():
-        for line in p.read_text().splitlines():
-            if line.strip().startswith("traffic_bytes_per_launch:"):
-                try:
-                    return int(line.split(":", 1)[1].strip().split()[0])
-                except ValueError:
-                    return None
-    return None
+def profiled_inputs():
+    """The roofline's ncu-measured inputs (profiles/roofline_inputs.json: DRAM
+    traffic per launch of the query kernel on this workload, L2 hit rates of it
+    and of the build), each with the commit it was measured at and whether the
+    kernel's sources have changed since (then the figure is stale)."""
+    import hashlib
+
+    p = ROOT / "profiles" / "roofline_inputs.json"
+    if not p.exists():
+        return None
+    j = json.loads(p.read_text())
+    for key in ("k_query_packet", "build"):
+        e = j.get(key)
+        if not e:
+            continue
+        h = hashlib.sha256()
+        for f in e.get("source_files", []):
+            h.update((ROOT / f).read_bytes())
+        e["stale"] = h.hexdigest()[:16] != e.get("source_sha16")
+    return j
 
 
 def run_reference(args):
@@ -278,11 +286,14 @@ def build_line(build_s, cpu_s, hbm_peak):
         levels += 1
     b = levels * N_POINTS * (3 * 8 * DIM + 8)
     gbs = b / build_s / 1e9
+    pb = (profiled_inputs() or {}).get("build", {})
     return {"gpu_s": build_s, "cpu_oracle_s": cpu_s, "levels": levels, "algorithmic_bytes": b,
             "achieved_gbs": gbs, "frac_of_hbm": gbs / hbm_peak if hbm_peak else None,
+            "l2_hit_rate_pct": pb.get("l2_hit_rate_pct_time_weighted"), "l2_stale": pb.get("stale"),
             "note": "host wall time of kd_build incl. the 24 MB upload; oracle build on all host cores; "
-                    "per level the build is a few dependent launches over L2-resident data, so it is "
-                    "launch- and latency-bound, not HBM-bound"}
+                    "the top levels run a chain of dependent launches and the rest one kernel over "
+                    "L2-resident data (L2 hit rate: time-weighted over the build's ncu-captured launches), "
+                    "so it is launch- and latency-bound, not HBM-bound"}
 
 
 def path_lib():
@@ -1067,7 +1078,9 @@ def main():
         # the launching stream around it), averaged over the timed steps
         mean_s = (sum(kernel_ms) / len(kernel_ms) / 1e3) if min(kernel_ms) > 0 else total_s / args.steps
         achieved = per_launch / mean_s / 1e9
-        traffic = profiled_traffic()
+        prof = profiled_inputs() or {}
+        pk = prof.get("k_query_packet", {})
+        traffic = pk.get("traffic_bytes_per_launch")
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                     "traffic": traffic, "peak_kind": peak_kind,
                     "algorithmic_bytes_per_launch": per_launch,
@@ -1077,7 +1090,10 @@ def main():
                     "compulsory_bytes_per_launch": compulsory_bytes(),
                     "traffic_over_compulsory": (traffic / compulsory_bytes()) if traffic else None,
                     "kernel": "k_query_packet<L2, d=3, K=16>", "kernel_ms": mean_s * 1e3,
-                    "traffic_note": "DRAM read+write bytes per launch from ncu (profiles/)"}
+                    "traffic_note": "DRAM read+write bytes per launch from ncu on this workload",
+                    "traffic_source": {"file": "profiles/roofline_inputs.json", "commit": prof.get("commit"),
+                                       "stale": pk.get("stale")},
+                    "l2_hit_rate_pct": pk.get("l2_hit_rate_pct")}
     line = {
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,

@@ -469,6 +469,8 @@ def batched_case(torch, dev, stream, reps=5):
         s = (time.perf_counter() - t0) / reps
         out[name] = {"qps": total_q / s, "ms": s * 1e3}
         results[name] = [(j[3].clone(), j[4].clone()) for j in jobs[:16]]
+        if name == "graph":  # the first graph run tuned the plan
+            out["autotuner"] = plan.choice()
     out["identical_across_modes"] = all(
         torch.equal(a[0], b[0]) and torch.equal(a[1], b[1])
         for other in ("fused_no_graph", "per_tree_launches") for a, b in zip(results["graph"], results[other]))
@@ -694,7 +696,7 @@ def compact_cases(cases):
     if ba:
         out["batched"] = {"graph_qps": _sig(ba["graph"]["qps"], 3),
                           "per_tree_qps": _sig(ba["per_tree_launches"]["qps"], 3),
-                          "identical": ba.get("identical_across_modes")}
+                          "identical": ba.get("identical_across_modes"), "autotuner": ba.get("autotuner")}
     sv = cases.get("serving")
     if sv:
         out["serving"] = {"peak_qps": _sig(sv["peak"]["queries_per_s"], 3),

@@ -224,6 +224,12 @@ enum kd_batch_mode {
 /* Run every job of the plan on `stream` and return once the work has finished
  * (a non-finite query in any job: KD_ERR_NONFINITE_DATA after all jobs ran). */
 int kd_batch_run(kd_batch* batch, void* stream);
+
+/* What the first graph run's autotuner chose (before it: the defaults):
+ * the persistent grid in CTAs, whether queries are sorted by landing leaf,
+ * and the widths whose jobs with k <= 4 run as packet tasks (bit 0: width 2,
+ * bit 1: 3, bit 2: 8) instead of one query a warp.  Any pointer may be NULL. */
+int kd_batch_choice(const kd_batch* batch, unsigned* blocks, int* sorted, unsigned* packet_widths);
 int kd_batch_run_mode(kd_batch* batch, void* stream, int mode);
 
 /* Release a plan (NULL is ignored). */

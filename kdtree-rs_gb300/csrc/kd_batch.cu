@@ -57,7 +57,11 @@ namespace {
 
 constexpr uint32_t CLS_OTHER = 0xffffffffu;
 constexpr uint64_t SORT_MIN_QUERIES = 1024;
-constexpr uint32_t TASK_QUERIES = 4;  // queries per task: one after another on one warp
+constexpr uint32_t TASK_QUERIES = 4;  // queries per warp-traversal task: one after another on one warp
+constexpr uint32_t PACKET_TASK = 32;  // queries per packet task: one per lane
+// Packet classes (the packet traversal, k-best lists in registers):
+// CLS_PACKET + 2 * width index + (k > 1 ? 1 : 0), for k <= 4.
+constexpr uint32_t CLS_PACKET = 8;
 
 // Class of a job in the fused kernel (width index, + 4 for k > 32: two list
 // slots per lane), or CLS_OTHER.
@@ -85,9 +89,14 @@ bool reference_order_forced() {
 struct BatchJob {
   QArgs a;             // the job's query arguments; a.order points into the batch order or is NULL
   uint64_t bin_start;  // the job's first landing-leaf bin
-  uint32_t cls;        // packet class
+  uint32_t cls;        // fused class (warp traversal 0-7, packet traversal CLS_PACKET + ...)
   uint32_t sorted;     // 1: bins per node (sorted by landing leaf); 0: one bin
 };
+
+// Queries per task of a job of class cls.
+__host__ __device__ __forceinline__ uint32_t task_queries(uint32_t cls) {
+  return cls >= CLS_PACKET ? PACKET_TASK : TASK_QUERIES;
+}
 
 struct BatchArgs {
   const BatchJob* jobs;
@@ -144,9 +153,11 @@ __device__ __forceinline__ void batch_query(const QArgs* a, uint64_t w, WarpStac
   warp_query<M, D, KS>(*a, w, stack, nullptr);
 }
 
-// The persistent kernel: warps take tasks -- TASK_QUERIES consecutive
-// positions of one job -- until none is left, and run each query with the
-// warp-per-query traversal (kd_query_warp.cuh) for the job's width.  W16: the
+// The persistent kernel: warps take tasks until none is left -- TASK_QUERIES
+// consecutive positions of one job, each run with the warp-per-query traversal
+// (kd_query_warp.cuh) for the job's width, or, for the packet classes, 32
+// consecutive positions of the job's landing-leaf order run together by the
+// packet traversal (kd_query_packet.cuh; k <= 4, lists in registers).  W16: the
 // batch holds 16-wide jobs; without them the kernel is held to 72 registers,
 // 7 blocks an SM instead of 5 (measured faster on the mixed 2/3/8-wide batch
 // than the 87 registers the compiler picks unbounded).
@@ -161,6 +172,20 @@ __global__ void __launch_bounds__(QUERY_THREADS, W16 ? 5 : 7) k_query_batch(Batc
     if (t >= b.n_tasks) return;
     const uint32_t j = find_range(b.task_start, b.n_jobs, t);
     const BatchJob* J = b.jobs + j;
+    if (J->cls >= CLS_PACKET) {
+      // the warp's own stack words (its WarpStack is free during a packet task)
+      uint32_t* stack = s_stack[wid].node;
+      const uint64_t tid = static_cast<uint64_t>(t - b.task_start[j]) * PACKET_TASK + lane;
+      switch (J->cls - CLS_PACKET) {
+        case 0: packet_queries<M, 2, 1>(J->a, tid, nullptr, nullptr, nullptr, stack); break;
+        case 1: packet_queries<M, 2, 4>(J->a, tid, nullptr, nullptr, nullptr, stack); break;
+        case 2: packet_queries<M, 3, 1>(J->a, tid, nullptr, nullptr, nullptr, stack); break;
+        case 3: packet_queries<M, 3, 4>(J->a, tid, nullptr, nullptr, nullptr, stack); break;
+        case 4: packet_queries<M, 8, 1>(J->a, tid, nullptr, nullptr, nullptr, stack); break;
+        default: packet_queries<M, 8, 4>(J->a, tid, nullptr, nullptr, nullptr, stack); break;
+      }
+      continue;
+    }
     const uint64_t first = static_cast<uint64_t>(t - b.task_start[j]) * TASK_QUERIES;
     const uint64_t last = min(first + TASK_QUERIES, J->a.nq);
     for (uint64_t w = first; w < last; ++w) {
@@ -197,15 +222,17 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_batch_rerun(const BatchJob* j
     const uint64_t e = list[w];
     const BatchJob* J = jobs + (e >> 32);
     const uint64_t qi = static_cast<uint32_t>(e);
+    // the warp class of the job (a packet class: its width, one list slot a lane)
+    const uint32_t wc = J->cls >= CLS_PACKET ? (J->cls - CLS_PACKET) / 2 : J->cls;
     bool stands;
-    switch (J->cls & 3) {  // widths 2, 3, 8, 16 (the class's low bits)
+    switch (wc & 3) {  // widths 2, 3, 8, 16 (the class's low bits)
       case 0: stands = ref_results_stand<M, 2>(J->a, qi); break;
       case 1: stands = ref_results_stand<M, 3>(J->a, qi); break;
       case 2: stands = ref_results_stand<M, 8>(J->a, qi); break;
       default: stands = ref_results_stand<M, 16>(J->a, qi); break;
     }
     if (stands) continue;
-    switch (J->cls) {
+    switch (wc) {
       case 0: ref_query<M, 2, 1>(J->a, qi, s_fr[wid], s_axes[wid], nullptr); break;
       case 1: ref_query<M, 3, 1>(J->a, qi, s_fr[wid], s_axes[wid], nullptr); break;
       case 2: ref_query<M, 8, 1>(J->a, qi, s_fr[wid], s_axes[wid], nullptr); break;
@@ -296,8 +323,10 @@ void fill_args(QArgs* a, const JobSpec& J, const QueryParams& qp) {
 // u32); sort = false gives every job one bin and no order.  The fused jobs
 // flag their near ties into (rerun_count, rerun_list), tagged with their
 // position in the table.
+// packet_widths: bit w (width index: 2, 3, 8) set -- that width's jobs with
+// k <= 4 run as packet tasks.
 void make_layout(const std::vector<JobSpec>& specs, const QueryParams& qp, bool sort, uint32_t* order,
-                 uint32_t* rerun_count, uint64_t* rerun_list, Layout* L) {
+                 uint32_t* rerun_count, uint64_t* rerun_list, Layout* L, uint32_t packet_widths = 0) {
   *L = Layout{};
   const bool ref = reference_order_forced();
   std::vector<uint32_t> cls(specs.size());
@@ -324,12 +353,14 @@ void make_layout(const std::vector<JobSpec>& specs, const QueryParams& qp, bool 
     B.a.rerun_tag = static_cast<uint32_t>(i);
     B.cls = cls[L->packet[i]];
     L->wide16 |= B.cls % 4 == 3;
+    if (B.cls < 3 && J.k <= 4 && ((packet_widths >> B.cls) & 1u)) B.cls = CLS_PACKET + 2 * B.cls + (J.k > 1 ? 1 : 0);
     B.sorted = sort && J.nq >= SORT_MIN_QUERIES;
     B.a.order = B.sorted ? order + L->q_start[i] : nullptr;
     B.bin_start = bins;
     bins += B.sorted ? J.tree->n_nodes : 1;
     L->q_start[i + 1] = L->q_start[i] + static_cast<uint32_t>(J.nq);
-    L->task_start[i + 1] = L->task_start[i] + static_cast<uint32_t>((J.nq + TASK_QUERIES - 1) / TASK_QUERIES);
+    const uint32_t tq = task_queries(B.cls);
+    L->task_start[i + 1] = L->task_start[i] + static_cast<uint32_t>((J.nq + tq - 1) / tq);
   }
   L->n_bins = std::max<uint64_t>(bins, 1);
   L->total_q = L->q_start[n];
@@ -539,6 +570,7 @@ struct kd_batch {
   bool tuned = false;
   unsigned blocks = 0;
   int table = 0;
+  uint32_t packet_widths = 0;  // widths (bit: index of 2, 3, 8) whose k <= 4 jobs run as packet tasks
   SideStreams side;
   cudaStream_t capture_stream = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -574,8 +606,26 @@ int finish_plan(kd_batch* b, cudaStream_t st) {
   return KD_OK;
 }
 
+// Lay the fused jobs out again with packet_widths and upload the tables (the
+// jobs and task ranges change; the query ranges and the other jobs do not).
+int apply_layouts(kd_batch* b, uint32_t packet_widths) {
+  for (int t = 0; t < 2; ++t)
+    make_layout(b->specs, b->qp, t == 0, b->buf.order, b->buf.rerun_count, b->buf.rerun_list, &b->layout[t],
+                packet_widths);
+  const size_t np = b->layout[0].packet.size();
+  if (np) {
+    KD_TRY_CUDA(cudaMemcpy(b->buf.jobs[0], b->layout[0].table.data(), np * sizeof(BatchJob), cudaMemcpyHostToDevice));
+    KD_TRY_CUDA(cudaMemcpy(b->buf.jobs[1], b->layout[1].table.data(), np * sizeof(BatchJob), cudaMemcpyHostToDevice));
+    KD_TRY_CUDA(cudaMemcpy(b->buf.task_start, b->layout[0].task_start.data(), (np + 1) * 4, cudaMemcpyHostToDevice));
+  }
+  b->packet_widths = packet_widths;
+  return KD_OK;
+}
+
 // The autotuner: every candidate launch shape runs the plan once to warm up
-// and twice timed; the fastest is kept.  Results are identical for all.
+// and twice timed; the fastest is kept.  Then, width by width (2, 3, 8), the
+// jobs with k <= 4 run as packet tasks instead of warp tasks, kept where that is
+// faster.  Results are identical for all.
 int tune(kd_batch* b, cudaStream_t st) {
   const int per_sm = resident_blocks_per_sm(b->qp.metric, b->layout[0].wide16);
   std::vector<unsigned> grids;
@@ -611,6 +661,30 @@ int tune(kd_batch* b, cudaStream_t st) {
         b->table = table;
       }
     }
+  }
+  auto time_plan = [&](float* t_min) {
+    *t_min = 1e30f;
+    for (int rep = 0; rep < 3 && rc == KD_OK; ++rep) {
+      cudaEventRecord(e0, st);
+      rc = enqueue_plan(b, st, false, b->blocks, b->table);
+      cudaEventRecord(e1, st);
+      if (rc == KD_OK) rc = finish_plan(b, st);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) *t_min = std::min(*t_min, ms);
+    }
+  };
+  for (uint32_t w = 0; w < 3 && rc == KD_OK; ++w) {
+    bool present = false;
+    for (const BatchJob& J : b->layout[0].table) present |= J.cls == w && J.a.k <= 4;
+    if (!present) continue;
+    const uint32_t keep = b->packet_widths;
+    if ((rc = apply_layouts(b, keep | (1u << w)))) break;
+    float t = 1e30f;
+    time_plan(&t);
+    if (rc != KD_OK) break;
+    if (t < best) best = t;
+    else rc = apply_layouts(b, keep);
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -1079,6 +1153,14 @@ int kd_batch_run_mode(kd_batch* b, void* stream, int mode) {
 }
 
 int kd_batch_run(kd_batch* b, void* stream) { return kd_batch_run_mode(b, stream, KD_BATCH_GRAPH); }
+
+int kd_batch_choice(const kd_batch* b, unsigned* blocks, int* sorted, unsigned* packet_widths) {
+  if (!b) return fail(KD_ERR_INVALID_ARGUMENT, "batch is NULL");
+  if (blocks) *blocks = b->blocks;
+  if (sorted) *sorted = b->table == 0;
+  if (packet_widths) *packet_widths = b->packet_widths;
+  return KD_OK;
+}
 
 void kd_batch_free(kd_batch* b) { release_plan(b); }
 

@@ -189,11 +189,10 @@ struct PacketSmem {
 // The 32 lanes of a warp run the sorted batch positions tid (one per lane) of
 // the queries described by `a`; every lane of the warp must call it together.
 // s_lo / s_hi / s_row: the block's heap arrays, K * QUERY_THREADS words each
-// (unused for K < 8); s_stack: the block's node stacks, PACKET_STACK words per
-// warp.
+// (unused for K < 8); stack: this warp's node stack, PACKET_STACK words.
 template <int M, int D, int K>
 __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, float* s_lo, float* s_hi,
-                                               uint32_t* s_row, uint32_t* s_stack) {
+                                               uint32_t* s_row, uint32_t* stack) {
   static_assert(D > 0 && M != M_LP, "packet path: compile-time width, metric without pow()");
 #ifdef KD_WORK_COUNTS
   long long kd_t_ = clock64();
@@ -293,7 +292,6 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
   // Every lane pushes the same ids to the same words and pops what it pushed
   // itself, so no lane depends on another's store.  An entered inner node
   // stacks its far child and continues with the near one.
-  uint32_t* stack = s_stack + (threadIdx.x >> 5) * PACKET_STACK;
   int sp = 0;
   uint32_t node = 0;  // the node at hand; the near child follows an entered node without a push
   KD_PHASE(11);
@@ -423,7 +421,7 @@ template <int M, int D, int K>
 __global__ void __launch_bounds__(QUERY_THREADS) k_query_packet(QArgs a) {
   __shared__ PacketSmem<K> sm;
   packet_queries<M, D, K>(a, blockIdx.x * static_cast<uint64_t>(QUERY_THREADS) + threadIdx.x, sm.lo, sm.hi,
-                          sm.row, sm.stack);
+                          sm.row, sm.stack + (threadIdx.x >> 5) * PACKET_STACK);
 }
 
 // The same with the shared memory supplied at launch (sizeof(PacketSmem<K>)
@@ -433,5 +431,5 @@ __global__ void __launch_bounds__(QUERY_THREADS) k_query_packet_dyn(QArgs a) {
   extern __shared__ __align__(16) unsigned char packet_dyn[];
   PacketSmem<K>* sm = reinterpret_cast<PacketSmem<K>*>(packet_dyn);
   packet_queries<M, D, K>(a, blockIdx.x * static_cast<uint64_t>(QUERY_THREADS) + threadIdx.x, sm->lo, sm->hi,
-                          sm->row, sm->stack);
+                          sm->row, sm->stack + (threadIdx.x >> 5) * PACKET_STACK);
 }

@@ -71,6 +71,9 @@ def _load():
     L.kd_batch_run_mode.restype = ctypes.c_int
     L.kd_batch_free.argtypes = [P]
     L.kd_batch_free.restype = None
+    L.kd_batch_choice.argtypes = [P, ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_int),
+                                  ctypes.POINTER(ctypes.c_uint)]
+    L.kd_batch_choice.restype = ctypes.c_int
     L.kd_server_create.argtypes = [P, u64, d, ctypes.c_int, d, d, u64, ctypes.POINTER(P)]
     L.kd_server_create.restype = ctypes.c_int
     L.kd_server_submit.argtypes = [P, u64, P, u64, u64, P, P, ctypes.POINTER(u64)]
@@ -369,6 +372,17 @@ class BatchQuery:
         st = _lib.kd_batch_run_mode(self._h, ctypes.c_void_p(s) if s else None, int(mode))
         if st != KD_OK:
             _raise(st)
+
+    def choice(self) -> dict:
+        """The autotuner's choice (kd_batch_choice): persistent grid in CTAs,
+        sorting by landing leaf, and the widths whose k <= 4 jobs run as
+        packet tasks."""
+        blocks, srt, pw = ctypes.c_uint(), ctypes.c_int(), ctypes.c_uint()
+        st = _lib.kd_batch_choice(self._h, ctypes.byref(blocks), ctypes.byref(srt), ctypes.byref(pw))
+        if st != KD_OK:
+            _raise(st)
+        return {"blocks": blocks.value, "sorted": bool(srt.value),
+                "packet_widths": [w for b, w in enumerate((2, 3, 8)) if (pw.value >> b) & 1]}
 
     def __del__(self):
         h = getattr(self, "_h", None)

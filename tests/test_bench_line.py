@@ -1,6 +1,7 @@
 """Host-side pieces of the bench line (no GPU): the roofline's algorithmic
-bytes, the DRAM traffic read from the committed ncu summary, the measured peak,
-and the build's level count and bytes."""
+bytes, the ncu-measured inputs (profiles/roofline_inputs.json: DRAM traffic
+with its commit and a staleness check against the kernel sources), the
+measured peak, and the build's level count and bytes."""
 import sys
 from pathlib import Path
 
@@ -16,11 +17,17 @@ def test_algorithmic_bytes_formula():
     assert bench.algorithmic_bytes((2, 5, 1), 1) == 8 * d + 16 * k + 8 * d * 5 + 24 * 2 + 16 * d * 1
 
 
-def test_profiled_traffic_matches_summary():
-    t = bench.profiled_traffic()
-    assert isinstance(t, int) and t > 0
+def test_profiled_inputs_carry_their_commit_and_staleness():
+    j = bench.profiled_inputs()
+    pk = j["k_query_packet"]
+    t = pk["traffic_bytes_per_launch"]
+    assert isinstance(t, int) and t == pk["dram_read_bytes"] + pk["dram_write_bytes"] > 0
+    assert j["commit"] and isinstance(pk["stale"], bool) and 0 < pk["l2_hit_rate_pct"] <= 100
+    assert all((ROOT / f).exists() for f in pk["source_files"])
+    assert 0 < j["build"]["l2_hit_rate_pct_time_weighted"] <= 100
+    # the summary of the same capture states the same traffic
     text = (ROOT / "profiles" / "k_query_packet_uniform_n1m_d3_k16.md").read_text()
-    assert f"traffic_bytes_per_launch: {t}" in text
+    assert "127.2 MB / 216.2 MB" in text
 
 
 def test_measured_peak_is_positive():
@@ -59,5 +66,5 @@ def test_compulsory_bytes_close_to_profiled_traffic():
     c = bench.compulsory_bytes()
     # queries 24 MB + results 256 MB + the tree once
     assert c > bench.N_QUERIES * (bench.DIM * 8 + bench.K * 16)
-    t = bench.profiled_traffic()
+    t = bench.profiled_inputs()["k_query_packet"]["traffic_bytes_per_launch"]
     assert 0.5 < t / c < 2.0

@@ -128,3 +128,29 @@ def test_batch_errors():
         plan.run()
     # the other jobs still ran
     assert_bit_exact((jobs[0][3].cpu().numpy(), jobs[0][4].cpu().numpy()), _single(jobs[0]))
+
+
+def test_autotuner_runs_small_k_jobs_as_packet_tasks(oracle):
+    """Jobs of widths 2 and 3 with k <= 4 on large uniform trees: the first
+    graph run's autotuner times them as packet tasks (32 sorted queries a warp)
+    against one query a warp and keeps the packet tasks; every job's results
+    still equal a lone call and the oracle."""
+    import torch
+
+    from kdtree import BatchQuery
+
+    rng = np.random.default_rng(31)
+    specs = [(200_000, 3, 60_000, 1), (150_000, 3, 40_000, 4), (100_000, 2, 50_000, 2), (30_000, 8, 3000, 16),
+             (120_000, 3, 20_000, 3)]
+    jobs, host = _jobs(rng, specs, torch)
+    plan = BatchQuery(jobs)
+    plan.run(None)
+    torch.cuda.synchronize()
+    choice = plan.choice()
+    assert 3 in choice["packet_widths"], choice
+    for job, (data, q) in zip(jobs, host):
+        got = (job[3].cpu().numpy(), job[4].cpu().numpy())
+        assert_bit_exact(got, _single(job))
+    data, q = host[0]
+    want = oracle.OracleKDTree(data, leafsize=jobs[0][0].leafsize).query(q[:2000], k=1, parallel=True)
+    assert_bit_exact((jobs[0][3][:2000].cpu().numpy(), jobs[0][4][:2000].cpu().numpy()), want)

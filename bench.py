@@ -431,14 +431,9 @@ def precision_cases(lib, torch, stream, dev, cpu_threads):
     return out
 
 
-def batched_case(torch, dev, stream, reps=5):
-    """Config 4: 256 trees, N log-uniform in [1e3, 5e5], d in {2, 3, 8}, uniform
-    [0,1)^d points, leafsize 32 (the reference's default); per tree Q queries,
-    Q log-uniform in [1, 5e4], k in {1, 4, 32}, L2; one seed (400) for the whole
-    draw.  Total queries/s of the batch plan: one CUDA graph holding the sort
-    and ONE persistent query launch, the same launches without the graph, and
-    per-tree launches (one kd_query_device launch sequence per tree)."""
-    from kdtree import BatchQuery, KDTree, _core
+def batched_jobs(torch, dev):
+    """The config-4 draw (batched_case): [(d, k, (tree, device queries, k, out_d, out_i))]."""
+    from kdtree import KDTree
 
     rng = np.random.default_rng(400)
     n_trees = 256
@@ -447,16 +442,68 @@ def batched_case(torch, dev, stream, reps=5):
     qs = np.exp(rng.uniform(np.log(1.0), np.log(5e4), n_trees)).astype(np.int64)
     ks = rng.choice([1, 4, 32], n_trees)
     jobs = []
-    t0 = time.perf_counter()
     for n, d, nq, k in zip(ns, ds, qs, ks):
         tree = KDTree(rng.uniform(size=(int(n), int(d))))
         dq = torch.from_numpy(rng.uniform(size=(int(nq), int(d)))).to(dev)
-        jobs.append((tree, dq, int(k), torch.empty((int(nq), int(k)), dtype=torch.float64, device=dev),
-                     torch.empty((int(nq), int(k)), dtype=torch.int64, device=dev)))
+        jobs.append((int(d), int(k), (tree, dq, int(k), torch.empty((int(nq), int(k)), dtype=torch.float64,
+                                                                  device=dev),
+                                      torch.empty((int(nq), int(k)), dtype=torch.int64, device=dev))))
+    return jobs
+
+
+def batched_classes(torch, dev, stream, reps=5):
+    """Config 4 split by (d, k) class: each class's jobs as a plan of their own
+    (graph mode, after the tuning run), ms per run and the tuner's choice; the
+    whole batch for comparison.  Classes overlap one another in the whole
+    batch, so their times add up to more than its time."""
+    from kdtree import BatchQuery, _core
+
+    jobs = batched_jobs(torch, dev)
+
+    def timed(js):
+        plan = BatchQuery(js)
+        for _ in range(2):
+            plan.run(stream, _core.BATCH_GRAPH)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            plan.run(stream, _core.BATCH_GRAPH)
+        torch.cuda.synchronize()
+        s = (time.perf_counter() - t0) / reps
+        choice = plan.choice()
+        del plan
+        return s, choice
+
+    out = {}
+    s, choice = timed([j for _, _, j in jobs])
+    nq = sum(j[1].shape[0] for _, _, j in jobs)
+    out["all"] = {"queries": nq, "ms": s * 1e3, "qps": nq / s, "choice": choice}
+    for d in (2, 3, 8):
+        for k in (1, 4, 32):
+            js = [j for dj, kj, j in jobs if dj == d and kj == k]
+            if not js:
+                continue
+            nq = sum(j[1].shape[0] for j in js)
+            s, choice = timed(js)
+            out[f"d{d}_k{k}"] = {"jobs": len(js), "queries": nq, "ms": s * 1e3, "qps": nq / s, "choice": choice}
+    return out
+
+
+def batched_case(torch, dev, stream, reps=5):
+    """Config 4: 256 trees, N log-uniform in [1e3, 5e5], d in {2, 3, 8}, uniform
+    [0,1)^d points, leafsize 32 (the reference's default); per tree Q queries,
+    Q log-uniform in [1, 5e4], k in {1, 4, 32}, L2; one seed (400) for the whole
+    draw.  Total queries/s of the batch plan: one CUDA graph holding the sort
+    and ONE persistent query launch, the same launches without the graph, and
+    per-tree launches (one kd_query_device launch sequence per tree)."""
+    from kdtree import BatchQuery, _core
+
+    t0 = time.perf_counter()
+    jobs = [j for _, _, j in batched_jobs(torch, dev)]
     build_s = time.perf_counter() - t0
     plan = BatchQuery(jobs)
-    total_q = int(qs.sum())
-    out = {"trees": n_trees, "points": int(ns.sum()), "queries": total_q, "build_all_s": build_s}
+    total_q = sum(j[1].shape[0] for j in jobs)
+    out = {"trees": len(jobs), "points": sum(j[0].n_points for j in jobs), "queries": total_q, "build_all_s": build_s}
     results = {}
     for name, mode in (("graph", _core.BATCH_GRAPH), ("fused_no_graph", _core.BATCH_FUSED),
                        ("per_tree_launches", _core.BATCH_PER_JOB)):
@@ -904,6 +951,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-cases", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--batched-only", action="store_true", help="only run the batched multi-tree case")
+    ap.add_argument("--batched-classes", action="store_true",
+                    help="only run the batched multi-tree case split by (d, k) class, one plan per class")
     ap.add_argument("--serving-only", action="store_true", help="only run the serving case")
     ap.add_argument("--precision-only", action="store_true",
                     help="only run the precision case (d=16 and d=64, tensor-core vs FP64 paths), no CPU leg")
@@ -939,6 +988,12 @@ def main():
         stream = torch.cuda.Stream()
         dev = torch.device("cuda", 0)
         print(json.dumps({"precision": precision_cases(path_lib(), torch, stream, dev, 0)}), flush=True)
+        return 0
+    if args.batched_classes:
+        import torch
+
+        stream = torch.cuda.Stream()
+        print(json.dumps({"batched_classes": batched_classes(torch, torch.device("cuda", 0), stream)}), flush=True)
         return 0
     if args.batched_only:
         import torch

@@ -166,6 +166,9 @@ __device__ __forceinline__ void ref_query(const QArgs& a, uint64_t qi, RefFrame*
       bool cand;
       if constexpr (FILTER) {
         const float s = filt.sum(rows32 + static_cast<uint64_t>(min(r, end - 1)) * rstride);
+        // s > thr proves the point lies beyond the bound: a chunk of such rows
+        // skips the enclosures
+        if (!__any_sync(FULL_MASK, r < end && !(s > thr))) continue;
         filt.enclose(s, &clo, &chi);
         cand = r < end && !(s > thr) && !(clo > best.bound32);
       } else {

@@ -125,6 +125,10 @@ __device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, WarpStack
         // divergent branch around the row sum
         const uint32_t r = c0 + lane;
         const float s = filt.sum(rows32 + static_cast<uint64_t>(min(r, end - 1)) * rstride);
+        // s > thr2 proves the point lies beyond the near-tie band above the
+        // bound: neither a candidate nor a note.  Most chunks hold only such
+        // rows, and skip the enclosures.
+        if (!__any_sync(FULL_MASK, r < end && !(s > thr2))) continue;
         float clo, chi;
         filt.enclose(s, &clo, &chi);
         const bool cand = r < end && !(s > thr) && !(clo > best.bound32);

@@ -36,6 +36,9 @@
 
 constexpr uint32_t FULL_MASK = 0xffffffffu;
 constexpr int WARP_STACK = 2 * KD_MAX_DEPTH;
+// Candidates in one leaf chunk from which the warp traversal ranks them
+// together (WarpList::offer_all) instead of offering them one at a time.
+constexpr int WARP_BULK_MIN = 4;
 constexpr uint32_t WARP_MAX_D = static_cast<uint32_t>(WARP_MAX_WIDTH);  // widest query (4 dimensions a lane)
 
 template <int D>
@@ -257,6 +260,13 @@ __device__ __forceinline__ void warp_box_lb2_dyn(const float* bl, const float* b
   *lb_r = __fmul_rd(b, LB_SHRINK);
 }
 
+// A warp's scratch for WarpList::offer_all: the merged list, one slot a rank.
+struct WarpSlots {
+  float lo[32], hi[32];
+  uint32_t row[32], id[32];
+  uint8_t chunk[32];
+};
+
 // ---------------------------------------------------------------------------
 // The warp's sorted k best, KS slots per lane (k <= 32 KS): rank r lives in
 // lane r % 32, slot r / 32.  An entry keeps an FP32 enclosure [lo, hi] of its
@@ -471,6 +481,83 @@ struct WarpList {
     refresh();
     if (ev_row != ROW_NONE && !(ev_lo > near_window(bound32))) note(mag_dn32(dbits(exact_of(ev_row, ev_chunk))));
   }
+  // Offer the candidates of one leaf chunk together (one slot a lane, k <=
+  // 32): lane j's (cl, ch, cr, cid, cchunk) where `mine`, `mask` the ballot
+  // of `mine`.  Each candidate is ranked against the entries and the other
+  // candidates on enclosures alone, and the first k of the merged order come
+  // back through `sl`: the list that offering them one at a time would leave,
+  // since that list too is the k first of the entries and the candidates in
+  // exact order.  When two enclosures overlap (an exact value would be
+  // needed) or a candidate may lie outside max_distance, nothing changes and
+  // it returns false: the caller then offers them one at a time.  Dropped
+  // points (the evicted entries, the candidates ranked k or later) are noted
+  // against the bound after the merge.
+  __device__ __forceinline__ bool offer_all(bool mine, float cl, float ch, uint32_t cr, uint32_t cid, bool cchunk,
+                                            uint32_t mask, WarpSlots* sl) {
+    static_assert(KS == 1, "one slot a lane");
+    if (!__all_sync(FULL_MASK, !mine || ch <= cut_lo)) return false;
+    const bool entry = lane < k && row[0] != ROW_NONE;
+    uint32_t e_rank = lane;  // this lane's entry: its rank plus the candidates before it
+    uint32_t c_rank = 0;     // this lane's candidate: the entries and candidates before it
+    bool amb = false;
+    for (uint32_t m = mask; m; m &= m - 1) {  // uniform
+      const int c = __ffs(m) - 1;
+      const float xl = __shfl_sync(FULL_MASK, cl, c), xh = __shfl_sync(FULL_MASK, ch, c);
+      const bool e_first = entry && hi[0] < xl;
+      const bool x_first = entry && xh < lo[0];
+      amb |= entry && !e_first && !x_first;
+      e_rank += x_first ? 1u : 0u;
+      if (mine && c != static_cast<int>(lane)) {
+        const bool y_first = xh < cl;
+        amb |= !y_first && !(ch < xl);
+        c_rank += y_first ? 1u : 0u;
+      }
+      const uint32_t eb = __popc(__ballot_sync(FULL_MASK, e_first));
+      if (c == static_cast<int>(lane)) c_rank += eb;
+    }
+    if (__any_sync(FULL_MASK, amb)) return false;
+    const float inf = __int_as_float(0x7f800000);
+    if (lane < k) {
+      sl->lo[lane] = inf;
+      sl->hi[lane] = inf;
+      sl->row[lane] = ROW_NONE;
+      sl->id[lane] = NO_ID;
+      sl->chunk[lane] = 0;
+    }
+    __syncwarp();
+    if (entry && e_rank < k) {
+      sl->lo[e_rank] = lo[0];
+      sl->hi[e_rank] = hi[0];
+      sl->row[e_rank] = row[0];
+      sl->id[e_rank] = id[0];
+      sl->chunk[e_rank] = chunk[0] ? 1 : 0;
+    }
+    if (mine && c_rank < k) {
+      sl->lo[c_rank] = cl;
+      sl->hi[c_rank] = ch;
+      sl->row[c_rank] = cr;
+      sl->id[c_rank] = cid;
+      sl->chunk[c_rank] = cchunk ? 1 : 0;
+    }
+    __syncwarp();
+    const bool evicted = entry && e_rank >= k;
+    const float ev_lo = lo[0];
+    const uint32_t ev_row = row[0];
+    const bool ev_chunk = chunk[0];
+    if (lane < k) {
+      lo[0] = sl->lo[lane];
+      hi[0] = sl->hi[lane];
+      row[0] = sl->row[lane];
+      id[0] = sl->id[lane];
+      chunk[0] = sl->chunk[lane] != 0;
+    }
+    __syncwarp();  // the slots are free again
+    refresh();
+    const float win = near_window(bound32);
+    if (evicted && !(ev_lo > win)) note(mag_dn32(dbits(exact_of(ev_row, ev_chunk))));
+    if (mine && c_rank >= k && !(cl > win)) note(mag_dn32(dbits(exact_of(cr, cchunk))));
+    return true;
+  }
   // write_results (query.rs:421-429, 483-493): lane j writes rank j (and
   // 32 + j, ...); the entries are in exact order already, their exact values
   // are computed once here.  Returns (to every lane) whether the query is a
@@ -515,4 +602,5 @@ struct WarpStack {
   uint32_t node[WARP_STACK];
   float lb[WARP_STACK];
   DNode nd[WARP_STACK];
+  WarpSlots slots;  // WarpList::offer_all's merge
 };

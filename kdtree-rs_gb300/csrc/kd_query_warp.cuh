@@ -138,8 +138,8 @@ __device__ __forceinline__ void warp_query(const QArgs& a, uint64_t w, WarpStack
         uint32_t mask = __ballot_sync(FULL_MASK, cand);
         if (!mask) continue;
         const uint32_t my_id = cand ? a.indices[r] : NO_ID;
-        // many candidates at once (the first leaves, while the bound is
-        // loose): ranked together when enclosures decide every comparison
+        // several candidates: ranked together when enclosures decide every
+        // comparison
         if constexpr (KS == 1) {
           if (__popc(mask) >= WARP_BULK_MIN &&
               best.offer_all(cand, clo, chi, r, my_id, r < chunk_end, mask, &stack->slots))

@@ -337,7 +337,7 @@ def time_path(lib, tree, dq, k, p, path, reps, torch, stream, survivors=None, wa
 
 
 def plain_scale_cases(lib, torch, stream, dev):
-    """Config 2: N=1M, d=3, leafsize 16, 1M queries; k in {1, 16}, p in {1, 2, inf},
+    """Plain scale: N=1M, d=3, leafsize 16, 1M queries; k in {1, 16}, p in {1, 2, inf},
     uniform and a 64-component Gaussian mixture (sigma 0.01)."""
     from kdtree import KDTree
 
@@ -363,7 +363,7 @@ def plain_scale_cases(lib, torch, stream, dev):
 
 
 def precision_cases(lib, torch, stream, dev, cpu_threads):
-    """Config 3: N=1M, d in {16, 64}, standard normal x per-dimension scale
+    """Precision: N=1M, d in {16, 64}, standard normal x per-dimension scale
     log-uniform in [0.1, 10], 100k queries, k=32, L2.  The tensor-core filter
     path against the plain CUDA-core path (the best-first warp traversal: FP32
     filters, exact FP64 values in the reference's summation order), both on all
@@ -432,7 +432,7 @@ def precision_cases(lib, torch, stream, dev, cpu_threads):
 
 
 def batched_jobs(torch, dev):
-    """The config-4 draw (batched_case): [(d, k, (tree, device queries, k, out_d, out_i))]."""
+    """The batched case's draw (256 trees, batched_case): [(d, k, (tree, device queries, k, out_d, out_i))]."""
     from kdtree import KDTree
 
     rng = np.random.default_rng(400)
@@ -452,7 +452,7 @@ def batched_jobs(torch, dev):
 
 
 def batched_classes(torch, dev, stream, reps=5):
-    """Config 4 split by (d, k) class: each class's jobs as a plan of their own
+    """The batched case split by (d, k) class: each class's jobs as a plan of their own
     (graph mode, after the tuning run), ms per run and the tuner's choice; the
     whole batch for comparison.  Classes overlap one another in the whole
     batch, so their times add up to more than its time."""
@@ -490,7 +490,7 @@ def batched_classes(torch, dev, stream, reps=5):
 
 
 def batched_case(torch, dev, stream, reps=5):
-    """Config 4: 256 trees, N log-uniform in [1e3, 5e5], d in {2, 3, 8}, uniform
+    """Batched: 256 trees, N log-uniform in [1e3, 5e5], d in {2, 3, 8}, uniform
     [0,1)^d points, leafsize 32 (the reference's default); per tree Q queries,
     Q log-uniform in [1, 5e4], k in {1, 4, 32}, L2; one seed (400) for the whole
     draw.  Total queries/s of the batch plan: one CUDA graph holding the sort
@@ -527,7 +527,7 @@ def batched_case(torch, dev, stream, reps=5):
 
 
 def serving_case(torch, duration_s=2.0, n_templates=256):
-    """Config 5: 32 trees, N log-uniform in [1e5, 4e6], d in {3, 8, 16}, each a
+    """Serving: 32 trees, N log-uniform in [1e5, 4e6], d in {3, 8, 16}, each a
     64-component Gaussian mixture (centres uniform in [0,1)^d, sigma 0.01),
     leafsize 32; requests: tree uniform, Q log-uniform in [1, 1e5] queries from
     the tree's mixture, k log-uniform in [1, 64] rounded, L2; seed 500.  Served

@@ -38,8 +38,8 @@ constexpr uint32_t FULL_MASK = 0xffffffffu;
 constexpr int WARP_STACK = 2 * KD_MAX_DEPTH;
 // Candidates in one leaf chunk from which the warp traversal ranks them
 // together (WarpList::offer_all) instead of offering them one at a time
-// (config-4 batch on GB300: 83.7 M q/s from 2, 83.5 from 3, 83.2 from 4,
-// 82.2 from 8).
+// (a batch of 256 trees of widths 2, 3 and 8, k in {1, 4, 32}, on GB300:
+// 83.7 M q/s from 2, 83.5 from 3, 83.2 from 4, 82.2 from 8).
 constexpr int WARP_BULK_MIN = 2;
 constexpr uint32_t WARP_MAX_D = static_cast<uint32_t>(WARP_MAX_WIDTH);  // widest query (4 dimensions a lane)
 

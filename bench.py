@@ -1148,7 +1148,7 @@ def main():
                     "traffic_over_compulsory": (traffic / compulsory_bytes()) if traffic else None,
                     "kernel": "k_query_packet<L2, d=3, K=16>", "kernel_ms": mean_s * 1e3,
                     "traffic_note": "DRAM read+write bytes per launch from ncu on this workload",
-                    "traffic_source": {"file": "profiles/roofline_inputs.json", "commit": prof.get("commit"),
+                    "traffic_source": {"file": "profiles/roofline_inputs.json", "commit": pk.get("commit", prof.get("commit")),
                                        "stale": pk.get("stale")},
                     "l2_hit_rate_pct": pk.get("l2_hit_rate_pct")}
     line = {

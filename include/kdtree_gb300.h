@@ -228,7 +228,10 @@ int kd_batch_run(kd_batch* batch, void* stream);
 /* What the first graph run's autotuner chose (before it: the defaults):
  * the persistent grid in CTAs, whether queries are sorted by landing leaf,
  * and the widths whose jobs with k <= 4 run as packet tasks (bit 0: width 2,
- * bit 1: 3, bit 2: 8) instead of one query a warp.  Any pointer may be NULL. */
+ * bit 1: 3, bit 2: 8) instead of one query a warp.  Any pointer may be NULL.
+ * The environment variable KD_BATCH_PACKET=all (or none), read when a plan is
+ * tuned, fixes the packet-task choice instead of timing it; results do not
+ * depend on it. */
 int kd_batch_choice(const kd_batch* batch, unsigned* blocks, int* sorted, unsigned* packet_widths);
 int kd_batch_run_mode(kd_batch* batch, void* stream, int mode);
 

@@ -674,12 +674,18 @@ int tune(kd_batch* b, cudaStream_t st) {
       if (rep > 0) *t_min = std::min(*t_min, ms);
     }
   };
-  for (uint32_t w = 0; w < 3 && rc == KD_OK; ++w) {
+  // KD_BATCH_PACKET=all (or none) fixes that choice instead of timing it:
+  // every width that has jobs with k <= 4 runs them as packet tasks (or none
+  // does).  Results are the same either way; tests use it to cover both.
+  const char* fix = std::getenv("KD_BATCH_PACKET");
+  const int fixed = !fix ? -1 : (std::strcmp(fix, "all") == 0 ? 1 : (std::strcmp(fix, "none") == 0 ? 0 : -1));
+  for (uint32_t w = 0; w < 3 && rc == KD_OK && fixed != 0; ++w) {
     bool present = false;
     for (const BatchJob& J : b->layout[0].table) present |= J.cls == w && J.a.k <= 4;
     if (!present) continue;
     const uint32_t keep = b->packet_widths;
     if ((rc = apply_layouts(b, keep | (1u << w)))) break;
+    if (fixed == 1) continue;
     float t = 1e30f;
     time_plan(&t);
     if (rc != KD_OK) break;

@@ -365,29 +365,32 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
           }
         }
         KD_PHASE(13);
-        // 2. offer them, all lanes with a pending point together
+        // 2. offer them, all lanes with a pending point together.  The
+        //    filter thresholds follow the bound once the chunk is done: within
+        //    it they may lag (a lagging threshold only lets more rows reach
+        //    the enclosure test against the present bound).
+        const float b_chunk = best.b_hi;
         while (__any_sync(0xffffffffu, pending != 0)) {
           if (pending) {
             const uint32_t r = c0 + __ffs(pending) - 1;
             pending &= pending - 1;
             const float sr = row_sum(r);
             KD_WORK(9, 1);
-            if (!(sr > thr2)) {  // the bound may have tightened meanwhile
+            if (!(sr > thr2)) {
               float clo, chi;
               filt.enclose(sr, &clo, &chi);
               if (!(sr > thr) && !(clo > best.b_hi)) {
                 KD_WORK(10, 1);
-                const float before = best.b_hi;
                 best.offer(clo, chi, r, r < chunk_end);
-                if (best.b_hi != before) {
-                  thr = filt.threshold(best.b_hi);
-                  thr2 = filt.threshold(band_of(best.b_hi));
-                }
               } else {
                 best.note_point(clo, r, r < chunk_end);
               }
             }
           }
+        }
+        if (best.b_hi != b_chunk) {
+          thr = filt.threshold(best.b_hi);
+          thr2 = filt.threshold(band_of(best.b_hi));
         }
         KD_PHASE(14);
       }

@@ -130,15 +130,21 @@ def test_batch_errors():
     assert_bit_exact((jobs[0][3].cpu().numpy(), jobs[0][4].cpu().numpy()), _single(jobs[0]))
 
 
-def test_autotuner_runs_small_k_jobs_as_packet_tasks(oracle):
-    """Jobs of widths 2 and 3 with k <= 4 on large uniform trees: the first
-    graph run's autotuner times them as packet tasks (32 sorted queries a warp)
-    against one query a warp and keeps the packet tasks; every job's results
-    still equal a lone call and the oracle."""
+@pytest.mark.parametrize("fixed", ["all", "none", None])
+def test_small_k_jobs_as_packet_or_warp_tasks(oracle, monkeypatch, fixed):
+    """Jobs of widths 2 and 3 with k <= 4 on large uniform trees run as packet
+    tasks (32 sorted queries a warp: KD_BATCH_PACKET=all), as one query a warp
+    (none), or as the first graph run's autotuner finds faster (unset: only
+    widths with such jobs may be chosen); every job's results equal a lone call
+    and the oracle in all three."""
     import torch
 
     from kdtree import BatchQuery
 
+    if fixed is None:
+        monkeypatch.delenv("KD_BATCH_PACKET", raising=False)
+    else:
+        monkeypatch.setenv("KD_BATCH_PACKET", fixed)
     rng = np.random.default_rng(31)
     specs = [(200_000, 3, 60_000, 1), (150_000, 3, 40_000, 4), (100_000, 2, 50_000, 2), (30_000, 8, 3000, 16),
              (120_000, 3, 20_000, 3)]
@@ -147,7 +153,12 @@ def test_autotuner_runs_small_k_jobs_as_packet_tasks(oracle):
     plan.run(None)
     torch.cuda.synchronize()
     choice = plan.choice()
-    assert 3 in choice["packet_widths"], choice
+    if fixed == "all":
+        assert choice["packet_widths"] == [2, 3], choice  # the 8-wide job has k = 16
+    elif fixed == "none":
+        assert choice["packet_widths"] == [], choice
+    else:
+        assert set(choice["packet_widths"]) <= {2, 3}, choice
     for job, (data, q) in zip(jobs, host):
         got = (job[3].cpu().numpy(), job[4].cpu().numpy())
         assert_bit_exact(got, _single(job))

@@ -350,9 +350,16 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
         float p[D];
         PointFilter<M, D>::load(rows32 + static_cast<uint64_t>(c0 + min(in_group, rows - 1)) * filter_stride<D>(a), p);
         uint32_t pending = 0;
+        uint32_t rem = take_mask;  // the takers not served yet
         for (uint32_t base = 0; base < n_take; base += 32 / gs) {  // uniform
           const uint32_t j = base + group;
-          const uint32_t src = j < n_take ? __fns(take_mask, 0, static_cast<int>(j) + 1) : 0;
+          // this group's taker: the group-th lowest of rem (group < 4)
+          uint32_t m = rem;
+          if (group >= 1) m &= m - 1;
+          if (group >= 2) m &= m - 1;
+          if (group >= 3) m &= m - 1;
+          const uint32_t src = m ? static_cast<uint32_t>(__ffs(m) - 1) : 0u;
+          for (uint32_t i = 0; i < 32 / gs; ++i) rem &= rem - 1;  // uniform
           float q[D];
 #pragma unroll
           for (int i = 0; i < D; ++i) q[i] = __shfl_sync(0xffffffffu, filt.q32[i], static_cast<int>(src));

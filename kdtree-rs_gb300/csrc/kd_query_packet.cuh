@@ -375,7 +375,9 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
         // 2. offer them, all lanes with a pending point together.  The
         //    filter thresholds follow the bound once the chunk is done: within
         //    it they may lag (a lagging threshold only lets more rows reach
-        //    the enclosure test against the present bound).
+        //    the enclosure test against the present bound).  A pending row's
+        //    sum is the one pass 1 compared with this lane's thr2 (the same
+        //    operations on the same FP32 values), so it passes thr2 again.
         const float b_chunk = best.b_hi;
         while (__any_sync(0xffffffffu, pending != 0)) {
           if (pending) {
@@ -383,15 +385,13 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
             pending &= pending - 1;
             const float sr = row_sum(r);
             KD_WORK(9, 1);
-            if (!(sr > thr2)) {
-              float clo, chi;
-              filt.enclose(sr, &clo, &chi);
-              if (!(sr > thr) && !(clo > best.b_hi)) {
-                KD_WORK(10, 1);
-                best.offer(clo, chi, r, r < chunk_end);
-              } else {
-                best.note_point(clo, r, r < chunk_end);
-              }
+            float clo, chi;
+            filt.enclose(sr, &clo, &chi);
+            if (!(sr > thr) && !(clo > best.b_hi)) {
+              KD_WORK(10, 1);
+              best.offer(clo, chi, r, r < chunk_end);
+            } else {
+              best.note_point(clo, r, r < chunk_end);
             }
           }
         }

@@ -115,7 +115,11 @@ int kd_query_async(const kd_tree* tree, const double* d_queries, uint64_t n_valu
 /* Query kernels kd_query_device_path can be asked for.  No reference
  * counterpart: the reference has one CPU descent; these are the engine's
  * implementations of it, for measurement and cross-checking.
- *   KD_PATH_AUTO            what kd_query / kd_query_device run
+ *   KD_PATH_AUTO            what kd_query / kd_query_device run: a rule per
+ *                           width, k and batch size, timed on the tree where
+ *                           the packet and warp traversals are close (widths 2
+ *                           and 3, 32,768 to 524,287 queries: the first such
+ *                           call of a class runs both and keeps the faster)
  *   KD_PATH_REFERENCE_ORDER the reference's depth-first order with its FP64
  *                           gate decisions (the only order for eps > 0 and
  *                           general p): one warp per query, leaf rows split

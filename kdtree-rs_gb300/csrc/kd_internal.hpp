@@ -50,6 +50,12 @@ struct kd_tree {
   // traversal, 1 tensor-core filter.
   std::mutex choice_mutex;
   int auto_choice[2] = {-1, -1};
+  // Widths 2 and 3, eps = 0, batches of TRAVERSAL_TIMED_MIN up to
+  // TRAVERSAL_TIMED_MAX queries: which traversal the automatic choice
+  // measured faster on this tree, per class (bit 1: k > 16, bit 0: at least
+  // TRAVERSAL_TIMED_SPLIT queries); -1 not yet measured, 0 one warp a query,
+  // 1 packet traversal.
+  int auto_traversal[4] = {-1, -1, -1, -1};
 };
 
 namespace kd {

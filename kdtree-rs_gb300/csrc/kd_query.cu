@@ -689,6 +689,52 @@ QArgs query_args(const kd_tree* t, const double* d_queries, uint64_t nq, const Q
 
 namespace {
 
+// Where neither traversal is clearly ahead (widths 2 and 3, eps = 0, batches
+// of 32,768 up to 524,287 queries), the first automatic call of each class
+// on a tree runs both on its whole batch and the tree keeps the faster for
+// later calls of that class; stream-ordered calls time nothing and take the
+// rule of warp_preferred.
+constexpr uint64_t TRAVERSAL_TIMED_MIN = 32768, TRAVERSAL_TIMED_MAX = 524288, TRAVERSAL_TIMED_SPLIT = 131072;
+
+bool traversal_timed(const kd_tree* t, uint64_t nq, const QueryParams& qp) {
+  const bool use_eps = qp.eps_factor != 1.0;
+  return !qp.no_sync && !force_reference_order() && (t->ndim == 2 || t->ndim == 3) && nq >= TRAVERSAL_TIMED_MIN &&
+         nq < TRAVERSAL_TIMED_MAX && warp_applicable(t->ndim, qp.metric, qp.k, t->n_points, use_eps) &&
+         packet_applicable(t->ndim, qp.metric, qp.k, t->n_points, use_eps);
+}
+
+// Run the query with the warp traversal, then with the packet traversal (the
+// same results), timing each with events; *choice = 1 when the packet
+// traversal was faster.  The first run counts no near-tie reruns, so the
+// counters count one run.
+int time_traversals(QArgs a, int metric, cudaStream_t st, int* choice) {
+  cudaEvent_t e[3];
+  for (int i = 0; i < 3; ++i) {
+    if (cudaEventCreate(&e[i]) != cudaSuccess) {
+      for (int j = 0; j < i; ++j) cudaEventDestroy(e[j]);
+      return cuda_fail(cudaErrorMemoryAllocation, "cudaEventCreate");
+    }
+  }
+  unsigned long long* total = a.rerun_total;
+  a.rerun_total = nullptr;
+  int rc = cudaEventRecord(e[0], st) == cudaSuccess ? KD_OK : cuda_fail(cudaErrorUnknown, "cudaEventRecord");
+  if (!rc) rc = run_kernels(a, metric, st, PATH_WARP);
+  if (!rc) cudaEventRecord(e[1], st);
+  a.rerun_total = total;
+  if (!rc) rc = run_kernels(a, metric, st, PATH_PACKET);
+  if (!rc) cudaEventRecord(e[2], st);
+  float ms_warp = 0.f, ms_packet = 0.f;
+  if (!rc) {
+    const cudaError_t err = cudaEventSynchronize(e[2]);
+    if (err != cudaSuccess) rc = cuda_fail(err, "cudaEventSynchronize");
+    cudaEventElapsedTime(&ms_warp, e[0], e[1]);
+    cudaEventElapsedTime(&ms_packet, e[1], e[2]);
+  }
+  for (cudaEvent_t x : e) cudaEventDestroy(x);
+  if (!rc) *choice = ms_packet < ms_warp ? 1 : 0;
+  return rc;
+}
+
 // Whether the call can reach the one-thread reference-order kernels with a
 // runtime width, which keep each query's CellBound axes in global scratch.
 bool uses_axes_scratch(const kd_tree* t, const QueryParams& qp) {
@@ -751,7 +797,20 @@ int query_on_device(const kd_tree* t, const double* d_queries, uint64_t nq, cons
       sort_mem = nullptr;
     }
   }
-  const int rc = run_kernels(a, qp.metric, st, qp.path);
+  int rc = KD_OK;
+  int path = qp.path;
+  if (path == PATH_AUTO && traversal_timed(t, nq, qp)) {
+    kd_tree* mt = const_cast<kd_tree*>(t);  // the choice is a cache on the tree
+    std::lock_guard<std::mutex> lock(mt->choice_mutex);
+    int& choice = mt->auto_traversal[(qp.k > 16 ? 2 : 0) + (nq >= TRAVERSAL_TIMED_SPLIT ? 1 : 0)];
+    if (choice < 0) {
+      rc = time_traversals(a, qp.metric, st, &choice);  // both write the same results
+      path = -1;
+    } else {
+      path = choice == 1 ? PATH_PACKET : PATH_WARP;
+    }
+  }
+  if (path >= 0) rc = run_kernels(a, qp.metric, st, path);
   if (axes) cudaFreeAsync(axes, st);
   cudaFreeAsync(rerun, st);
   if (sort_mem) cudaFreeAsync(sort_mem, st);

@@ -34,9 +34,12 @@ constexpr int PACKET_STACK = 2 * KD_MAX_DEPTH;
 //   clock64 at the phase boundaries, the warp synchronised there): 11 setup
 //   and seed leaf, 12 node steps, 13 leaf filter rounds, 14 offers, 15 sort
 //   and write.
+// Each thread adds into its own 32-bit counters (registers) and flushes them
+// with one atomic each when its queries are done, so the counting does not
+// contend on the global counters inside the phases it times.
 #ifdef KD_WORK_COUNTS
 __device__ unsigned long long g_work[16];
-#define KD_WORK(i, v) atomicAdd(&g_work[i], static_cast<unsigned long long>(v))
+#define KD_WORK(i, v) (kd_acc_[i] += static_cast<uint32_t>(v))
 #define KD_PHASE(i)                                          \
   do {                                                       \
     __syncwarp();                                            \
@@ -44,9 +47,15 @@ __device__ unsigned long long g_work[16];
     if ((threadIdx.x & 31) == 0) KD_WORK(i, kd_now_ - kd_t_); \
     kd_t_ = kd_now_;                                         \
   } while (0)
+#define KD_WORK_FLUSH()                                                                    \
+  do {                                                                                     \
+    _Pragma("unroll") for (int kd_i_ = 0; kd_i_ < 16; ++kd_i_) if (kd_acc_[kd_i_])         \
+        atomicAdd(&g_work[kd_i_], static_cast<unsigned long long>(kd_acc_[kd_i_]));         \
+  } while (0)
 #else
 #define KD_WORK(i, v) ((void)0)
 #define KD_PHASE(i) ((void)0)
+#define KD_WORK_FLUSH() ((void)0)
 #endif
 
 // Cheap rigorous point filter.  With a = p32 - q32 (exact reals) and every
@@ -195,6 +204,7 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
                                                uint32_t* s_row, uint32_t* stack) {
   static_assert(D > 0 && M != M_LP, "packet path: compile-time width, metric without pow()");
 #ifdef KD_WORK_COUNTS
+  uint32_t kd_acc_[16] = {};
   long long kd_t_ = clock64();
 #endif
   const bool in_range = tid < a.nq;
@@ -425,6 +435,7 @@ __device__ __forceinline__ void packet_queries(const QArgs& a, uint64_t tid, flo
     if (live && best.write(a.out_d + qi * a.k, a.out_i + qi * a.k, a.k, a.n_points)) flag_rerun(a, qi);
   }
   KD_PHASE(15);
+  KD_WORK_FLUSH();
 }
 
 template <int M, int D, int K>

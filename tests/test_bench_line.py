@@ -27,7 +27,7 @@ def test_profiled_inputs_carry_their_commit_and_staleness():
     assert 0 < j["build"]["l2_hit_rate_pct_time_weighted"] <= 100
     # the summary of the same capture states the same traffic
     text = (ROOT / "profiles" / "k_query_packet_uniform_n1m_d3_k16.md").read_text()
-    assert "127.2 MB / 216.2 MB" in text
+    assert "126.4 MB / 216.0 MB" in text
 
 
 def test_measured_peak_is_positive():
